@@ -1,0 +1,325 @@
+"""Throughput of one RK3 step of the cbns3d right-hand side on GB300.
+
+Metric: cell-RK3-steps/s (interior cells x full 3-stage RK3 steps per second).
+Workload: Taylor-Green vortex 256^3, binary64, Re 1600, Ma 0.1, CFL 0.5, the
+reference's initial condition and mesh (synthetic analytic data; no dataset).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+ours:       W untimed steps, then K steps timed with CUDA events on the solve's
+            stream (the replayed step graph; state resident in HBM, 1.5 GB of
+            state per step >> the 129 MB L2).  Then, inside the same run:
+              * per-kernel timing of K more steps (events around every launch),
+                giving the dominant kernel's roofline against the FP64 FMA peak
+                measured live by cbns_probe_peak;
+              * e2e: K steps through the C ABI with host buffers: upload Q from
+                pinned memory, one step, download Q, every step;
+              * cpu_baseline: the oracle's CPU restatement of the reference (all
+                host threads) on a bounded sample of the same workload.
+reference:  the reference algorithm on the host cores (the oracle's restatement,
+            bitwise equal to the reference compiled unmodified), W + K steps.
+Multi-GPU: replicas only (independent solves, one per rank, no collective on the
+data path); the JSON value is the aggregate over ranks, time = max over ranks.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "cell-RK3-steps/s TGV 256^3 FP64"
+UNIT = "cell-RK3-steps/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--N", type=int, default=256)
+    ap.add_argument("--cpu-steps", type=int, default=1, help="steps of the CPU-baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def reduce_max(value, world):
+    """Max of a float over ranks (identity at world size 1)."""
+    if world == 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    dev = torch.device("cuda", torch.cuda.current_device()) if dist.get_backend() == "nccl" else torch.device("cpu")
+    t = torch.tensor([value], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle sampling during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.QUERY,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def cpu_sample(N, steps):
+    """The oracle's CPU restatement of the reference on `steps` steps of the N^3
+    workload, all host threads; returns (cell-steps/s, threads, seconds)."""
+    from cbns3d_cart_mpi_gb300._abi import tgv_params
+    from oracle.build import build_port
+    from oracle.oracle import OracleBlock, num_threads
+    build_port()
+    b = OracleBlock(tgv_params(N, t_end=2.0))
+    b.initial_condition()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        b.step()
+    sec = time.perf_counter() - t0
+    th = num_threads()
+    b.close()
+    return N ** 3 * steps / sec, th, sec
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    from oracle.build import build_port
+    from oracle.oracle import OracleBlock, num_threads
+    from cbns3d_cart_mpi_gb300._abi import tgv_params
+    build_port()
+    N = args.N
+    b = OracleBlock(tgv_params(N, t_end=2.0))
+    b.initial_condition()
+    for _ in range(args.warmup):
+        b.step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        b.step()
+    sec = time.perf_counter() - t0
+    value = N ** 3 * args.steps / sec
+    th = num_threads()
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sec / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "taylor-green vortex %d^3 FP64, Re 1600, Ma 0.1, CFL 0.5" % N, "grid": [N, N, N],
+                   "parallelism": "host threads (OpenMP over k-planes)"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": th, "kind": "port",
+                         "sample": "%d warm-up + %d timed full RK3 steps of the %d^3 workload" % (
+                             args.warmup, args.steps, N)},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "gpu_launches": 0,
+        "note": "oracle/cbns_oracle.c: the reference's arithmetic restated in C, bitwise equal to the reference "
+                "compiled unmodified (tests/test_oracle_golden.py); the reference binary itself is built only "
+                "where its sources are present, and the box has no MPI",
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, rank, world, local):
+    import numpy as np
+    import torch
+
+    from cbns3d_cart_mpi_gb300 import build as pkg_build
+    from cbns3d_cart_mpi_gb300._abi import NEQ, NG, tgv_params
+    from cbns3d_cart_mpi_gb300.solver import Solver, initial_condition, probe_peak
+    from cbns3d_cart_mpi_gb300.workload import kernel_flops, state_bytes_per_step
+
+    pkg_build.build()
+    os.environ["CBNS_DEVICE"] = str(local)
+    torch.cuda.set_device(local)
+    N = args.N
+    p = tgv_params(N, t_end=2.0)
+    Q0 = initial_condition(p)
+    s = Solver(p)
+    s.upload_Q(Q0, 0.0)
+    stream = torch.cuda.ExternalStream(s.stream)
+
+    # Warm-up (also builds the step graph).
+    s.run(args.warmup)
+    torch.cuda.synchronize()
+
+    sampler = ClockSampler(local)
+    sampler.start()
+    barrier(world)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    done = s.run(args.steps)
+    e1.record(stream)
+    e1.synchronize()
+    torch.cuda.synchronize()
+    barrier(world)
+    clocks = sampler.stop()
+    ms = e0.elapsed_time(e1)
+    ms = reduce_max(ms, world)
+    assert done == args.steps, "solve finished early (%d of %d steps)" % (done, args.steps)
+    cells = N ** 3
+    value = world * cells * args.steps / (ms * 1e-3)
+    launches_per_step = 2 + 3 * 5
+
+    line = None
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "taylor-green vortex %d^3 FP64, Re 1600, Ma 0.1, CFL 0.5 (one solve per GPU)" % N,
+                       "grid": [N, N, N], "precision": "fp64",
+                       "parallelism": "replicas" if world > 1 else "single GPU",
+                       "l2": "state 2x%.0f MB per step, larger than the 129 MB L2; no flush" % (
+                           NEQ * (N + 2 * NG) ** 3 * 8 / 1e6)},
+            "clocks": clocks,
+            "gpu_launches": launches_per_step * args.steps,
+        }
+
+    # Per-kernel timing over K more steps: roofline of the dominant kernel.
+    s.profile_begin()
+    s.run(args.steps)
+    prof = s.profile_end()
+    if rank == 0:
+        tot = sum(v[1] for v in prof.values())
+        kernels = {k: {"launches": v[0], "ms_per_launch": v[1] / v[0], "share": v[1] / tot} for k, v in prof.items()}
+        dom = max(prof, key=lambda k: prof[k][1])
+        per_launch_ms = prof[dom][1] / prof[dom][0]
+        flops = kernel_flops(dom, N, N, N)
+        achieved = flops / (per_launch_ms * 1e-3) * 1e-12
+        peak = probe_peak(fp64=True)
+        traffic = None
+        tpath = os.path.join(ROOT, "profiles", "traffic.json")
+        if os.path.exists(tpath):
+            with open(tpath) as f:
+                traffic = json.load(f).get(dom)
+        line["roofline"] = {
+            "bound": "fp64-pipe", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+            "frac": achieved / peak, "traffic": traffic,
+            "peak_source": "binary64 FMA throughput measured live on this GPU (cbns_probe_peak); "
+                           "MEASURED_PEAKS.json holds no FP64 figure",
+            "algorithmic_flops_per_launch": flops,
+            "flop_count": "reference's own op count per face/cell (tests/golden/opcount.txt)",
+        }
+        step_ms = ms / args.steps
+        line["kernels"] = kernels
+        line["step_roofline"] = {
+            "algorithmic_tflops": 15198.25 * cells / (step_ms * 1e-3) * 1e-12,
+            "hbm_gbs_min_state": state_bytes_per_step(N, N, N) / (step_ms * 1e-3) * 1e-9,
+        }
+
+    # e2e: host buffers through the C ABI, copies inside the timed region.
+    if not args.no_e2e:
+        n = int(np.prod(s.shape))
+        hin = torch.empty(n, dtype=torch.float64, pin_memory=True).numpy()
+        hout = torch.empty(n, dtype=torch.float64, pin_memory=True).numpy()
+        hin[:] = Q0.reshape(-1)
+        s.upload_Q(hin, 0.0)
+        s.step()
+        s.download_Q(out=hout.reshape(s.shape))
+        barrier(world)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            s.upload_Q(hin, 0.0)
+            s.step()
+            s.download_Q(out=hout.reshape(s.shape))
+        sec = reduce_max(time.perf_counter() - t0, world)
+        if rank == 0:
+            line["e2e"] = {"value": world * cells * args.steps / sec, "unit": UNIT,
+                           "h2d_bytes_per_step": n * 8, "d2h_bytes_per_step": n * 8,
+                           "path": "cbns_upload_Q (pinned) + cbns_step + cbns_download_Q (pinned), per step"}
+    s.close()
+
+    if rank == 0 and not args.no_cpu_baseline:
+        v, th, sec = cpu_sample(N, args.cpu_steps)
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": th, "kind": "port",
+                                "sample": "%d full RK3 step(s) of the %d^3 workload, %.1f s" % (args.cpu_steps, N, sec)}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        if world > 1:
+            # The CPU reference runs once on rank 0; other ranks exit without work.
+            run_reference(args, rank, world)
+            return
+        run_reference(args, rank, world)
+        return
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    run_ours(args, rank, world, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

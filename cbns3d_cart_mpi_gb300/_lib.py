@@ -1,0 +1,95 @@
+"""ctypes bindings of the two native libraries (include/cbns_gpu.h, include/cbns_host.h).
+
+The GPU library is the only compute path: if it is not built, loading fails
+with an error that says so; nothing falls back to a CPU implementation.
+"""
+import ctypes
+import os
+
+from ._abi import CbnsParams
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_DIR = os.path.join(PKG, "lib")
+GPU_LIB = os.path.join(LIB_DIR, "libcbns_gpu.so")
+HOST_LIB = os.path.join(LIB_DIR, "libcbns_host.so")
+
+_gpu = None
+
+
+class KernelTime(ctypes.Structure):
+    _fields_ = [("name", ctypes.c_char * 32), ("launches", ctypes.c_uint32), ("total_ms", ctypes.c_double)]
+_host = None
+
+c_int, c_u32, c_u64, c_d, c_vp = ctypes.c_int, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_double, ctypes.c_void_p
+c_dp = ctypes.POINTER(ctypes.c_double)
+P_params = ctypes.POINTER(CbnsParams)
+
+# name -> (restype, argtypes); every entry point include/cbns_gpu.h declares.
+GPU_API = {
+    "cbns_params_derive": (c_int, [P_params]),
+    "cbns_create": (c_int, [P_params, c_u32, c_u32, c_u32, c_int, ctypes.POINTER(c_vp)]),
+    "cbns_destroy": (c_int, [c_vp]),
+    "cbns_upload_Q": (c_int, [c_vp, c_vp, c_d]),
+    "cbns_download_Q": (c_int, [c_vp, c_vp]),
+    "cbns_download_Q_p": (c_int, [c_vp, c_vp]),
+    "cbns_download_prims": (c_int, [c_vp] + [c_vp] * 6),
+    "cbns_calc_dt": (c_int, [c_vp, c_dp]),
+    "cbns_stage": (c_int, [c_vp, c_d, c_int]),
+    "cbns_step": (c_int, [c_vp, c_d, c_dp, c_dp]),
+    "cbns_run": (c_int, [c_vp, c_u32, c_d, ctypes.POINTER(c_u32)]),
+    "cbns_get_time": (c_int, [c_vp, c_dp, c_dp]),
+    "cbns_diagnostics": (c_int, [c_vp, c_dp, c_dp]),
+    "cbns_check_state": (c_int, [c_vp]),
+    "cbns_stream": (c_vp, [c_vp]),
+    "cbns_get_info": (c_int, [c_vp, ctypes.POINTER(c_u32), ctypes.POINTER(c_u64), ctypes.POINTER(c_int)]),
+    "cbns_profile_begin": (c_int, [c_vp]),
+    "cbns_profile_end": (c_int, [c_vp, c_vp, c_int, ctypes.POINTER(c_int)]),
+    "cbns_probe_peak": (c_int, [c_int, c_dp]),
+    "cbns_last_error": (ctypes.c_char_p, []),
+    "cbns_version": (ctypes.c_char_p, []),
+}
+
+HOST_API = {
+    "cbns_host_read_input": (c_int, [ctypes.c_char_p, P_params]),
+    "cbns_host_gen_mesh": (c_int, [P_params, c_u32, c_u32, c_u32, c_u32, c_u32, c_u32, c_vp, c_vp, c_vp]),
+    "cbns_host_initial_condition": (c_int, [P_params, c_u32, c_u32, c_u32, c_u32, c_u32, c_u32, c_vp]),
+    "cbns_host_initial_condition_perturbed": (c_int, [P_params, c_u32, c_u32, c_u32, c_u64, c_d, c_int, c_int,
+                                                      c_vp]),
+    "cbns_host_output_bin": (c_int, [ctypes.c_char_p, c_d, c_u32, c_u32, c_u32, c_vp]),
+    "cbns_host_read_bin": (c_int, [ctypes.c_char_p, c_u32, c_u32, c_u32, c_vp, c_dp]),
+    "cbns_host_output_vtk_xml": (c_int, [ctypes.c_char_p, ctypes.c_char_p, c_int, c_u32, c_u32, c_u32, c_u32]
+                                 + [c_vp] * 8),
+}
+
+
+def _bind(lib, table):
+    for name, (res, args) in table.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    return lib
+
+
+def gpu():
+    """The GPU library; raises if it has not been built (no fallback exists)."""
+    global _gpu
+    if _gpu is None:
+        if not os.path.exists(GPU_LIB):
+            raise RuntimeError("libcbns_gpu.so is not built (%s); run cbns3d_cart_mpi_gb300.build.build() "
+                               "or __graft_entry__.build()" % GPU_LIB)
+        _gpu = _bind(ctypes.CDLL(GPU_LIB), GPU_API)
+    return _gpu
+
+
+def host():
+    global _host
+    if _host is None:
+        if not os.path.exists(HOST_LIB):
+            raise RuntimeError("libcbns_host.so is not built (%s); run cbns3d_cart_mpi_gb300.build.build()"
+                               % HOST_LIB)
+        _host = _bind(ctypes.CDLL(HOST_LIB), HOST_API)
+    return _host
+
+
+def last_error():
+    return gpu().cbns_last_error().decode(errors="replace")

@@ -1,0 +1,117 @@
+"""Build the native parts in-tree, with nvcc and g++ only (no CMake).
+
+  lib/libcbns_gpu.so   CUDA kernels + C ABI of include/cbns_gpu.h (sm_103a only)
+  lib/libcbns_host.so  host C++ of include/cbns_host.h (input.txt, IC, checkpoint, VTK)
+  lib/cbns3d_gb300     the Block3d-style driver executable
+
+Translation units compile in parallel and are skipped when up to date, so a
+rebuild on the GPU machine takes about a minute from scratch.
+"""
+import os
+import shutil
+import subprocess
+from concurrent.futures import ThreadPoolExecutor
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(PKG)
+CSRC = os.path.join(PKG, "csrc")
+LIB = os.path.join(PKG, "lib")
+INCLUDE = os.path.join(ROOT, "include")
+
+GPU_SOURCES = ["cbns_kernels.cu", "cbns_api.cu", "cbns_probe.cu"]
+HOST_SOURCES = ["host/cbns_host.cpp"]
+DRIVER_SOURCE = "host/cbns3d_gb300.cpp"
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
+
+GPU_LIB = os.path.join(LIB, "libcbns_gpu.so")
+HOST_LIB = os.path.join(LIB, "libcbns_host.so")
+DRIVER = os.path.join(LIB, "cbns3d_gb300")
+
+
+def _cuda_home():
+    for c in (os.environ.get("CUDA_HOME"), "/usr/local/cuda"):
+        if c and os.path.isdir(c):
+            return c
+    nvcc = shutil.which("nvcc")
+    return os.path.dirname(os.path.dirname(nvcc)) if nvcc else "/usr/local/cuda"
+
+
+def _nvcc():
+    return shutil.which("nvcc") or os.path.join(_cuda_home(), "bin", "nvcc")
+
+
+def _run(cmd):
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("build step failed:\n  %s\n%s%s" % (" ".join(cmd), r.stdout, r.stderr))
+    return r
+
+
+def _headers():
+    hs = [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE) if f.endswith(".h")]
+    hs += [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
+    return hs
+
+
+def _stale(target, deps):
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(d) > t for d in deps if os.path.exists(d))
+
+
+def _atomic(cmd_fn, target):
+    tmp = target + ".tmp%d" % os.getpid()
+    _run(cmd_fn(tmp))
+    os.replace(tmp, target)
+
+
+def build(verbose=False, extra_nvcc=()):
+    """Compile everything that is out of date; returns the paths built."""
+    os.makedirs(LIB, exist_ok=True)
+    objdir = os.path.join(LIB, "obj")
+    os.makedirs(objdir, exist_ok=True)
+    hdrs = _headers()
+    nvcc = _nvcc()
+    extra = list(extra_nvcc)
+
+    def cu_obj(src):
+        path = os.path.join(CSRC, src)
+        obj = os.path.join(objdir, os.path.basename(src) + ".o")
+        if _stale(obj, [path] + hdrs + [__file__]):
+            _atomic(lambda out: [nvcc] + ARCH + NVCC_FLAGS + extra + ["-c", path, "-o", out], obj)
+        return obj
+
+    def cpp_obj(src):
+        path = os.path.join(CSRC, src)
+        obj = os.path.join(objdir, os.path.basename(src) + ".o")
+        if _stale(obj, [path] + hdrs + [__file__]):
+            _atomic(lambda out: ["g++", "-O2", "-std=c++17", "-fPIC", "-Wall", "-c", path, "-o", out], obj)
+        return obj
+
+    with ThreadPoolExecutor(max_workers=max(2, os.cpu_count() or 2)) as ex:
+        gpu_f = [ex.submit(cu_obj, s) for s in GPU_SOURCES]
+        host_f = [ex.submit(cpp_obj, s) for s in HOST_SOURCES]
+        drv_f = ex.submit(cpp_obj, DRIVER_SOURCE)
+        gpu_objs = [f.result() for f in gpu_f]
+        host_objs = [f.result() for f in host_f]
+        drv_obj = drv_f.result()
+
+    cudalib = os.path.join(_cuda_home(), "lib64")
+    if _stale(GPU_LIB, gpu_objs):
+        _atomic(lambda out: [nvcc] + ARCH + ["-shared", "-o", out] + gpu_objs + ["-lcudart"], GPU_LIB)
+    if _stale(HOST_LIB, host_objs):
+        _atomic(lambda out: ["g++", "-shared", "-o", out] + host_objs, HOST_LIB)
+    if _stale(DRIVER, [drv_obj, GPU_LIB, HOST_LIB]):
+        _atomic(lambda out: ["g++", "-o", out, drv_obj, "-L" + LIB, "-lcbns_gpu", "-lcbns_host",
+                             "-L" + cudalib, "-lcudart", "-Wl,-rpath,$ORIGIN", "-Wl,-rpath," + cudalib],
+                DRIVER)
+    if verbose:
+        for p in (GPU_LIB, HOST_LIB, DRIVER):
+            print(p)
+    return GPU_LIB, HOST_LIB, DRIVER
+
+
+if __name__ == "__main__":
+    build(verbose=True)

@@ -1,0 +1,530 @@
+// cbns_api.cu — the C ABI of include/cbns_gpu.h over the kernels of cbns_kernels.cu.
+//
+// A handle owns one solve: a single device arena holding the padded state, the
+// primitives, the face and viscous fluxes, the control block and the tile
+// tables, plus a CUDA stream.  The host never sees device pointers.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/cbns_gpu.h"
+#include "cbns_device.cuh"
+#include "cbns_prof.h"
+
+namespace cbns {
+cudaError_t launch_prepare(const SolveDev* d, const TileRef* tiles, int ntiles, cudaStream_t st, Profiler* pf);
+cudaError_t launch_layout(const SolveDev* d, int sidx, const double* src, double* dst, bool to_soa,
+                          long long V, cudaStream_t st, Profiler* pf);
+cudaError_t launch_dt(const SolveDev* d, int nsolves, const TileRef* tiles, int ntiles, double t_end,
+                      bool use_t_end, cudaStream_t st, Profiler* pf);
+cudaError_t launch_dt_raw(const SolveDev* d, int sidx, const TileRef* tiles, int ntiles, double* out,
+                          cudaStream_t st, Profiler* pf);
+cudaError_t launch_set_dt(const SolveDev* d, int sidx, double dt, cudaStream_t st);
+cudaError_t launch_stage(const SolveDev* d, const TileRef* tiles, int ntiles, const TileRef* ring_tiles,
+                         int nring, int stage, int max_ctas, cudaStream_t st, Profiler* pf);
+cudaError_t launch_diag(const SolveDev* d, int sidx, const TileRef* tiles, int ntiles, double* partials,
+                        int nparts, double inv_n, double* out, cudaStream_t st, Profiler* pf);
+}  // namespace cbns
+
+using namespace cbns;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+cbns_status fail(cbns_status st, const std::string& msg) {
+  g_last_error = msg;
+  return st;
+}
+
+cbns_status cuda_fail(cudaError_t e, const char* what) {
+  g_last_error = std::string(what) + ": " + cudaGetErrorString(e);
+  if (e == cudaErrorMemoryAllocation) return CBNS_ERR_OUT_OF_MEMORY;
+  return CBNS_ERR_CUDA;
+}
+
+#define CBNS_CUDA(call)                                   \
+  do {                                                    \
+    cudaError_t e_ = (call);                              \
+    if (e_ != cudaSuccess) return cuda_fail(e_, #call);   \
+  } while (0)
+
+// Tiles of TILE_X x TILE_Y x 1 cells over a box of extents ex, ey, ez.
+void append_tiles(std::vector<TileRef>& out, int solve, int ex, int ey, int ez) {
+  const int tx = (ex + TILE_X - 1) / TILE_X, ty = (ey + TILE_Y - 1) / TILE_Y;
+  for (int k = 0; k < ez; ++k)
+    for (int j = 0; j < ty; ++j)
+      for (int i = 0; i < tx; ++i)
+        out.push_back(TileRef{(uint16_t)solve, (uint16_t)i, (uint16_t)j, (uint16_t)k});
+}
+
+size_t align_up(size_t x) { return (x + 255) & ~size_t(255); }
+
+}  // namespace
+
+struct cbns_handle {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int precision = CBNS_FP64;
+  cbns_params params{};
+  uint32_t IM = 0, JM = 0, KM = 0;
+  char* arena = nullptr;
+  size_t arena_bytes = 0;
+  SolveDev desc{};
+  SolveDev* d_desc = nullptr;
+  SolveCtl* d_ctl = nullptr;
+  TileRef* d_tiles_int = nullptr;
+  TileRef* d_tiles_ring = nullptr;
+  TileRef* d_tiles_pad = nullptr;
+  int n_int = 0, n_ring = 0, n_pad = 0;
+  double* d_stage = nullptr;
+  double* d_partials = nullptr;
+  int nparts = 0;
+  double* d_out = nullptr;  // small device results (diagnostics, raw dt)
+  SolveCtl* h_ctl = nullptr;  // pinned
+  double* h_out = nullptr;    // pinned
+  cudaGraphExec_t step_graph = nullptr;
+  double graph_t_end = 0.0;
+  Profiler prof;
+  Profiler* pf() { return prof.on ? &prof : nullptr; }
+};
+
+extern "C" {
+
+const char* cbns_last_error(void) { return g_last_error.c_str(); }
+const char* cbns_version(void) { return "cbns3d-gb300 0.1.0 (sm_103a)"; }
+
+cbns_status cbns_params_derive(cbns_params* p) {
+  if (!p) return fail(CBNS_ERR_INVALID_ARG, "cbns_params_derive: null params");
+  // src/read_input.cpp:78-90
+  p->Mach2 = p->Mach * p->Mach;
+  p->Re_inv = 1.0 / p->Re;
+  p->Pr_inv = 1.0 / p->Pr;
+  p->gam1 = p->gamma - 1.0;
+  p->gM2 = p->gamma * p->Mach2;
+  p->gam1_inv = 1.0 / p->gam1;
+  p->p_inf = 1.0 / p->gM2;
+  p->C_T_inf = 110.5 / p->T_inf;
+  double a = 4.0 / 3.0, g = p->gamma * p->Pr_inv;
+  p->C_dt_v = (a < g ? g : a) * p->Re_inv;
+  return CBNS_OK;
+}
+
+cbns_status cbns_destroy(cbns_handle* h) {
+  if (!h) return CBNS_OK;
+  cudaSetDevice(h->device);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  if (h->step_graph) cudaGraphExecDestroy(h->step_graph);
+  if (h->arena) cudaFree(h->arena);
+  if (h->h_ctl) cudaFreeHost(h->h_ctl);
+  if (h->h_out) cudaFreeHost(h->h_out);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+  return CBNS_OK;
+}
+
+cbns_status cbns_create(const cbns_params* p, uint32_t IM, uint32_t JM, uint32_t KM, int precision,
+                        cbns_handle** out) {
+  if (!p || !out) return fail(CBNS_ERR_INVALID_ARG, "cbns_create: null argument");
+  *out = nullptr;
+  if (precision != CBNS_FP64 && precision != CBNS_FP32_MIXED)
+    return fail(CBNS_ERR_INVALID_ARG, "cbns_create: unknown precision");
+  if (precision == CBNS_FP32_MIXED)
+    return fail(CBNS_ERR_INVALID_ARG, "cbns_create: FP32-mixed precision is not available in this build");
+  // The reference's halo exchange sends NG interior layers; a block narrower than
+  // NG would send ghost cells.  Tile coordinates are 16-bit and padded offsets fit
+  // a 31-bit index per array.
+  if (IM < (uint32_t)NG || JM < (uint32_t)NG || KM < (uint32_t)NG)
+    return fail(CBNS_ERR_BAD_DIMS, "cbns_create: every extent must be >= 4 (NG)");
+  const double vol = (double)(IM + 2 * NG) * (JM + 2 * NG) * (KM + 2 * NG);
+  if (IM > 16384 || JM > 16384 || KM > 16384 || vol * NEQ > 2147483647.0)
+    return fail(CBNS_ERR_BAD_DIMS, "cbns_create: block too large (5*(IM+8)(JM+8)(KM+8) must be < 2^31)");
+  if (!(p->gamma > 1.0) || !(p->Re > 0.0) || !(p->Mach > 0.0) || !(p->Pr > 0.0) || !(p->CFL > 0.0) ||
+      !(p->T_inf > 0.0) || p->IM == 0 || p->JM == 0 || p->KM == 0)
+    return fail(CBNS_ERR_INVALID_ARG, "cbns_create: parameters out of range (gamma>1, Re, Mach, Pr, CFL, T_inf > 0)");
+
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return fail(CBNS_ERR_NO_DEVICE, "cbns_create: no CUDA device");
+  }
+  int dev = 0;
+  if (const char* e = std::getenv("CBNS_DEVICE")) dev = std::atoi(e);
+  if (dev < 0 || dev >= ndev) return fail(CBNS_ERR_NO_DEVICE, "cbns_create: CBNS_DEVICE out of range");
+  cudaDeviceProp prop;
+  CBNS_CUDA(cudaGetDeviceProperties(&prop, dev));
+  if (prop.major != 10 || prop.minor != 3)
+    return fail(CBNS_ERR_NO_DEVICE, std::string("cbns_create: built for sm_103a, device is ") + prop.name);
+
+  cbns_handle* h = new cbns_handle();
+  h->device = dev;
+  h->precision = precision;
+  h->params = *p;
+  cbns_params_derive(&h->params);
+  h->IM = IM;
+  h->JM = JM;
+  h->KM = KM;
+  cbns_status st = CBNS_OK;
+  auto bail = [&](cbns_status s) {
+    cbns_destroy(h);
+    return s;
+  };
+  if (cudaSetDevice(dev) != cudaSuccess) return bail(cuda_fail(cudaGetLastError(), "cudaSetDevice"));
+  if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess)
+    return bail(cuda_fail(cudaGetLastError(), "cudaStreamCreate"));
+
+  SolveDev& s = h->desc;
+  s.IM = IM;
+  s.JM = JM;
+  s.KM = KM;
+  s.nx = IM + 2 * NG;
+  s.ny = JM + 2 * NG;
+  s.nz = KM + 2 * NG;
+  s.V = (long long)s.nx * s.ny * s.nz;
+  s.rx = IM + 2 * NGV;
+  s.ry = JM + 2 * NGV;
+  s.rz = KM + 2 * NGV;
+  s.RV = (long long)s.rx * s.ry * s.rz;
+  s.IV = (long long)IM * JM * KM;
+
+  std::vector<TileRef> t_int, t_ring, t_pad;
+  append_tiles(t_int, 0, IM, JM, KM);
+  append_tiles(t_ring, 0, s.rx, s.ry, s.rz);
+  append_tiles(t_pad, 0, s.nx, s.ny, s.nz);
+  h->n_int = (int)t_int.size();
+  h->n_ring = (int)t_ring.size();
+  h->n_pad = (int)t_pad.size();
+  h->nparts = 1024;
+
+  // Arena layout.
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    size_t o = off;
+    off += align_up(bytes);
+    return o;
+  };
+  const size_t dV = sizeof(double) * (size_t)s.V;
+  size_t oQ = take(NEQ * dV), oQp = take(NEQ * dV), oStage = take(NEQ * dV);
+  size_t oPrim = take(9 * dV);
+  size_t oF[3], oFv[3];
+  for (int d = 0; d < 3; ++d) oF[d] = take(sizeof(double) * NEQ * (size_t)s.IV);
+  for (int d = 0; d < 3; ++d) oFv[d] = take(sizeof(double) * (NEQ - 1) * (size_t)s.RV);
+  size_t oCtl = take(sizeof(SolveCtl));
+  size_t oDesc = take(sizeof(SolveDev));
+  size_t oTi = take(sizeof(TileRef) * t_int.size());
+  size_t oTr = take(sizeof(TileRef) * t_ring.size());
+  size_t oTp = take(sizeof(TileRef) * t_pad.size());
+  size_t oPart = take(sizeof(double) * 4 * h->nparts);
+  size_t oOut = take(sizeof(double) * 8);
+  h->arena_bytes = off;
+  cudaError_t e = cudaMalloc(&h->arena, off);
+  if (e != cudaSuccess) return bail(cuda_fail(e, "cudaMalloc(arena)"));
+  e = cudaMemsetAsync(h->arena, 0, off, h->stream);
+  if (e != cudaSuccess) return bail(cuda_fail(e, "cudaMemset(arena)"));
+
+  char* A = h->arena;
+  s.Q = (double*)(A + oQ);
+  s.Qp = (double*)(A + oQp);
+  h->d_stage = (double*)(A + oStage);
+  double* prim = (double*)(A + oPrim);
+  s.rho = prim + 0 * s.V;
+  s.u = prim + 1 * s.V;
+  s.v = prim + 2 * s.V;
+  s.w = prim + 3 * s.V;
+  s.p = prim + 4 * s.V;
+  s.T = prim + 5 * s.V;
+  s.srho = prim + 6 * s.V;
+  s.H = prim + 7 * s.V;
+  s.mu = prim + 8 * s.V;
+  for (int d = 0; d < 3; ++d) {
+    s.F[d] = (double*)(A + oF[d]);
+    s.Fv[d] = (double*)(A + oFv[d]);
+  }
+  const cbns_params& P = h->params;
+  s.gamma = P.gamma;
+  s.gam1 = P.gam1;
+  s.gam1_inv = P.gam1_inv;
+  s.gM2 = P.gM2;
+  s.Re_inv = P.Re_inv;
+  s.kappa = -P.Pr_inv * P.gam1_inv / P.Mach2;  // src/Block3d.cpp:766-767
+  s.C_T_inf = P.C_T_inf;
+  s.CFL = P.CFL;
+  s.C_dt_v = P.C_dt_v;
+  // gen_mesh (src/Block3d.cpp:215-219): spacing from the global grid size.
+  const double two_pi = 2.0 * 3.14159265358979323846;
+  s.dx = two_pi / P.IM;
+  s.dy = two_pi / P.JM;
+  s.dz = two_pi / P.KM;
+  s.inv_dx = 1.0 / s.dx;
+  s.inv_dy = 1.0 / s.dy;
+  s.inv_dz = 1.0 / s.dz;
+  h->d_ctl = (SolveCtl*)(A + oCtl);
+  s.ctl = h->d_ctl;
+  h->d_desc = (SolveDev*)(A + oDesc);
+  h->d_tiles_int = (TileRef*)(A + oTi);
+  h->d_tiles_ring = (TileRef*)(A + oTr);
+  h->d_tiles_pad = (TileRef*)(A + oTp);
+  h->d_partials = (double*)(A + oPart);
+  h->d_out = (double*)(A + oOut);
+
+  if ((e = cudaMallocHost(&h->h_ctl, sizeof(SolveCtl))) != cudaSuccess) return bail(cuda_fail(e, "cudaMallocHost"));
+  if ((e = cudaMallocHost(&h->h_out, sizeof(double) * 8)) != cudaSuccess) return bail(cuda_fail(e, "cudaMallocHost"));
+  std::memset(h->h_ctl, 0, sizeof(SolveCtl));
+  h->h_ctl->t_cur = P.t_cur;
+  h->h_ctl->t_end = P.t_end;
+
+  if ((e = cudaMemcpyAsync(h->d_desc, &h->desc, sizeof(SolveDev), cudaMemcpyHostToDevice, h->stream)) != cudaSuccess ||
+      (e = cudaMemcpyAsync(h->d_tiles_int, t_int.data(), sizeof(TileRef) * t_int.size(), cudaMemcpyHostToDevice,
+                           h->stream)) != cudaSuccess ||
+      (e = cudaMemcpyAsync(h->d_tiles_ring, t_ring.data(), sizeof(TileRef) * t_ring.size(),
+                           cudaMemcpyHostToDevice, h->stream)) != cudaSuccess ||
+      (e = cudaMemcpyAsync(h->d_tiles_pad, t_pad.data(), sizeof(TileRef) * t_pad.size(), cudaMemcpyHostToDevice,
+                           h->stream)) != cudaSuccess ||
+      (e = cudaMemcpyAsync(h->d_ctl, h->h_ctl, sizeof(SolveCtl), cudaMemcpyHostToDevice, h->stream)) != cudaSuccess)
+    return bail(cuda_fail(e, "cudaMemcpyAsync(setup)"));
+  if ((e = cudaStreamSynchronize(h->stream)) != cudaSuccess) return bail(cuda_fail(e, "cudaStreamSynchronize"));
+  (void)st;
+  *out = h;
+  return CBNS_OK;
+}
+
+static cbns_status check_handle(cbns_handle* h, const char* fn) {
+  if (!h) return fail(CBNS_ERR_INVALID_ARG, std::string(fn) + ": null handle");
+  cudaError_t e = cudaSetDevice(h->device);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+  return CBNS_OK;
+}
+
+cbns_status cbns_upload_Q(cbns_handle* h, const double* Q, double t) {
+  cbns_status st = check_handle(h, "cbns_upload_Q");
+  if (st != CBNS_OK) return st;
+  if (!Q) return fail(CBNS_ERR_INVALID_ARG, "cbns_upload_Q: null Q");
+  const SolveDev& s = h->desc;
+  // The host array goes to the staging buffer as-is, is transposed into Q (SoA),
+  // then the start-up kernel fills ghosts, primitives, Q_p and mu.
+  CBNS_CUDA(cudaMemcpyAsync(h->d_stage, Q, sizeof(double) * NEQ * (size_t)s.V, cudaMemcpyHostToDevice, h->stream));
+  CBNS_CUDA(launch_layout(h->d_desc, 0, h->d_stage, s.Q, true, s.V, h->stream, h->pf()));
+  CBNS_CUDA(launch_prepare(h->d_desc, h->d_tiles_pad, h->n_pad, h->stream, h->pf()));
+  std::memset(h->h_ctl, 0, sizeof(SolveCtl));
+  h->h_ctl->t_cur = t;
+  h->h_ctl->t_end = h->params.t_end;
+  h->h_ctl->active = 1;
+  CBNS_CUDA(cudaMemcpyAsync(h->d_ctl, h->h_ctl, sizeof(SolveCtl), cudaMemcpyHostToDevice, h->stream));
+  CBNS_CUDA(cudaStreamSynchronize(h->stream));
+  return CBNS_OK;
+}
+
+static cbns_status download_state(cbns_handle* h, const double* src, double* dst, const char* fn) {
+  cbns_status st = check_handle(h, fn);
+  if (st != CBNS_OK) return st;
+  if (!dst) return fail(CBNS_ERR_INVALID_ARG, std::string(fn) + ": null output");
+  const SolveDev& s = h->desc;
+  CBNS_CUDA(launch_layout(h->d_desc, 0, src, h->d_stage, false, s.V, h->stream, h->pf()));
+  CBNS_CUDA(cudaMemcpyAsync(dst, h->d_stage, sizeof(double) * NEQ * (size_t)s.V, cudaMemcpyDeviceToHost, h->stream));
+  CBNS_CUDA(cudaStreamSynchronize(h->stream));
+  return CBNS_OK;
+}
+
+cbns_status cbns_download_Q(cbns_handle* h, double* Q) {
+  if (!h) return fail(CBNS_ERR_INVALID_ARG, "cbns_download_Q: null handle");
+  return download_state(h, h->desc.Q, Q, "cbns_download_Q");
+}
+
+cbns_status cbns_download_Q_p(cbns_handle* h, double* Qp) {
+  if (!h) return fail(CBNS_ERR_INVALID_ARG, "cbns_download_Q_p: null handle");
+  return download_state(h, h->desc.Qp, Qp, "cbns_download_Q_p");
+}
+
+cbns_status cbns_download_prims(cbns_handle* h, double* rho, double* u, double* v, double* w, double* p,
+                                double* T) {
+  cbns_status st = check_handle(h, "cbns_download_prims");
+  if (st != CBNS_OK) return st;
+  const SolveDev& s = h->desc;
+  const size_t bytes = sizeof(double) * (size_t)s.V;
+  double* dst[6] = {rho, u, v, w, p, T};
+  double* src[6] = {s.rho, s.u, s.v, s.w, s.p, s.T};
+  for (int a = 0; a < 6; ++a)
+    if (dst[a]) CBNS_CUDA(cudaMemcpyAsync(dst[a], src[a], bytes, cudaMemcpyDeviceToHost, h->stream));
+  CBNS_CUDA(cudaStreamSynchronize(h->stream));
+  return CBNS_OK;
+}
+
+cbns_status cbns_calc_dt(cbns_handle* h, double* dt) {
+  cbns_status st = check_handle(h, "cbns_calc_dt");
+  if (st != CBNS_OK) return st;
+  if (!dt) return fail(CBNS_ERR_INVALID_ARG, "cbns_calc_dt: null output");
+  CBNS_CUDA(launch_dt_raw(h->d_desc, 0, h->d_tiles_int, h->n_int, h->d_out, h->stream, h->pf()));
+  CBNS_CUDA(cudaMemcpyAsync(h->h_out, h->d_out, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  CBNS_CUDA(cudaStreamSynchronize(h->stream));
+  *dt = h->h_out[0];
+  return CBNS_OK;
+}
+
+static cbns_status enqueue_stage(cbns_handle* h, int stage) {
+  CBNS_CUDA(launch_stage(h->d_desc, h->d_tiles_int, h->n_int, h->d_tiles_ring, h->n_ring, stage, 0, h->stream,
+                         h->pf()));
+  return CBNS_OK;
+}
+
+cbns_status cbns_stage(cbns_handle* h, double dt, int stage) {
+  cbns_status st = check_handle(h, "cbns_stage");
+  if (st != CBNS_OK) return st;
+  if (stage < 1 || stage > 3) return fail(CBNS_ERR_INVALID_ARG, "cbns_stage: stage must be 1, 2 or 3");
+  CBNS_CUDA(launch_set_dt(h->d_desc, 0, dt, h->stream));
+  if ((st = enqueue_stage(h, stage)) != CBNS_OK) return st;
+  CBNS_CUDA(cudaStreamSynchronize(h->stream));
+  return CBNS_OK;
+}
+
+static cbns_status enqueue_step(cbns_handle* h, double t_end, bool use_t_end) {
+  CBNS_CUDA(launch_dt(h->d_desc, 1, h->d_tiles_int, h->n_int, t_end, use_t_end, h->stream, h->pf()));
+  for (int s = 1; s <= 3; ++s) {
+    cbns_status st = enqueue_stage(h, s);
+    if (st != CBNS_OK) return st;
+  }
+  return CBNS_OK;
+}
+
+cbns_status cbns_step(cbns_handle* h, double t_end, double* dt_out, double* t_out) {
+  cbns_status st = check_handle(h, "cbns_step");
+  if (st != CBNS_OK) return st;
+  if ((st = enqueue_step(h, t_end, true)) != CBNS_OK) return st;
+  CBNS_CUDA(cudaMemcpyAsync(h->h_ctl, h->d_ctl, sizeof(SolveCtl), cudaMemcpyDeviceToHost, h->stream));
+  CBNS_CUDA(cudaStreamSynchronize(h->stream));
+  if (dt_out) *dt_out = h->h_ctl->dt;
+  if (t_out) *t_out = h->h_ctl->t_cur;
+  if (h->h_ctl->status) return fail(CBNS_ERR_NONPHYSICAL, "cbns_step: non-physical state (rho <= 0, p <= 0 or NaN)");
+  return h->h_ctl->active ? CBNS_OK : CBNS_FINISHED;
+}
+
+cbns_status cbns_run(cbns_handle* h, uint32_t nsteps, double t_end, uint32_t* steps_done) {
+  cbns_status st = check_handle(h, "cbns_run");
+  if (st != CBNS_OK) return st;
+  CBNS_CUDA(cudaMemcpyAsync(h->h_ctl, h->d_ctl, sizeof(SolveCtl), cudaMemcpyDeviceToHost, h->stream));
+  CBNS_CUDA(cudaStreamSynchronize(h->stream));
+  const unsigned start = h->h_ctl->steps;
+  if (h->prof.on) {
+    // Profiling: direct launches, each bracketed by events.
+    for (uint32_t n = 0; n < nsteps; ++n)
+      if ((st = enqueue_step(h, t_end, true)) != CBNS_OK) return st;
+  } else if (!h->step_graph || h->graph_t_end != t_end) {
+    if (h->step_graph) {
+      cudaGraphExecDestroy(h->step_graph);
+      h->step_graph = nullptr;
+    }
+    cudaGraph_t g;
+    CBNS_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    st = enqueue_step(h, t_end, true);
+    cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+    if (st != CBNS_OK) return st;
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+    e = cudaGraphInstantiate(&h->step_graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+    h->graph_t_end = t_end;
+  }
+  if (!h->prof.on)
+    for (uint32_t n = 0; n < nsteps; ++n) CBNS_CUDA(cudaGraphLaunch(h->step_graph, h->stream));
+  CBNS_CUDA(cudaMemcpyAsync(h->h_ctl, h->d_ctl, sizeof(SolveCtl), cudaMemcpyDeviceToHost, h->stream));
+  CBNS_CUDA(cudaStreamSynchronize(h->stream));
+  if (steps_done) *steps_done = h->h_ctl->steps - start;
+  if (h->h_ctl->status) return fail(CBNS_ERR_NONPHYSICAL, "cbns_run: non-physical state (rho <= 0, p <= 0 or NaN)");
+  return CBNS_OK;
+}
+
+cbns_status cbns_get_time(cbns_handle* h, double* t_cur, double* dt_last) {
+  cbns_status st = check_handle(h, "cbns_get_time");
+  if (st != CBNS_OK) return st;
+  CBNS_CUDA(cudaMemcpyAsync(h->h_ctl, h->d_ctl, sizeof(SolveCtl), cudaMemcpyDeviceToHost, h->stream));
+  CBNS_CUDA(cudaStreamSynchronize(h->stream));
+  if (t_cur) *t_cur = h->h_ctl->t_cur;
+  if (dt_last) *dt_last = h->h_ctl->dt;
+  return CBNS_OK;
+}
+
+cbns_status cbns_diagnostics(cbns_handle* h, double* ke, double* enstrophy) {
+  cbns_status st = check_handle(h, "cbns_diagnostics");
+  if (st != CBNS_OK) return st;
+  const double inv_n = 1.0 / ((double)h->IM * (double)h->JM * (double)h->KM);
+  CBNS_CUDA(launch_diag(h->d_desc, 0, h->d_tiles_int, h->n_int, h->d_partials, h->nparts, inv_n, h->d_out,
+                        h->stream, h->pf()));
+  CBNS_CUDA(cudaMemcpyAsync(h->h_out, h->d_out, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  CBNS_CUDA(cudaStreamSynchronize(h->stream));
+  if (ke) *ke = h->h_out[0];
+  if (enstrophy) *enstrophy = h->h_out[1];
+  return CBNS_OK;
+}
+
+cbns_status cbns_check_state(cbns_handle* h) {
+  cbns_status st = check_handle(h, "cbns_check_state");
+  if (st != CBNS_OK) return st;
+  CBNS_CUDA(cudaMemcpyAsync(h->h_ctl, h->d_ctl, sizeof(SolveCtl), cudaMemcpyDeviceToHost, h->stream));
+  CBNS_CUDA(cudaStreamSynchronize(h->stream));
+  if (h->h_ctl->status) {
+    h->h_ctl->status = 0;
+    CBNS_CUDA(cudaMemcpyAsync(&h->d_ctl->status, &h->h_ctl->status, sizeof(int), cudaMemcpyHostToDevice,
+                              h->stream));
+    CBNS_CUDA(cudaStreamSynchronize(h->stream));
+    return fail(CBNS_ERR_NONPHYSICAL, "non-physical state (rho <= 0, p <= 0 or NaN) met since the last check");
+  }
+  return CBNS_OK;
+}
+
+void* cbns_stream(cbns_handle* h) { return h ? (void*)h->stream : nullptr; }
+
+cbns_status cbns_profile_begin(cbns_handle* h) {
+  cbns_status st = check_handle(h, "cbns_profile_begin");
+  if (st != CBNS_OK) return st;
+  h->prof.reset();
+  h->prof.on = true;
+  return CBNS_OK;
+}
+
+cbns_status cbns_profile_end(cbns_handle* h, cbns_kernel_time* out, int cap, int* n) {
+  cbns_status st = check_handle(h, "cbns_profile_end");
+  if (st != CBNS_OK) return st;
+  CBNS_CUDA(cudaStreamSynchronize(h->stream));
+  double total[KID_COUNT] = {0};
+  unsigned count[KID_COUNT] = {0};
+  for (const Profiler::Rec& r : h->prof.recs) {
+    if (!r.b) continue;
+    float ms = 0.f;
+    CBNS_CUDA(cudaEventElapsedTime(&ms, r.a, r.b));
+    total[r.id] += ms;
+    count[r.id] += 1;
+  }
+  h->prof.on = false;
+  h->prof.reset();
+  int k = 0;
+  for (int id = 0; id < KID_COUNT; ++id) {
+    if (!count[id]) continue;
+    if (out && k < cap) {
+      std::memset(out[k].name, 0, sizeof out[k].name);
+      std::strncpy(out[k].name, kernel_name(id), sizeof out[k].name - 1);
+      out[k].launches = count[id];
+      out[k].total_ms = total[id];
+    }
+    ++k;
+  }
+  if (n) *n = k < cap ? k : cap;
+  return CBNS_OK;
+}
+
+cbns_status cbns_get_info(cbns_handle* h, uint32_t dims[3], uint64_t* device_bytes, int* precision) {
+  if (!h) return fail(CBNS_ERR_INVALID_ARG, "cbns_get_info: null handle");
+  if (dims) {
+    dims[0] = h->IM;
+    dims[1] = h->JM;
+    dims[2] = h->KM;
+  }
+  if (device_bytes) *device_bytes = h->arena_bytes;
+  if (precision) *precision = h->precision;
+  return CBNS_OK;
+}
+
+}  // extern "C"

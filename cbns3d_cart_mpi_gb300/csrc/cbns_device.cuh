@@ -1,0 +1,91 @@
+// cbns_device.cuh — device-side data model of the GB300 right-hand-side library.
+//
+// A "solve" is one periodic block (the reference's Block3d).  Its arrays live in
+// HBM as structure-of-arrays, padded by NG = 4 ghost layers on every side like
+// the reference's (include/Block3d.h:169-199), so stencils need no wrap logic:
+//
+//   padded cell (i,j,k), i in [-NG, IM+NG):  off = (i+NG) + nx*((j+NG) + ny*(k+NG))
+//   Q[n*V + off], n = 0..4 (rho, rho*u, rho*v, rho*w, E);  V = nx*ny*nz
+//
+// Face fluxes are stored per direction at the cell on the face's high side (face
+// i-1/2 at cell i), over the interior only: the periodic face IM-1/2... +1/2 is
+// face -1/2 (same stencil values), so F[IM] reads F[0].
+//
+// Work is cut into tiles of TILE_X x TILE_Y x 1 cells; a batch of solves is one
+// flattened table of tiles, so a single launch covers every solve of a batch.
+#pragma once
+
+#include <cstdint>
+
+namespace cbns {
+
+constexpr int NEQ = 5;
+constexpr int NG = 4;
+constexpr int NGV = 2;
+constexpr int TILE_X = 32;
+constexpr int TILE_Y = 4;
+constexpr int TILE_THREADS = TILE_X * TILE_Y;
+
+// Per-solve time control, kept on the device so a replayed step graph needs no
+// host round trip (the loop of src/cbns3d.cpp:176-198).
+struct SolveCtl {
+  double t_cur;
+  double t_end;
+  double dt;
+  unsigned long long smax_bits;  // running max of calc_dt's wave-speed sum (bits of a double >= 0)
+  int active;                    // 0 once is_finished held: later kernels of the step do nothing
+  int status;                    // CBNS_ERR_NONPHYSICAL bit pattern once a stage met a bad state
+  unsigned int steps;            // steps taken since upload
+  int pad;
+};
+
+struct SolveDev {
+  int IM, JM, KM;      // interior extents
+  int nx, ny, nz;      // padded extents (IM + 2*NG ...)
+  long long V;         // padded volume
+  int rx, ry, rz;      // NGV-ring extents (IM + 2*NGV ...)
+  long long RV;        // ring volume
+  long long IV;        // interior volume
+  // conserved state (SoA, padded)
+  double* Q;
+  double* Qp;
+  // primitives of the current stage input (padded)
+  double* rho;
+  double* u;
+  double* v;
+  double* w;
+  double* p;
+  double* T;
+  double* srho;  // sqrt(rho): Roe weights
+  double* H;     // total enthalpy
+  double* mu;    // Sutherland viscosity, interior; lagged into calc_dt like the reference
+  // face fluxes (interior, 5 components each)
+  double* F[3];
+  // viscous fluxes Ev, Fv, Gv on the NGV ring, 4 components each
+  double* Fv[3];
+  // parameters (src/read_input.cpp:78-90)
+  double gamma, gam1, gam1_inv, gM2, Re_inv, kappa, C_T_inf, CFL, C_dt_v;
+  double dx, dy, dz, inv_dx, inv_dy, inv_dz;
+  SolveCtl* ctl;
+};
+
+struct TileRef {
+  uint16_t solve;
+  uint16_t ti;
+  uint16_t tj;
+  uint16_t tk;
+};
+
+__host__ __device__ inline long long pad_off(const SolveDev& s, int i, int j, int k) {
+  return (long long)(i + NG) + (long long)s.nx * ((long long)(j + NG) + (long long)s.ny * (k + NG));
+}
+__host__ __device__ inline long long ring_off(const SolveDev& s, int i, int j, int k) {
+  return (long long)(i + NGV) + (long long)s.rx * ((long long)(j + NGV) + (long long)s.ry * (k + NGV));
+}
+__host__ __device__ inline long long int_off(const SolveDev& s, int i, int j, int k) {
+  return (long long)i + (long long)s.IM * ((long long)j + (long long)s.JM * k);
+}
+
+enum Domain { DOM_INTERIOR = 0, DOM_RING = 1, DOM_PADDED = 2 };
+
+}  // namespace cbns

@@ -1,0 +1,738 @@
+// cbns_kernels.cu — sm_103a kernels of one RK3 stage of the cbns3d right-hand side.
+//
+// One stage (src/cbns3d.cpp:203-240) is four launches over a flattened tile
+// table that may span many solves:
+//   k_inviscid<0,1,2>  characteristic WENO5 + Roe eigenvectors + local Lax-Friedrichs
+//                      flux at every face normal to x, y, z (Block3d::rec_riemann_x/y/z)
+//   k_viscous          4th-order velocity/temperature gradients, Sutherland mu, stress,
+//                      heat flux and the viscous fluxes Ev, Fv, Gv on the NGV ring
+//                      (calc_viscous_terms + calc_viscous_flux)
+//   k_update           flux differences + 4th-order viscous divergence, SSP-RK3 update,
+//                      then the periodic ghost fill and the primitive recovery of the
+//                      new state, written to the cell and all its ghost images
+//                      (calc_viscous_flux_contribution tail, update_rk3,
+//                      boundary_condition, calc_primitive)
+// plus, once per step, k_dt_reduce + k_dt_finalize (calc_dt, the MIN all-reduce,
+// the clip to t_end and is_finished).
+//
+// The arithmetic is binary64 throughout.  GB300 issues binary64 at about 1/64 of
+// the binary32 rate (about 2 DFMA per clock per SM), so the kernels are bound by
+// the FP64 pipe and are written to issue few binary64 instructions: the
+// eigenvector products use the structure of L and R for axis-aligned normals,
+// the stencil projections are shared by the two biased reconstructions of a
+// face, the five WENO normalisations of a state share one division, and
+// divisions by constants become multiplications.  These rewrites change
+// rounding only (a few ulp per operation); the results stay within the 1e-11
+// relative tolerance of the reference after 100 steps.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdint>
+
+#include "cbns_device.cuh"
+#include "cbns_prof.h"
+
+namespace cbns {
+
+// ---------------------------------------------------------------------------
+// Tile walk.  Every kernel loops over its tile table with a grid stride, so it
+// runs either one tile per CTA or persistently with fewer CTAs than tiles.
+
+struct TileCell {
+  int s;  // solve index
+  int i, j, k;
+};
+
+__device__ __forceinline__ TileCell tile_cell(const TileRef& t, int origin) {
+  TileCell c;
+  c.s = t.solve;
+  c.i = origin + t.ti * TILE_X + (int)(threadIdx.x % TILE_X);
+  c.j = origin + t.tj * TILE_Y + (int)(threadIdx.x / TILE_X);
+  c.k = origin + t.tk;
+  return c;
+}
+
+// ---------------------------------------------------------------------------
+// Start-up: ghost fill, primitives, Q_p = Q, mu = 1 (src/cbns3d.cpp:149-153 and
+// src/Block3d.cpp:265).  Over the padded domain; each cell reads only its
+// interior source, so ghosts and interior are written without races.
+
+__device__ __forceinline__ int wrap(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
+
+__device__ __forceinline__ void store_prims(const SolveDev& s, long long o, double r, double ru,
+                                            double rv, double rw, double E) {
+  double ir = 1.0 / r;
+  double uu = ru * ir, vv = rv * ir, ww = rw * ir;
+  double q2 = uu * uu + vv * vv + ww * ww;
+  double pp = s.gam1 * (E - 0.5 * r * q2);
+  s.rho[o] = r;
+  s.u[o] = uu;
+  s.v[o] = vv;
+  s.w[o] = ww;
+  s.p[o] = pp;
+  s.T[o] = s.gM2 * pp * ir;
+  s.srho[o] = sqrt(r);
+  s.H[o] = s.gamma * s.gam1_inv * pp * ir + 0.5 * q2;
+}
+
+__global__ void k_aos_to_soa(const SolveDev* __restrict__ solves, int sidx, const double* __restrict__ aos,
+                             double* __restrict__ soa) {
+  const SolveDev& s = solves[sidx];
+  for (long long o = blockIdx.x * (long long)blockDim.x + threadIdx.x; o < s.V;
+       o += (long long)gridDim.x * blockDim.x) {
+#pragma unroll
+    for (int n = 0; n < NEQ; ++n) soa[n * s.V + o] = aos[NEQ * o + n];
+  }
+}
+
+__global__ void k_soa_to_aos(const SolveDev* __restrict__ solves, int sidx, const double* __restrict__ soa,
+                             double* __restrict__ aos) {
+  const SolveDev& s = solves[sidx];
+  for (long long o = blockIdx.x * (long long)blockDim.x + threadIdx.x; o < s.V;
+       o += (long long)gridDim.x * blockDim.x) {
+#pragma unroll
+    for (int n = 0; n < NEQ; ++n) aos[NEQ * o + n] = soa[n * s.V + o];
+  }
+}
+
+__global__ void k_prepare(const SolveDev* __restrict__ solves, const TileRef* __restrict__ tiles,
+                          int ntiles) {
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    TileCell tc = tile_cell(tiles[t], -NG);
+    const SolveDev& s = solves[tc.s];
+    if (tc.i >= s.IM + NG || tc.j >= s.JM + NG) continue;
+    const long long o = pad_off(s, tc.i, tc.j, tc.k);
+    const long long src = pad_off(s, wrap(tc.i, s.IM), wrap(tc.j, s.JM), wrap(tc.k, s.KM));
+    double q[NEQ];
+#pragma unroll
+    for (int n = 0; n < NEQ; ++n) q[n] = s.Q[n * s.V + src];
+#pragma unroll
+    for (int n = 0; n < NEQ; ++n) {
+      s.Q[n * s.V + o] = q[n];
+      s.Qp[n * s.V + o] = q[n];
+    }
+    store_prims(s, o, q[0], q[1], q[2], q[3], q[4]);
+    const bool interior = tc.i >= 0 && tc.i < s.IM && tc.j >= 0 && tc.j < s.JM && tc.k >= 0 && tc.k < s.KM;
+    if (interior) s.mu[o] = 1.0;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Time step: Block3d::calc_dt (src/Block3d.cpp:515-553) as a max-reduction, then
+// the MIN all-reduce (trivial on one block), clip to t_end and is_finished
+// (src/cbns3d.cpp:178-194, src/Block3d.cpp:502-513).
+
+__device__ __forceinline__ double warp_max(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+__global__ void k_dt_reduce(const SolveDev* __restrict__ solves, const TileRef* __restrict__ tiles,
+                            int ntiles, double t_end, int use_t_end, int skip_finished) {
+  __shared__ double red[TILE_THREADS / 32];
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    TileCell tc = tile_cell(tiles[t], 0);
+    const SolveDev& s = solves[tc.s];
+    const SolveCtl* ctl = s.ctl;
+    const double te = use_t_end ? t_end : ctl->t_end;
+    if (skip_finished && ctl->t_cur + 1.0e-5 > te) continue;  // uniform over the tile
+    double sm = 0.0;
+    if (tc.i < s.IM && tc.j < s.JM) {
+      const long long o = pad_off(s, tc.i, tc.j, tc.k);
+      double rr = s.rho[o], uu = s.u[o], vv = s.v[o], ww = s.w[o], pp = s.p[o];
+      double c = sqrt(s.gamma * pp / rr);
+      double fv = 2.0 * s.mu[o] * s.C_dt_v * sqrt(uu * uu + vv * vv + ww * ww) / (c * rr);
+      double t1 = fabs(uu) + c * s.inv_dx + fv * s.inv_dx * s.inv_dx;
+      double t2 = fabs(vv) + c * s.inv_dy + fv * s.inv_dy * s.inv_dy;
+      double t3 = fabs(ww) + c * s.inv_dz + fv * s.inv_dz * s.inv_dz;
+      double sum = t1 + t2 + t3;
+      sm = (sum > 0.0) ? sum : 0.0;  // a NaN is skipped, as the reference's ternary does
+    }
+    sm = warp_max(sm);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = sm;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double m = red[0];
+#pragma unroll
+      for (int a = 1; a < TILE_THREADS / 32; ++a) m = fmax(m, red[a]);
+      // Positive doubles order like their bit patterns.
+      atomicMax(&s.ctl->smax_bits, (unsigned long long)__double_as_longlong(m));
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void k_dt_finalize(const SolveDev* __restrict__ solves, int nsolves, double t_end,
+                              int use_t_end) {
+  int si = blockIdx.x * blockDim.x + threadIdx.x;
+  if (si >= nsolves) return;
+  SolveCtl* ctl = solves[si].ctl;
+  if (use_t_end) ctl->t_end = t_end;
+  double smax = __longlong_as_double((long long)ctl->smax_bits);
+  ctl->smax_bits = 0ull;
+  if (ctl->t_cur + 1.0e-5 > ctl->t_end) {
+    ctl->active = 0;
+    return;
+  }
+  double dt = solves[si].CFL / smax;
+  if (ctl->t_end - ctl->t_cur < dt) dt = ctl->t_end - ctl->t_cur;
+  ctl->t_cur += dt;
+  ctl->dt = dt;
+  ctl->active = 1;
+  ctl->steps += 1;
+}
+
+// calc_dt's value alone (cbns_calc_dt): CFL / max, no clip, no time advance.
+__global__ void k_dt_raw(const SolveDev* __restrict__ solves, int sidx, double* __restrict__ out) {
+  SolveCtl* ctl = solves[sidx].ctl;
+  out[0] = solves[sidx].CFL / __longlong_as_double((long long)ctl->smax_bits);
+  ctl->smax_bits = 0ull;
+}
+
+// Explicit dt for a single stage called from the host (cbns_stage).
+__global__ void k_set_dt(const SolveDev* __restrict__ solves, int sidx, double dt) {
+  SolveCtl* ctl = solves[sidx].ctl;
+  ctl->dt = dt;
+  ctl->active = 1;
+}
+
+// ---------------------------------------------------------------------------
+// WENO5 (src/weno.cpp:25-56).  The reference forms w_k = d_k / IS_k^2 and returns
+// (sum w_k f_k) / (sum w_k).  Multiplying numerator and denominator by
+// 10 * IS_1^2 IS_2^2 IS_3^2 gives the same value with one division,
+//   num = a2 a3 f1 + 6 a1 a3 f2 + 3 a1 a2 f3,  den = a2 a3 + 6 a1 a3 + 3 a1 a2,
+// a_k = IS_k^2; the division is deferred so five of them can share one.
+
+struct Weno {
+  double num, den;
+};
+
+__device__ __forceinline__ Weno weno5_parts(double a, double b, double c, double d, double e) {
+  const double eps = 1.0e-6;
+  const double c13 = 13.0 / 12.0;
+  double d1 = a - 2.0 * b + c;
+  double d2 = a - 4.0 * b + 3.0 * c;
+  double d3 = b - 2.0 * c + d;
+  double d4 = b - d;
+  double d5 = c - 2.0 * d + e;
+  double d6 = 3.0 * c - 4.0 * d + e;
+  double is1 = c13 * d1 * d1 + 0.25 * d2 * d2 + eps;
+  double is2 = c13 * d3 * d3 + 0.25 * d4 * d4 + eps;
+  double is3 = c13 * d5 * d5 + 0.25 * d6 * d6 + eps;
+  double a1 = is1 * is1, a2 = is2 * is2, a3 = is3 * is3;
+  double p1 = a2 * a3;
+  double p2 = (6.0 * a1) * a3;
+  double p3 = (3.0 * a1) * a2;
+  const double s6 = 1.0 / 6.0;
+  double f1 = (2.0 * s6) * a - (7.0 * s6) * b + (11.0 * s6) * c;
+  double f2 = -s6 * b + (5.0 * s6) * c + (2.0 * s6) * d;
+  double f3 = (2.0 * s6) * c + (5.0 * s6) * d - s6 * e;
+  Weno r;
+  r.num = p1 * f1 + p2 * f2 + p3 * f3;
+  r.den = p1 + p2 + p3;
+  return r;
+}
+
+// r[n] = num[n] / den[n] for five parts with one division (Montgomery's
+// simultaneous inversion).  Every den lies in [1e-23, 1e61] unless a smoothness
+// indicator exceeds ~1e15; outside that the product leaves the normal range and
+// each quotient is divided on its own.
+__device__ __forceinline__ void weno_divide5(const Weno (&w)[5], double (&r)[5]) {
+  double p1 = w[0].den;
+  double p2 = p1 * w[1].den;
+  double p3 = p2 * w[2].den;
+  double p4 = p3 * w[3].den;
+  double p5 = p4 * w[4].den;
+  if (p5 > 1.0e-300 && p5 < 1.0e300) {
+    double inv = 1.0 / p5;
+    r[4] = w[4].num * (inv * p4);
+    inv *= w[4].den;
+    r[3] = w[3].num * (inv * p3);
+    inv *= w[3].den;
+    r[2] = w[2].num * (inv * p2);
+    inv *= w[2].den;
+    r[1] = w[1].num * (inv * p1);
+    inv *= w[1].den;
+    r[0] = w[0].num * inv;
+  } else {
+#pragma unroll
+    for (int n = 0; n < 5; ++n) r[n] = w[n].num / w[n].den;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Numerical flux at one face (src/Block3d.cpp:566-616 and its y/z twins).
+//
+// Eigenvectors (src/eigenvectors_roe.cpp:32-171).  For a face normal to axis D
+// the tangent vectors l, m are the other two axes up to sign, so with the Roe
+// state (U, H, c), K = (gamma-1)/(2c^2) and t = q^2/2 f0 - U.m + f4 (m the
+// momentum of the projected conserved vector f):
+//   L f = ( A + B, f0 - 2A, A - B, f_t1 - U_t1 f0, f_t2 - U_t2 f0 ),
+//   A = K t,  B = (U_D f0 - f_D) / (2c)
+// (the signs of the two shear fields are dropped: WENO5 is odd, R flips them back).
+// R r, with s = r0 + r2 and d = r2 - r0:
+//   rho = s + r1,  m_D = U_D rho + c d,  m_ti = U_ti rho + r_ti,
+//   E = H s + U_D c d + q^2/2 r1 + U_t1 r3 + U_t2 r4.
+// The Roe average (ratio = sqrt(rho_R/rho_L)) is formed from per-cell sqrt(rho).
+// lf_flux (src/lf_flux.cpp:32-99) takes the reconstructed conserved states.
+
+template <int D>
+__device__ __forceinline__ void face_flux(const SolveDev& s, const double* __restrict__ U,
+                                          long long c, double (&out)[NEQ]) {
+  constexpr int T1 = (D + 1) % 3;
+  constexpr int T2 = (D + 2) % 3;
+  const long long st = D == 0 ? 1ll : (D == 1 ? (long long)s.nx : (long long)s.nx * s.ny);
+  const long long V = s.V;
+  const long long cl = c - st;
+
+  // Roe-averaged state of the two cells either side (src/eigenvectors_roe.cpp:87-106).
+  const double sL = s.srho[cl], sR = s.srho[c];
+  const double inv = 1.0 / (sL + sR);
+  double Uv[3];
+  Uv[0] = (sL * s.u[cl] + sR * s.u[c]) * inv;
+  Uv[1] = (sL * s.v[cl] + sR * s.v[c]) * inv;
+  Uv[2] = (sL * s.w[cl] + sR * s.w[c]) * inv;
+  const double HH = (sL * s.H[cl] + sR * s.H[c]) * inv;
+  const double q2 = Uv[0] * Uv[0] + Uv[1] * Uv[1] + Uv[2] * Uv[2];
+  const double hq2 = 0.5 * q2;
+  const double cc = sqrt(s.gam1 * (HH - hq2));
+  const double ic = 1.0 / cc;
+  const double K = (0.5 * s.gam1) * ic * ic;
+  const double hic = 0.5 * ic;
+  const double un = Uv[D], u1 = Uv[T1], u2 = Uv[T2];
+
+  // Characteristic projections of the six cells c-3 .. c+2 (shared by both
+  // biased stencils).
+  double w[NEQ][6];
+#pragma unroll
+  for (int m = 0; m < 6; ++m) {
+    const long long o = c + (m - 3) * st;
+    const double f0 = U[o], f1 = U[V + o], f2 = U[2 * V + o], f3 = U[3 * V + o], f4 = U[4 * V + o];
+    const double fm[3] = {f1, f2, f3};
+    const double t = hq2 * f0 - (Uv[0] * f1 + Uv[1] * f2 + Uv[2] * f3) + f4;
+    const double A = K * t;
+    const double B = hic * (un * f0 - fm[D]);
+    w[0][m] = A + B;
+    w[1][m] = f0 - 2.0 * A;
+    w[2][m] = A - B;
+    w[3][m] = fm[T1] - u1 * f0;
+    w[4][m] = fm[T2] - u2 * f0;
+  }
+
+  // Left-biased (cells -3..+1) and right-biased mirrored (+2..-2) reconstructions
+  // (src/Block3d.cpp:591-607, src/weno.cpp:77-152).
+  double rl[NEQ], rr[NEQ];
+  {
+    Weno wl[NEQ];
+#pragma unroll
+    for (int n = 0; n < NEQ; ++n) wl[n] = weno5_parts(w[n][0], w[n][1], w[n][2], w[n][3], w[n][4]);
+    weno_divide5(wl, rl);
+  }
+  {
+    Weno wr[NEQ];
+#pragma unroll
+    for (int n = 0; n < NEQ; ++n) wr[n] = weno5_parts(w[n][5], w[n][4], w[n][3], w[n][2], w[n][1]);
+    weno_divide5(wr, rr);
+  }
+
+  // Back to conserved variables.
+  double rhoL, mL[3], EL, rhoR, mR[3], ER;
+  {
+    double sp = rl[0] + rl[2], dm = rl[2] - rl[0];
+    rhoL = sp + rl[1];
+    mL[D] = un * rhoL + cc * dm;
+    mL[T1] = u1 * rhoL + rl[3];
+    mL[T2] = u2 * rhoL + rl[4];
+    EL = HH * sp + (un * cc) * dm + hq2 * rl[1] + u1 * rl[3] + u2 * rl[4];
+  }
+  {
+    double sp = rr[0] + rr[2], dm = rr[2] - rr[0];
+    rhoR = sp + rr[1];
+    mR[D] = un * rhoR + cc * dm;
+    mR[T1] = u1 * rhoR + rr[3];
+    mR[T2] = u2 * rhoR + rr[4];
+    ER = HH * sp + (un * cc) * dm + hq2 * rr[1] + u1 * rr[3] + u2 * rr[4];
+  }
+
+  // Local Lax-Friedrichs flux (src/lf_flux.cpp:32-99); both 1/rho from one division.
+  const double ip = 1.0 / (rhoL * rhoR);
+  const double iL = ip * rhoR, iR = ip * rhoL;
+  double vL[3], vR[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    vL[a] = mL[a] * iL;
+    vR[a] = mR[a] * iR;
+  }
+  const double q2L = vL[0] * vL[0] + vL[1] * vL[1] + vL[2] * vL[2];
+  const double q2R = vR[0] * vR[0] + vR[1] * vR[1] + vR[2] * vR[2];
+  const double pL = s.gam1 * (EL - 0.5 * rhoL * q2L);
+  const double pR = s.gam1 * (ER - 0.5 * rhoR * q2R);
+  const double c2L = s.gamma * pL * iL, c2R = s.gamma * pR * iR;
+  const double cL = sqrt(c2L), cR = sqrt(c2R);
+  const double HL = c2L * s.gam1_inv + 0.5 * q2L;
+  const double HR = c2R * s.gam1_inv + 0.5 * q2R;
+  const double alpha = fmax(fabs(vR[D]) + cR, fabs(vL[D]) + cL);
+  const double fL = mL[D], fR = mR[D];  // mass fluxes rho*q_n
+  out[0] = 0.5 * (fL + fR - alpha * (rhoR - rhoL));
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    double pf = (a == D) ? (pL + pR) : 0.0;
+    out[1 + a] = 0.5 * (fL * vL[a] + fR * vR[a] + pf - alpha * (mR[a] - mL[a]));
+  }
+  out[4] = 0.5 * (fL * HL + fR * HR - alpha * (ER - EL));
+}
+
+template <int D>
+__global__ void __launch_bounds__(TILE_THREADS) k_inviscid(const SolveDev* __restrict__ solves,
+                                                           const TileRef* __restrict__ tiles, int ntiles,
+                                                           int stage) {
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    TileCell tc = tile_cell(tiles[t], 0);
+    const SolveDev& s = solves[tc.s];
+    if (!s.ctl->active) continue;
+    if (tc.i >= s.IM || tc.j >= s.JM) continue;
+    const double* U = stage == 1 ? s.Q : s.Qp;
+    double f[NEQ];
+    face_flux<D>(s, U, pad_off(s, tc.i, tc.j, tc.k), f);
+    const long long fo = int_off(s, tc.i, tc.j, tc.k);
+    double* F = s.F[D];
+#pragma unroll
+    for (int n = 0; n < NEQ; ++n) F[n * s.IV + fo] = f[n];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Viscous fluxes on the NGV ring (src/calc_gradient.cpp:17-66,
+// src/Block3d.cpp:750-868).  d/dx f = ((f[-2]-f[+2])/12 + (f[+1]-f[-1])*2/3) / dx.
+
+__device__ __forceinline__ double d4(const double* __restrict__ f, long long o, long long st, double inv_h) {
+  const double c12 = 1.0 / 12.0, c23 = 2.0 / 3.0;
+  return ((f[o - 2 * st] - f[o + 2 * st]) * c12 + (f[o + st] - f[o - st]) * c23) * inv_h;
+}
+
+__global__ void __launch_bounds__(TILE_THREADS) k_viscous(const SolveDev* __restrict__ solves,
+                                                          const TileRef* __restrict__ tiles, int ntiles) {
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    TileCell tc = tile_cell(tiles[t], -NGV);
+    const SolveDev& s = solves[tc.s];
+    if (!s.ctl->active) continue;
+    if (tc.i >= s.IM + NGV || tc.j >= s.JM + NGV) continue;
+    const long long o = pad_off(s, tc.i, tc.j, tc.k);
+    const long long sy = s.nx, sz = (long long)s.nx * s.ny;
+    const double ux = d4(s.u, o, 1, s.inv_dx), uy = d4(s.u, o, sy, s.inv_dy), uz = d4(s.u, o, sz, s.inv_dz);
+    const double vx = d4(s.v, o, 1, s.inv_dx), vy = d4(s.v, o, sy, s.inv_dy), vz = d4(s.v, o, sz, s.inv_dz);
+    const double wx = d4(s.w, o, 1, s.inv_dx), wy = d4(s.w, o, sy, s.inv_dy), wz = d4(s.w, o, sz, s.inv_dz);
+    const double Tx = d4(s.T, o, 1, s.inv_dx), Ty = d4(s.T, o, sy, s.inv_dy), Tz = d4(s.T, o, sz, s.inv_dz);
+    const double Tl = s.T[o];
+    // Sutherland's law, (1 + C) / (T + C) * T^1.5 (src/Block3d.cpp:777).
+    const double mu = (1.0 + s.C_T_inf) * Tl * sqrt(Tl) / (Tl + s.C_T_inf);
+    if (tc.i >= 0 && tc.i < s.IM && tc.j >= 0 && tc.j < s.JM && tc.k >= 0 && tc.k < s.KM) s.mu[o] = mu;
+    const double mr = mu * s.Re_inv;
+    const double m23 = (2.0 / 3.0) * mr;
+    const double txx = m23 * (2.0 * ux - vy - wz);
+    const double tyy = m23 * (2.0 * vy - ux - wz);
+    const double tzz = m23 * (2.0 * wz - ux - vy);
+    const double txy = mr * (uy + vx);
+    const double txz = mr * (uz + wx);
+    const double tyz = mr * (vz + wy);
+    const double mk = mr * s.kappa;
+    const double uu = s.u[o], vv = s.v[o], ww = s.w[o];
+    const long long r = ring_off(s, tc.i, tc.j, tc.k);
+    const long long RV = s.RV;
+    double* Ev = s.Fv[0];
+    double* Fv = s.Fv[1];
+    double* Gv = s.Fv[2];
+    Ev[r] = txx;
+    Ev[RV + r] = txy;
+    Ev[2 * RV + r] = txz;
+    Ev[3 * RV + r] = uu * txx + vv * txy + ww * txz - mk * Tx;
+    Fv[r] = txy;
+    Fv[RV + r] = tyy;
+    Fv[2 * RV + r] = tyz;
+    Fv[3 * RV + r] = uu * txy + vv * tyy + ww * tyz - mk * Ty;
+    Gv[r] = txz;
+    Gv[RV + r] = tyz;
+    Gv[2 * RV + r] = tzz;
+    Gv[3 * RV + r] = uu * txz + vv * tyz + ww * tzz - mk * Tz;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// RK3 stage update fused with the periodic ghost fill and the primitive
+// recovery (src/Block3d.cpp:870-962, src/boundary_condition.cpp:4-231,
+// src/Block3d.cpp:359-385).  Each interior cell writes its new state and
+// primitives to itself and to every ghost cell that is its periodic image, which
+// is exactly what the reference's x, y, z halo sweeps leave there.
+
+__global__ void __launch_bounds__(TILE_THREADS) k_update(const SolveDev* __restrict__ solves,
+                                                         const TileRef* __restrict__ tiles, int ntiles,
+                                                         int stage) {
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    TileCell tc = tile_cell(tiles[t], 0);
+    const SolveDev& s = solves[tc.s];
+    SolveCtl* ctl = s.ctl;
+    if (!ctl->active) continue;
+    const int i = tc.i, j = tc.j, k = tc.k;
+    if (i >= s.IM || j >= s.JM) continue;
+    const double dt = ctl->dt;
+    const long long o = pad_off(s, i, j, k);
+    const long long fo = int_off(s, i, j, k);
+    const long long fx = int_off(s, i + 1 == s.IM ? 0 : i + 1, j, k);
+    const long long fy = int_off(s, i, j + 1 == s.JM ? 0 : j + 1, k);
+    const long long fz = int_off(s, i, j, k + 1 == s.KM ? 0 : k + 1);
+    const long long r = ring_off(s, i, j, k);
+    const long long ry = s.rx, rz = (long long)s.rx * s.ry;
+    const long long IV = s.IV, V = s.V, RV = s.RV;
+
+    double qn[NEQ];
+#pragma unroll
+    for (int n = 0; n < NEQ; ++n) {
+      double df = (s.F[0][n * IV + fx] - s.F[0][n * IV + fo]) * s.inv_dx +
+                  (s.F[1][n * IV + fy] - s.F[1][n * IV + fo]) * s.inv_dy +
+                  (s.F[2][n * IV + fz] - s.F[2][n * IV + fo]) * s.inv_dz;
+      if (n > 0) {
+        const double* Ev = s.Fv[0] + (n - 1) * RV;
+        const double* Fv = s.Fv[1] + (n - 1) * RV;
+        const double* Gv = s.Fv[2] + (n - 1) * RV;
+        // -(d/dx) of the viscous fluxes, as 4th-order central differences
+        // (src/Block3d.cpp:887-910): ((f[-2]-f[+2])/12 + (f[+1]-f[-1])*2/3) / h.
+        double dv = d4(Ev, r, 1, s.inv_dx) + d4(Fv, r, ry, s.inv_dy) + d4(Gv, r, rz, s.inv_dz);
+        df -= dv;
+      }
+      const double q0 = s.Q[n * V + o];
+      if (stage == 1) {
+        qn[n] = q0 - dt * df;
+      } else if (stage == 2) {
+        qn[n] = 0.75 * q0 + 0.25 * (s.Qp[n * V + o] - dt * df);
+      } else {
+        qn[n] = (q0 + 2.0 * (s.Qp[n * V + o] - dt * df)) * (1.0 / 3.0);
+      }
+    }
+    double* out = stage == 3 ? s.Q : s.Qp;
+
+    // Primitives of the new state (once), then the cell and its ghost images.
+    const double ir = 1.0 / qn[0];
+    const double uu = qn[1] * ir, vv = qn[2] * ir, ww = qn[3] * ir;
+    const double q2 = uu * uu + vv * vv + ww * ww;
+    const double pp = s.gam1 * (qn[4] - 0.5 * qn[0] * q2);
+    const double TT = s.gM2 * pp * ir;
+    const double sr = sqrt(qn[0]);
+    const double HH = s.gamma * s.gam1_inv * pp * ir + 0.5 * q2;
+    if (!(qn[0] > 0.0) || !(pp > 0.0)) atomicOr(&ctl->status, 1);
+
+    int xi[3], yi[3], zi[3];
+    int nxi = 0, nyi = 0, nzi = 0;
+    xi[nxi++] = i;
+    if (i < NG) xi[nxi++] = i + s.IM;
+    if (i >= s.IM - NG) xi[nxi++] = i - s.IM;
+    yi[nyi++] = j;
+    if (j < NG) yi[nyi++] = j + s.JM;
+    if (j >= s.JM - NG) yi[nyi++] = j - s.JM;
+    zi[nzi++] = k;
+    if (k < NG) zi[nzi++] = k + s.KM;
+    if (k >= s.KM - NG) zi[nzi++] = k - s.KM;
+    for (int c3 = 0; c3 < nzi; ++c3)
+      for (int b2 = 0; b2 < nyi; ++b2)
+        for (int a1 = 0; a1 < nxi; ++a1) {
+          const long long d = pad_off(s, xi[a1], yi[b2], zi[c3]);
+#pragma unroll
+          for (int n = 0; n < NEQ; ++n) out[n * V + d] = qn[n];
+          s.rho[d] = qn[0];
+          s.u[d] = uu;
+          s.v[d] = vv;
+          s.w[d] = ww;
+          s.p[d] = pp;
+          s.T[d] = TT;
+          s.srho[d] = sr;
+          s.H[d] = HH;
+        }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Diagnostics (project-defined): kinetic energy and enstrophy with compensated
+// binary64 sums.  Each CTA reduces its tiles to one (sum, error) pair per
+// quantity in `partials` (scratch, 4 doubles per CTA); k_diag_finalize folds them
+// in a fixed order, so the result is deterministic.
+
+struct Comp {
+  double s, e;
+};
+
+__device__ __forceinline__ Comp comp_add(Comp a, Comp b) {
+  double t = a.s + b.s;
+  double z = t - a.s;
+  double err = (a.s - (t - z)) + (b.s - z);
+  Comp r;
+  r.s = t;
+  r.e = a.e + b.e + err;
+  return r;
+}
+
+__device__ __forceinline__ Comp warp_comp(Comp v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    Comp other;
+    other.s = __shfl_down_sync(0xffffffffu, v.s, o);
+    other.e = __shfl_down_sync(0xffffffffu, v.e, o);
+    v = comp_add(v, other);
+  }
+  return v;
+}
+
+__device__ __forceinline__ double vel(const double* Q, long long V, long long o, int n) {
+  return Q[n * V + o] / Q[o];
+}
+__device__ __forceinline__ double dvel(const double* Q, long long V, long long o, long long st, int n,
+                                       double inv_h) {
+  const double c12 = 1.0 / 12.0, c23 = 2.0 / 3.0;
+  return ((vel(Q, V, o - 2 * st, n) - vel(Q, V, o + 2 * st, n)) * c12 +
+          (vel(Q, V, o + st, n) - vel(Q, V, o - st, n)) * c23) * inv_h;
+}
+
+__global__ void __launch_bounds__(TILE_THREADS) k_diag(const SolveDev* __restrict__ solves, int sidx,
+                                                       const TileRef* __restrict__ tiles, int ntiles,
+                                                       double* __restrict__ partials) {
+  __shared__ Comp red[2][TILE_THREADS / 32];
+  const SolveDev& s = solves[sidx];
+  Comp ke{0.0, 0.0}, en{0.0, 0.0};
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    TileCell tc = tile_cell(tiles[t], 0);
+    if (tc.i >= s.IM || tc.j >= s.JM) continue;
+    const long long o = pad_off(s, tc.i, tc.j, tc.k);
+    const long long V = s.V, sy = s.nx, sz = (long long)s.nx * s.ny;
+    const double* Q = s.Q;
+    const double r = Q[o];
+    const double u = vel(Q, V, o, 1), v = vel(Q, V, o, 2), w = vel(Q, V, o, 3);
+    const double wxc = dvel(Q, V, o, sy, 3, s.inv_dy) - dvel(Q, V, o, sz, 2, s.inv_dz);
+    const double wyc = dvel(Q, V, o, sz, 1, s.inv_dz) - dvel(Q, V, o, 1, 3, s.inv_dx);
+    const double wzc = dvel(Q, V, o, 1, 2, s.inv_dx) - dvel(Q, V, o, sy, 1, s.inv_dy);
+    ke = comp_add(ke, Comp{0.5 * r * (u * u + v * v + w * w), 0.0});
+    en = comp_add(en, Comp{0.5 * r * (wxc * wxc + wyc * wyc + wzc * wzc), 0.0});
+  }
+  ke = warp_comp(ke);
+  en = warp_comp(en);
+  if ((threadIdx.x & 31) == 0) {
+    red[0][threadIdx.x >> 5] = ke;
+    red[1][threadIdx.x >> 5] = en;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    Comp a = red[0][0], b = red[1][0];
+    for (int q = 1; q < TILE_THREADS / 32; ++q) {
+      a = comp_add(a, red[0][q]);
+      b = comp_add(b, red[1][q]);
+    }
+    partials[4 * blockIdx.x + 0] = a.s;
+    partials[4 * blockIdx.x + 1] = a.e;
+    partials[4 * blockIdx.x + 2] = b.s;
+    partials[4 * blockIdx.x + 3] = b.e;
+  }
+}
+
+__global__ void k_diag_finalize(const double* __restrict__ partials, int nparts, double inv_n,
+                                double* __restrict__ out) {
+  __shared__ Comp red[2][32];
+  Comp ke{0.0, 0.0}, en{0.0, 0.0};
+  for (int q = threadIdx.x; q < nparts; q += blockDim.x) {
+    ke = comp_add(ke, Comp{partials[4 * q], partials[4 * q + 1]});
+    en = comp_add(en, Comp{partials[4 * q + 2], partials[4 * q + 3]});
+  }
+  ke = warp_comp(ke);
+  en = warp_comp(en);
+  if ((threadIdx.x & 31) == 0) {
+    red[0][threadIdx.x >> 5] = ke;
+    red[1][threadIdx.x >> 5] = en;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    Comp a = red[0][0], b = red[1][0];
+    for (int q = 1; q < (int)(blockDim.x / 32); ++q) {
+      a = comp_add(a, red[0][q]);
+      b = comp_add(b, red[1][q]);
+    }
+    out[0] = (a.s + a.e) * inv_n;
+    out[1] = (b.s + b.e) * inv_n;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Host-side launchers.  Each launch is bracketed by the profiler's events when
+// profiling is on (pf may be null).
+
+static int grid_for(int ntiles, int max_ctas) {
+  if (ntiles <= 0) return 0;
+  return max_ctas > 0 && ntiles > max_ctas ? max_ctas : ntiles;
+}
+
+#define CBNS_LAUNCH(pf, id, st, ...) \
+  do {                               \
+    if (pf) (pf)->before(id, st);    \
+    __VA_ARGS__;                     \
+    if (pf) (pf)->after(st);         \
+  } while (0)
+
+cudaError_t launch_prepare(const SolveDev* d, const TileRef* tiles, int ntiles, cudaStream_t st, Profiler* pf) {
+  if (ntiles == 0) return cudaSuccess;
+  CBNS_LAUNCH(pf, KID_PREPARE, st, (k_prepare<<<grid_for(ntiles, 0), TILE_THREADS, 0, st>>>(d, tiles, ntiles)));
+  return cudaGetLastError();
+}
+
+cudaError_t launch_layout(const SolveDev* d, int sidx, const double* src, double* dst, bool to_soa,
+                          long long V, cudaStream_t st, Profiler* pf) {
+  int blocks = (int)((V + 255) / 256);
+  if (blocks > 65535) blocks = 65535;
+  if (to_soa)
+    CBNS_LAUNCH(pf, KID_LAYOUT, st, (k_aos_to_soa<<<blocks, 256, 0, st>>>(d, sidx, src, dst)));
+  else
+    CBNS_LAUNCH(pf, KID_LAYOUT, st, (k_soa_to_aos<<<blocks, 256, 0, st>>>(d, sidx, src, dst)));
+  return cudaGetLastError();
+}
+
+cudaError_t launch_dt(const SolveDev* d, int nsolves, const TileRef* tiles, int ntiles, double t_end,
+                      bool use_t_end, cudaStream_t st, Profiler* pf) {
+  if (ntiles > 0)
+    CBNS_LAUNCH(pf, KID_DT_REDUCE, st,
+                (k_dt_reduce<<<grid_for(ntiles, 0), TILE_THREADS, 0, st>>>(d, tiles, ntiles, t_end,
+                                                                           use_t_end ? 1 : 0, 1)));
+  CBNS_LAUNCH(pf, KID_DT_FINALIZE, st,
+              (k_dt_finalize<<<(nsolves + 127) / 128, 128, 0, st>>>(d, nsolves, t_end, use_t_end ? 1 : 0)));
+  return cudaGetLastError();
+}
+
+cudaError_t launch_dt_raw(const SolveDev* d, int sidx, const TileRef* tiles, int ntiles, double* out,
+                          cudaStream_t st, Profiler* pf) {
+  if (ntiles > 0)
+    CBNS_LAUNCH(pf, KID_DT_REDUCE, st,
+                (k_dt_reduce<<<grid_for(ntiles, 0), TILE_THREADS, 0, st>>>(d, tiles, ntiles, 0.0, 0, 0)));
+  CBNS_LAUNCH(pf, KID_DT_FINALIZE, st, (k_dt_raw<<<1, 1, 0, st>>>(d, sidx, out)));
+  return cudaGetLastError();
+}
+
+cudaError_t launch_set_dt(const SolveDev* d, int sidx, double dt, cudaStream_t st) {
+  k_set_dt<<<1, 1, 0, st>>>(d, sidx, dt);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_stage(const SolveDev* d, const TileRef* tiles, int ntiles, const TileRef* ring_tiles,
+                         int nring, int stage, int max_ctas, cudaStream_t st, Profiler* pf) {
+  if (ntiles == 0) return cudaSuccess;
+  const int g = grid_for(ntiles, max_ctas);
+  CBNS_LAUNCH(pf, KID_INVISCID_X, st, (k_inviscid<0><<<g, TILE_THREADS, 0, st>>>(d, tiles, ntiles, stage)));
+  CBNS_LAUNCH(pf, KID_INVISCID_Y, st, (k_inviscid<1><<<g, TILE_THREADS, 0, st>>>(d, tiles, ntiles, stage)));
+  CBNS_LAUNCH(pf, KID_INVISCID_Z, st, (k_inviscid<2><<<g, TILE_THREADS, 0, st>>>(d, tiles, ntiles, stage)));
+  CBNS_LAUNCH(pf, KID_VISCOUS, st,
+              (k_viscous<<<grid_for(nring, max_ctas), TILE_THREADS, 0, st>>>(d, ring_tiles, nring)));
+  CBNS_LAUNCH(pf, KID_UPDATE, st, (k_update<<<g, TILE_THREADS, 0, st>>>(d, tiles, ntiles, stage)));
+  return cudaGetLastError();
+}
+
+cudaError_t launch_diag(const SolveDev* d, int sidx, const TileRef* tiles, int ntiles, double* partials,
+                        int nparts, double inv_n, double* out, cudaStream_t st, Profiler* pf) {
+  CBNS_LAUNCH(pf, KID_DIAG, st, (k_diag<<<nparts, TILE_THREADS, 0, st>>>(d, sidx, tiles, ntiles, partials)));
+  CBNS_LAUNCH(pf, KID_DIAG, st, (k_diag_finalize<<<1, 1024, 0, st>>>(partials, nparts, inv_n, out)));
+  return cudaGetLastError();
+}
+
+}  // namespace cbns

@@ -1,0 +1,60 @@
+// cbns_probe.cu — pipe-throughput probes used as roofline denominators.
+//
+// The binary64 stencil kernels are bound by the FP64 pipe, whose peak no
+// vendor table gives for this part, so it is measured here: each thread runs
+// eight independent FMA chains for a fixed count, on 8 CTAs of 256 threads per
+// SM, timed with CUDA events.  FLOPs count 2 per FMA.
+#include <cuda_runtime.h>
+
+#include "../../include/cbns_gpu.h"
+
+namespace {
+
+template <typename T>
+__global__ void k_fma_chains(T* out, int iters, T a, T b) {
+  T x0 = (T)threadIdx.x * (T)1e-3, x1 = x0 + (T)1, x2 = x0 + (T)2, x3 = x0 + (T)3;
+  T x4 = x0 + (T)4, x5 = x0 + (T)5, x6 = x0 + (T)6, x7 = x0 + (T)7;
+  for (int it = 0; it < iters; ++it) {
+    x0 = x0 * a + b; x1 = x1 * a + b; x2 = x2 * a + b; x3 = x3 * a + b;
+    x4 = x4 * a + b; x5 = x5 * a + b; x6 = x6 * a + b; x7 = x7 * a + b;
+  }
+  out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+}
+
+template <typename T>
+cbns_status probe(int iters, double* tflops) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, dev) != cudaSuccess) return CBNS_ERR_CUDA;
+  const int blocks = prop.multiProcessorCount * 8, threads = 256;
+  T* out = nullptr;
+  if (cudaMalloc(&out, sizeof(T) * blocks * threads) != cudaSuccess) return CBNS_ERR_OUT_OF_MEMORY;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float best = 1e30f;
+  for (int rep = 0; rep < 3; ++rep) {
+    cudaEventRecord(e0);
+    k_fma_chains<T><<<blocks, threads>>>(out, iters, (T)0.999999, (T)1e-7);
+    cudaEventRecord(e1);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms < best) best = ms;
+  }
+  cudaError_t err = cudaGetLastError();
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  if (err != cudaSuccess) return CBNS_ERR_CUDA;
+  *tflops = 2.0 * 8.0 * (double)blocks * threads * iters / (best * 1e-3) * 1e-12;
+  return CBNS_OK;
+}
+
+}  // namespace
+
+extern "C" cbns_status cbns_probe_peak(int fp64, double* tflops) {
+  if (!tflops) return CBNS_ERR_INVALID_ARG;
+  return fp64 ? probe<double>(4096, tflops) : probe<float>(65536, tflops);
+}

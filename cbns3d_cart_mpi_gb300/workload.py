@@ -1,0 +1,54 @@
+"""Algorithmic work of the hot path, pinned by counting the reference's own operations.
+
+The per-unit figures are FLOPs (each +, -, *, / and sqrt on a binary64 value, as
+written in the reference's source) that the reference executes per unit of
+each hot-path function.  They were counted by compiling the reference's
+sources with value_type replaced by an op-counting type (oracle/opcount/) and
+are recorded in tests/golden/opcount.txt; a test checks these constants
+against that record.
+"""
+FLOPS_PER_FACE = 1570            # rec_riemann_x/y/z, per face (src/Block3d.cpp:555-748)
+FLOPS_VISC_TERMS_PER_RING = 129  # calc_viscous_terms incl. 4 calc_gradient, per NGV-ring point
+FLOPS_VISC_FLUX_PER_RING = 18    # calc_viscous_flux, per NGV-ring point
+FLOPS_VISC_DIV_PER_CELL = 104    # divergence in calc_viscous_flux_contribution, per cell
+FLOPS_UPDATE_PER_CELL = 54       # update_rk3, per cell
+FLOPS_PRIM_PER_PADDED = 14       # calc_primitive, per padded cell
+FLOPS_DT_PER_CELL = 31           # calc_dt, per cell (plus a data-dependent re-add)
+
+NG, NGV = 4, 2
+
+
+def faces_per_direction(IM, JM, KM, d):
+    """Faces the reference computes per direction: (IM+1)*JM*KM for x, etc."""
+    ext = [IM, JM, KM]
+    ext[d] += 1
+    return ext[0] * ext[1] * ext[2]
+
+
+def kernel_flops(name, IM, JM, KM):
+    """Algorithmic FLOPs of one launch of the named kernel (one solve)."""
+    cells = IM * JM * KM
+    ring = (IM + 2 * NGV) * (JM + 2 * NGV) * (KM + 2 * NGV)
+    padded = (IM + 2 * NG) * (JM + 2 * NG) * (KM + 2 * NG)
+    if name.startswith("inviscid_"):
+        d = "xyz".index(name[-1])
+        return FLOPS_PER_FACE * faces_per_direction(IM, JM, KM, d)
+    if name == "viscous":
+        return (FLOPS_VISC_TERMS_PER_RING + FLOPS_VISC_FLUX_PER_RING) * ring
+    if name == "update":
+        return (FLOPS_VISC_DIV_PER_CELL + FLOPS_UPDATE_PER_CELL) * cells + FLOPS_PRIM_PER_PADDED * padded
+    if name == "dt_reduce":
+        return FLOPS_DT_PER_CELL * cells
+    return 0
+
+
+def flops_per_step(IM, JM, KM):
+    """Algorithmic FLOPs of one RK3 step (3 stages + calc_dt)."""
+    stage = sum(kernel_flops(n, IM, JM, KM) for n in ("inviscid_x", "inviscid_y", "inviscid_z", "viscous", "update"))
+    return 3 * stage + kernel_flops("dt_reduce", IM, JM, KM)
+
+
+def state_bytes_per_step(IM, JM, KM):
+    """Minimum HBM traffic of one step: read Q, write Q_p (stage 1); read Q, Q_p,
+    write one (stages 2, 3) -> 320 B per cell (binary64, 5 fields)."""
+    return 320 * IM * JM * KM

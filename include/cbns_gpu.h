@@ -1,0 +1,173 @@
+/*
+ * cbns_gpu.h — C ABI of the GB300 (sm_103a) right-hand-side library for the
+ * cbns3d compressible Navier-Stokes solver.
+ *
+ * One handle is one Block3d-equivalent solve living in device memory.  The
+ * library owns every device allocation behind the opaque handle; the caller
+ * keeps its host arrays (the reference allocates them in Block3d::allocate_mem,
+ * src/Block3d.cpp:41-135) and passes plain host pointers.  Nothing throws across
+ * this boundary: every entry point returns a cbns_status.
+ *
+ * Host array layouts are the reference's (include/Block3d.h:169-199):
+ *   Q          Q[n + 5*((NG+i) + IM_G*((NG+j) + JM_G*(NG+k)))], ghosts included,
+ *              IM_G = IM + 2*NG, NG = 4   (get_idx_Q)
+ *   primitives f[(NG+i) + IM_G*((NG+j) + JM_G*(NG+k))]            (get_idx)
+ *
+ * Threading: one handle per host thread at a time; each handle runs on its own
+ * CUDA stream.  Batch entry points take a set of handles and launch their
+ * stages together.
+ */
+#ifndef CBNS_GPU_H
+#define CBNS_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CBNS_NEQ 5 /* equations, include/constants.h:13 */
+#define CBNS_NG 4  /* ghost layers of Q and primitives, include/constants.h:15-17 */
+#define CBNS_NGV 2 /* ghost layers of gradients, include/constants.h:16 */
+
+typedef enum cbns_status {
+  CBNS_OK = 0,
+  CBNS_FINISHED = 1,              /* t_cur + 1e-5 > t_end: no step taken (Block3d::is_finished) */
+  CBNS_ERR_INVALID_ARG = -1,      /* null pointer, unknown stage/precision, bad parameter */
+  CBNS_ERR_BAD_DIMS = -2,         /* a block dimension below CBNS_NG or above the limit */
+  CBNS_ERR_CUDA = -3,             /* a CUDA runtime call failed; see cbns_last_error() */
+  CBNS_ERR_OUT_OF_MEMORY = -4,    /* device allocation failed */
+  CBNS_ERR_NONPHYSICAL = -5,      /* a stage produced rho <= 0, p <= 0 or a NaN */
+  CBNS_ERR_TIMEOUT = -6,          /* a bounded device-side wait gave up */
+  CBNS_ERR_NO_DEVICE = -7,        /* no CUDA device, or not an sm_103 device */
+  CBNS_ERR_IO = -8,               /* host file could not be read or written */
+  CBNS_ERR_FORMAT = -9            /* host file is truncated or its dimensions do not match */
+} cbns_status;
+
+typedef enum cbns_precision {
+  CBNS_FP64 = 0,       /* every operation in IEEE binary64 */
+  CBNS_FP32_MIXED = 1  /* WENO, projections and fluxes in binary32; state, RK3 and sums in binary64 */
+} cbns_precision;
+
+/*
+ * Simulation parameters: the fields of SimulationParams
+ * (include/simulation_params.h:15-53), in the order read_input() reads them
+ * from input.txt (src/read_input.cpp:24-72), then the derived constants of
+ * src/read_input.cpp:78-90 (filled by cbns_params_derive).
+ */
+typedef struct cbns_params {
+  char checkpoint_fname[256];
+  double CFL;
+  double t_cur;
+  double t_end;
+  double Pr;
+  double gamma;
+  double Mach;
+  double Re;
+  double T_inf;
+  double L; /* read but unused, as in the reference */
+  uint32_t IM, JM, KM;
+  uint32_t nstep_max;
+  uint32_t checkpoint_freq;
+  uint32_t num_output;
+  int32_t is_restart; /* 1 = start from the initial condition, 0 = read the checkpoint */
+  /* derived */
+  double Mach2, Re_inv, Pr_inv, gam1, gM2, gam1_inv, p_inf, C_T_inf, C_dt_v;
+} cbns_params;
+
+typedef struct cbns_handle cbns_handle;
+
+/* Derived constants of src/read_input.cpp:78-90. */
+cbns_status cbns_params_derive(cbns_params* p);
+
+/* Block3d::Block3d + allocate_mem (src/Block3d.cpp:11-135) and gen_mesh's spacing
+ * (src/Block3d.cpp:208-219): dx = 2*pi/p->IM etc.  IM, JM, KM are this block's
+ * extents (the whole grid on one GPU).  Selects device 0 unless CBNS_DEVICE is set. */
+cbns_status cbns_create(const cbns_params* p, uint32_t IM, uint32_t JM, uint32_t KM,
+                        int precision, cbns_handle** out);
+cbns_status cbns_destroy(cbns_handle* h);
+
+/* Upload the conserved state (get_idx_Q layout, ghosts ignored and refilled) and
+ * run the start-up sequence of src/cbns3d.cpp:149-153: boundary_condition(Q),
+ * calc_primitive(Q), init_Q_p().  mu is reset to 1 in the interior, the value
+ * Block3d::initial_condition gives it (src/Block3d.cpp:265).  Sets t_cur = t. */
+cbns_status cbns_upload_Q(cbns_handle* h, const double* Q, double t);
+
+/* Block3d::get_Q / get_Q_p (src/Block3d.cpp:302-316): copy Q or Q_p, ghosts
+ * included, into a host array of NEQ*IM_G*JM_G*KM_G doubles. */
+cbns_status cbns_download_Q(cbns_handle* h, double* Q);
+cbns_status cbns_download_Q_p(cbns_handle* h, double* Q_p);
+
+/* The primitive arrays of the current state (Block3d::calc_primitive,
+ * src/Block3d.cpp:359-385) in the padded get_idx layout; any pointer may be NULL. */
+cbns_status cbns_download_prims(cbns_handle* h, double* rho, double* u, double* v,
+                                double* w, double* p, double* T);
+
+/* Block3d::calc_dt (src/Block3d.cpp:515-553): CFL / max over interior cells. */
+cbns_status cbns_calc_dt(cbns_handle* h, double* dt);
+
+/* One RK3 stage with a given dt (src/cbns3d.cpp:203-240): rec_riemann_x/y/z,
+ * calc_viscous_flux_contribution, update_rk3(dt, stage), boundary_condition and
+ * calc_primitive of the stage's output.  stage is 1, 2 or 3. */
+cbns_status cbns_stage(cbns_handle* h, double dt, int stage);
+
+/* One iteration of the time loop of src/cbns3d.cpp:176-241: returns
+ * CBNS_FINISHED without stepping if t_cur + 1e-5 > t_end (Block3d::is_finished),
+ * else dt = calc_dt() clipped to t_end - t_cur, t_cur += dt, three stages.
+ * dt_out / t_out may be NULL (then the call does not wait for the device). */
+cbns_status cbns_step(cbns_handle* h, double t_end, double* dt_out, double* t_out);
+
+/* nsteps iterations of cbns_step as a replayed CUDA graph with the
+ * is_finished test, dt and t_cur kept on the device; steps taken go to
+ * *steps_done (may be NULL). */
+cbns_status cbns_run(cbns_handle* h, uint32_t nsteps, double t_end, uint32_t* steps_done);
+
+/* Current simulated time and last dt, read from the device. */
+cbns_status cbns_get_time(cbns_handle* h, double* t_cur, double* dt_last);
+
+/* Kinetic energy and enstrophy of the current state (project-defined
+ * diagnostics, absent from the reference): KE = sum(0.5*rho*|u|^2)/N,
+ * Omega = sum(0.5*rho*|curl u|^2)/N over interior cells, N = IM*JM*KM, with the
+ * 4th-order central difference of src/calc_gradient.cpp:29-64 for the curl and
+ * compensated binary64 sums. */
+cbns_status cbns_diagnostics(cbns_handle* h, double* ke, double* enstrophy);
+
+/* Device status word: CBNS_OK, or CBNS_ERR_NONPHYSICAL once any stage met
+ * rho <= 0, p <= 0 or a NaN.  Clears the word. */
+cbns_status cbns_check_state(cbns_handle* h);
+
+/* The handle's cudaStream_t (as void*), for callers that time or order work. */
+void* cbns_stream(cbns_handle* h);
+
+/* Block extents and device bytes the handle holds. */
+cbns_status cbns_get_info(cbns_handle* h, uint32_t dims[3], uint64_t* device_bytes,
+                          int* precision);
+
+/* Per-kernel timing.  Between cbns_profile_begin and cbns_profile_end every kernel
+ * the handle launches is bracketed by CUDA events on its stream and launched
+ * directly rather than through the step graph.  cbns_profile_end waits for the
+ * device and fills up to cap records, one per kernel name, *n set to the count. */
+typedef struct cbns_kernel_time {
+  char name[32];
+  uint32_t launches;
+  double total_ms;
+} cbns_kernel_time;
+cbns_status cbns_profile_begin(cbns_handle* h);
+cbns_status cbns_profile_end(cbns_handle* h, cbns_kernel_time* out, int cap, int* n);
+
+/* Measured FMA throughput of the current device in TFLOP/s (2 FLOPs per FMA),
+ * binary64 when fp64 != 0 else binary32: the pipe peaks the roofline uses. */
+cbns_status cbns_probe_peak(int fp64, double* tflops);
+
+/* Text of the last error on this host thread ("" if none). */
+const char* cbns_last_error(void);
+
+/* Library version string. */
+const char* cbns_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CBNS_GPU_H */

@@ -1,0 +1,221 @@
+"""GPU path (through the C ABI) against the reference's golden states and the oracle.
+
+Tolerances, all relative to the largest magnitude of each conserved field
+(rho, rho*u, rho*v, rho*w, E):
+  * 1e-13 after one stage or a few steps on small grids (the GPU kernels reorder
+    binary64 operations — shared projections, one division per five WENO weights,
+    fused multiply-adds — so they differ from the reference by rounding only);
+  * 1e-11 after 100 RK3 steps at 64^3 (the spec parity bar), and 1e-10 on
+    the kinetic-energy and enstrophy histories.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from cbns3d_cart_mpi_gb300._abi import CBNS_ERR_BAD_DIMS, CBNS_ERR_NONPHYSICAL, NG, tgv_params
+
+pytestmark = [pytest.mark.gpu, pytest.mark.usefixtures("built")]
+
+FIELDS = ["rho", "rho*u", "rho*v", "rho*w", "E"]
+
+
+def load(golden_dir, name):
+    return np.load(os.path.join(golden_dir, name))
+
+
+def pad(Qi):
+    KM, JM, IM, _ = Qi.shape
+    Q = np.zeros((KM + 2 * NG, JM + 2 * NG, IM + 2 * NG, 5))
+    Q[NG:-NG, NG:-NG, NG:-NG] = Qi
+    return Q
+
+
+def interior(Q):
+    return Q[NG:-NG, NG:-NG, NG:-NG]
+
+
+def rel_linf(a, b):
+    """Per-field max|a-b| / max|b| over the last axis."""
+    a = a.reshape(-1, 5)
+    b = b.reshape(-1, 5)
+    return np.abs(a - b).max(axis=0) / np.abs(b).max(axis=0)
+
+
+def assert_close(a, b, tol, what=""):
+    err = rel_linf(a, b)
+    assert (err <= tol).all(), "%s rel Linf %s > %g" % (what, dict(zip(FIELDS, err)), tol)
+
+
+def solver_from(Qi, params):
+    from cbns3d_cart_mpi_gb300.solver import Solver
+    s = Solver(params)
+    s.upload_Q(pad(Qi), 0.0)
+    return s
+
+
+def test_upload_ghost_fill_and_prims(golden_dir):
+    from oracle.oracle import OracleBlock
+    g = load(golden_dir, "tgv16.npz")
+    p = tgv_params(16)
+    s = solver_from(g["Q0"], p)
+    o = OracleBlock(p)
+    o.set_Q(pad(g["Q0"]), 0.0)
+    # Ghost fill is an exact copy: bitwise equal to the reference's halo sweeps.
+    assert np.array_equal(s.download_Q(), o.get_Q())
+    assert np.array_equal(s.download_Q_p(), o.get_Q())
+    gp, op = s.download_prims(), o.get_prims()
+    for k in ("rho", "u", "v", "w", "p", "T"):
+        np.testing.assert_allclose(gp[k], op[k], rtol=1e-15, atol=1e-15, err_msg=k)
+
+
+def test_calc_dt(golden_dir):
+    g = load(golden_dir, "tgv16.npz")
+    s = solver_from(g["Q0"], tgv_params(16))
+    assert abs(s.calc_dt() - g["dt"][0]) <= 1e-14 * g["dt"][0]
+
+
+def test_stage1(golden_dir):
+    g = load(golden_dir, "tgv16.npz")
+    s = solver_from(g["Q0"], tgv_params(16))
+    s.stage(g["dt"][0], 1)
+    assert_close(interior(s.download_Q_p()), g["Qp_stage1"], 1e-13, "stage 1")
+
+
+def test_three_steps(golden_dir):
+    g = load(golden_dir, "tgv16.npz")
+    s = solver_from(g["Q0"], tgv_params(16))
+    for n in range(3):
+        dt, t = s.step()
+        assert abs(dt - g["dt"][n]) <= 1e-14 * g["dt"][n]
+        assert abs(t - g["t"][n]) <= 1e-14 * g["t"][n]
+    assert_close(interior(s.download_Q()), g["Q3"], 1e-13, "16^3 step 3")
+
+
+@pytest.mark.parametrize("name,steps,key", [("tgv_odd.npz", 2, "Q2"), ("tgv_min.npz", 2, "Q2"),
+                                            ("tgv_pert.npz", 3, "Q3")])
+def test_cases(golden_dir, name, steps, key):
+    g = load(golden_dir, name)
+    IM, JM, KM = (int(x) for x in g["N"])
+    kw = dict(Re=float(g["Re"]), Mach=float(g["Mach"])) if "Re" in g.files else {}
+    s = solver_from(g["Q0"], tgv_params(IM, JM=JM, KM=KM, **kw))
+    for n in range(steps):
+        dt, t = s.step()
+        assert abs(dt - g["dt"][n]) <= 1e-14 * g["dt"][n]
+    assert_close(interior(s.download_Q()), g[key], 1e-13, name)
+
+
+def test_ghosts_after_step_are_periodic_images(golden_dir):
+    g = load(golden_dir, "tgv_odd.npz")
+    IM, JM, KM = (int(x) for x in g["N"])
+    s = solver_from(g["Q0"], tgv_params(IM, JM=JM, KM=KM))
+    s.step()
+    Q = s.download_Q()
+    Qi = interior(Q)
+    ix = np.arange(-NG, IM + NG) % IM
+    jx = np.arange(-NG, JM + NG) % JM
+    kx = np.arange(-NG, KM + NG) % KM
+    assert np.array_equal(Q, Qi[np.ix_(kx, jx, ix)])
+
+
+def test_history_64_100_steps(golden_dir):
+    """North-star parity: 64^3 TGV, 100 RK3 steps, against the reference's own
+    history and the oracle's full state; KE and enstrophy every 10 steps."""
+    from oracle.oracle import OracleBlock
+    from cbns3d_cart_mpi_gb300.solver import initial_condition
+    g = load(golden_dir, "tgv64_hist.npz")
+    p = tgv_params(64)
+    from cbns3d_cart_mpi_gb300.solver import Solver
+    s = Solver(p)
+    s.upload_Q(initial_condition(p), 0.0)
+    o = OracleBlock(p)
+    o.initial_condition()
+    ke0, en0 = s.diagnostics()
+    assert abs(ke0 - g["ke"][0]) <= 1e-12 * g["ke"][0]
+    assert abs(en0 - g["enstrophy"][0]) <= 1e-12 * g["enstrophy"][0]
+    for n in range(1, 101):
+        dt, t = s.step()
+        o.step()
+        assert abs(dt - g["dt"][n - 1]) <= 1e-12 * g["dt"][n - 1], n
+        if n % 10 == 0:
+            m = n // 10
+            ke, en = s.diagnostics()
+            assert abs(ke - g["ke"][m]) <= 1e-10 * g["ke"][m], (n, ke, g["ke"][m])
+            assert abs(en - g["enstrophy"][m]) <= 1e-10 * g["enstrophy"][m], (n, en, g["enstrophy"][m])
+    Qg = s.download_Q()
+    Qo = o.get_Q()
+    assert_close(interior(Qg), interior(Qo), 1e-11, "64^3 step 100 vs oracle")
+    assert_close(interior(Qg)[::4, ::4, ::4], g["Q100_sub"], 1e-11, "64^3 step 100 vs reference")
+    sums = interior(Qg).reshape(-1, 5).sum(axis=0)
+    np.testing.assert_allclose(sums, g["sums"][10], rtol=1e-11, atol=1e-9)
+
+
+def test_run_graph_matches_step_loop_and_stops_at_t_end():
+    from cbns3d_cart_mpi_gb300.solver import Solver, initial_condition
+    p = tgv_params(16, t_end=0.03)
+    Q0 = initial_condition(p)
+    a, b = Solver(p), Solver(p)
+    a.upload_Q(Q0, 0.0)
+    b.upload_Q(Q0, 0.0)
+    n = 0
+    while a.step() is not None:
+        n += 1
+    done = b.run(50)
+    assert done == n
+    ta, _ = a.time()
+    tb, _ = b.time()
+    assert ta == tb and abs(ta - 0.03) < 1e-5 + 1e-15
+    assert np.array_equal(a.download_Q(), b.download_Q())
+
+
+def test_free_stream_is_preserved():
+    """A uniform state has an exactly zero right-hand side: every face sees the
+    same stencil, so every flux difference is 0.  Stage 1 (Q - dt*0) is then
+    bitwise Q; full steps keep Q to within the rounding of the RK3 weights."""
+    from cbns3d_cart_mpi_gb300.solver import Solver
+    p = tgv_params(12, JM=8, KM=10)
+    Q = np.zeros((10 + 2 * NG, 8 + 2 * NG, 12 + 2 * NG, 5))
+    rho, u, v, w, pr = 1.1, 0.3, -0.2, 0.15, p.p_inf
+    Q[...] = [rho, rho * u, rho * v, rho * w, pr / p.gam1 + 0.5 * rho * (u * u + v * v + w * w)]
+    s = Solver(p)
+    s.upload_Q(Q, 0.0)
+    s.stage(1e-3, 1)
+    assert np.array_equal(s.download_Q_p(), Q)
+    s.upload_Q(Q, 0.0)
+    s.step()
+    s.step()
+    np.testing.assert_allclose(s.download_Q(), Q, rtol=1e-15, atol=0)
+
+
+def test_nonphysical_state_is_reported():
+    """A host-injected negative density gives a status, not a fault."""
+    from cbns3d_cart_mpi_gb300.solver import CbnsError, Solver, initial_condition
+    p = tgv_params(8)
+    Q = initial_condition(p)
+    Q[NG + 3, NG + 3, NG + 3, 0] = -1.0
+    s = Solver(p)
+    s.upload_Q(Q, 0.0)
+    with pytest.raises(CbnsError) as ei:
+        s.step()
+    assert ei.value.status == CBNS_ERR_NONPHYSICAL
+
+
+def test_bad_dims_rejected():
+    from cbns3d_cart_mpi_gb300.solver import CbnsError, Solver
+    with pytest.raises(CbnsError) as ei:
+        Solver(tgv_params(3, JM=8, KM=8))
+    assert ei.value.status == CBNS_ERR_BAD_DIMS
+
+
+def test_diagnostics_match_oracle():
+    from oracle.oracle import OracleBlock
+    from cbns3d_cart_mpi_gb300.solver import Solver, initial_condition_perturbed
+    p = tgv_params(24, JM=20, KM=16, Re=500.0, Mach=0.2)
+    Q0 = initial_condition_perturbed(p, seed=3, amp=1e-2)
+    s = Solver(p)
+    s.upload_Q(Q0, 0.0)
+    o = OracleBlock(p)
+    o.set_Q(Q0, 0.0)
+    ke, en = s.diagnostics()
+    ko, eo = o.diagnostics()
+    assert abs(ke - ko) <= 1e-13 * ko and abs(en - eo) <= 1e-13 * eo
