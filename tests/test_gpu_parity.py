@@ -1,12 +1,15 @@
 """GPU path (through the C ABI) against the reference's golden states and the oracle.
 
-Tolerances, all relative to the largest magnitude of each conserved field
-(rho, rho*u, rho*v, rho*w, E):
-  * 1e-13 after one stage or a few steps on small grids (the GPU kernels reorder
-    binary64 operations — shared projections, one division per five WENO weights,
-    fused multiply-adds — so they differ from the reference by rounding only);
-  * 1e-11 after 100 RK3 steps at 64^3 (the spec parity bar), and 1e-10 on
-    the kinetic-energy and enstrophy histories.
+Tolerances:
+  * per conserved field (rho, rho*u, rho*v, rho*w, E), max|a-b| / max|b| <= 1e-11
+    (the spec parity bar, checked after 100 RK3 steps at 64^3 and on every
+    short case); the kinetic-energy and enstrophy histories to 1e-10;
+  * on short runs also an absolute bound: max|a-b| <= 1e-13 times the field's
+    scale, where the three momentum components share the momentum scale.  The
+    per-field bound alone is loose for rho*w early on, because w starts at 0
+    (max|rho*w| is 1.4e-3 after one step at 16^3).  The GPU kernels reorder
+    binary64 operations (shared projections, one division per five WENO weights,
+    fused multiply-adds), so they differ from the reference by rounding only.
 """
 import os
 
@@ -42,9 +45,15 @@ def rel_linf(a, b):
     return np.abs(a - b).max(axis=0) / np.abs(b).max(axis=0)
 
 
-def assert_close(a, b, tol, what=""):
+def assert_close(a, b, tol, what="", tight=None):
     err = rel_linf(a, b)
     assert (err <= tol).all(), "%s rel Linf %s > %g" % (what, dict(zip(FIELDS, err)), tol)
+    if tight is not None:
+        a2, b2 = a.reshape(-1, 5), b.reshape(-1, 5)
+        scale = np.abs(b2).max(axis=0)
+        scale[1:4] = scale[1:4].max()
+        e2 = np.abs(a2 - b2).max(axis=0) / scale
+        assert (e2 <= tight).all(), "%s scaled error %s > %g" % (what, dict(zip(FIELDS, e2)), tight)
 
 
 def solver_from(Qi, params):
@@ -79,7 +88,7 @@ def test_stage1(golden_dir):
     g = load(golden_dir, "tgv16.npz")
     s = solver_from(g["Q0"], tgv_params(16))
     s.stage(g["dt"][0], 1)
-    assert_close(interior(s.download_Q_p()), g["Qp_stage1"], 1e-13, "stage 1")
+    assert_close(interior(s.download_Q_p()), g["Qp_stage1"], 1e-11, "stage 1", tight=1e-14)
 
 
 def test_three_steps(golden_dir):
@@ -89,7 +98,7 @@ def test_three_steps(golden_dir):
         dt, t = s.step()
         assert abs(dt - g["dt"][n]) <= 1e-14 * g["dt"][n]
         assert abs(t - g["t"][n]) <= 1e-14 * g["t"][n]
-    assert_close(interior(s.download_Q()), g["Q3"], 1e-13, "16^3 step 3")
+    assert_close(interior(s.download_Q()), g["Q3"], 1e-11, "16^3 step 3", tight=1e-13)
 
 
 @pytest.mark.parametrize("name,steps,key", [("tgv_odd.npz", 2, "Q2"), ("tgv_min.npz", 2, "Q2"),
@@ -102,7 +111,7 @@ def test_cases(golden_dir, name, steps, key):
     for n in range(steps):
         dt, t = s.step()
         assert abs(dt - g["dt"][n]) <= 1e-14 * g["dt"][n]
-    assert_close(interior(s.download_Q()), g[key], 1e-13, name)
+    assert_close(interior(s.download_Q()), g[key], 1e-11, name, tight=1e-13)
 
 
 def test_ghosts_after_step_are_periodic_images(golden_dir):
