@@ -20,13 +20,14 @@ namespace cbns {
 cudaError_t launch_prepare(const SolveDev* d, const TileRef* tiles, int ntiles, cudaStream_t st, Profiler* pf);
 cudaError_t launch_layout(const SolveDev* d, int sidx, const double* src, double* dst, bool to_soa,
                           long long V, cudaStream_t st, Profiler* pf);
+cudaError_t launch_prims_double(const SolveDev* d, const TileRef* tiles, int ntiles, cudaStream_t st);
 cudaError_t launch_dt(const SolveDev* d, int nsolves, const TileRef* tiles, int ntiles, double t_end,
-                      bool use_t_end, cudaStream_t st, Profiler* pf);
+                      bool use_t_end, bool mixed, cudaStream_t st, Profiler* pf);
 cudaError_t launch_dt_raw(const SolveDev* d, int sidx, const TileRef* tiles, int ntiles, double* out,
-                          cudaStream_t st, Profiler* pf);
+                          bool mixed, cudaStream_t st, Profiler* pf);
 cudaError_t launch_set_dt(const SolveDev* d, int sidx, double dt, cudaStream_t st);
 cudaError_t launch_stage(const SolveDev* d, const TileRef* tiles, int ntiles, const TileRef* ring_tiles,
-                         int nring, int stage, int max_ctas, cudaStream_t st, Profiler* pf);
+                         int nring, int stage, int max_ctas, bool mixed, cudaStream_t st, Profiler* pf);
 cudaError_t launch_diag(const SolveDev* d, int sidx, const TileRef* tiles, int ntiles, double* partials,
                         int nparts, double inv_n, double* out, cudaStream_t st, Profiler* pf);
 }  // namespace cbns
@@ -134,8 +135,6 @@ cbns_status cbns_create(const cbns_params* p, uint32_t IM, uint32_t JM, uint32_t
   *out = nullptr;
   if (precision != CBNS_FP64 && precision != CBNS_FP32_MIXED)
     return fail(CBNS_ERR_INVALID_ARG, "cbns_create: unknown precision");
-  if (precision == CBNS_FP32_MIXED)
-    return fail(CBNS_ERR_INVALID_ARG, "cbns_create: FP32-mixed precision is not available in this build");
   // The reference's halo exchange sends NG interior layers; a block narrower than
   // NG would send ghost cells.  Tile coordinates are 16-bit and padded offsets fit
   // a 31-bit index per array.
@@ -201,19 +200,30 @@ cbns_status cbns_create(const cbns_params* p, uint32_t IM, uint32_t JM, uint32_t
   h->n_pad = (int)t_pad.size();
   h->nparts = 1024;
 
-  // Arena layout.
+  // Arena layout.  Both modes hold the binary64 state (Q, Q_p, staging) and
+  // binary64 primitives; binary64 solves add binary64 face/viscous fluxes,
+  // FP32-mixed solves the binary32 perturbation state, primitives and fluxes.
+  const bool mixed = precision == CBNS_FP32_MIXED;
+  s.mixed = mixed ? 1 : 0;
   size_t off = 0;
   auto take = [&](size_t bytes) {
     size_t o = off;
     off += align_up(bytes);
     return o;
   };
-  const size_t dV = sizeof(double) * (size_t)s.V;
+  const size_t dV = sizeof(double) * (size_t)s.V, fV = sizeof(float) * (size_t)s.V;
   size_t oQ = take(NEQ * dV), oQp = take(NEQ * dV), oStage = take(NEQ * dV);
   size_t oPrim = take(9 * dV);
-  size_t oF[3], oFv[3];
-  for (int d = 0; d < 3; ++d) oF[d] = take(sizeof(double) * NEQ * (size_t)s.IV);
-  for (int d = 0; d < 3; ++d) oFv[d] = take(sizeof(double) * (NEQ - 1) * (size_t)s.RV);
+  size_t oF[3] = {0, 0, 0}, oFv[3] = {0, 0, 0}, oFf[3] = {0, 0, 0}, oFvf[3] = {0, 0, 0}, oUf = 0, oPf = 0;
+  if (!mixed) {
+    for (int d = 0; d < 3; ++d) oF[d] = take(sizeof(double) * NEQ * (size_t)s.IV);
+    for (int d = 0; d < 3; ++d) oFv[d] = take(sizeof(double) * (NEQ - 1) * (size_t)s.RV);
+  } else {
+    oUf = take(NEQ * fV);
+    oPf = take(9 * fV);
+    for (int d = 0; d < 3; ++d) oFf[d] = take(sizeof(float) * NEQ * (size_t)s.IV);
+    for (int d = 0; d < 3; ++d) oFvf[d] = take(sizeof(float) * (NEQ - 1) * (size_t)s.RV);
+  }
   size_t oCtl = take(sizeof(SolveCtl));
   size_t oDesc = take(sizeof(SolveDev));
   size_t oTi = take(sizeof(TileRef) * t_int.size());
@@ -232,20 +242,36 @@ cbns_status cbns_create(const cbns_params* p, uint32_t IM, uint32_t JM, uint32_t
   s.Qp = (double*)(A + oQp);
   h->d_stage = (double*)(A + oStage);
   double* prim = (double*)(A + oPrim);
-  s.rho = prim + 0 * s.V;
-  s.u = prim + 1 * s.V;
-  s.v = prim + 2 * s.V;
-  s.w = prim + 3 * s.V;
-  s.p = prim + 4 * s.V;
-  s.T = prim + 5 * s.V;
-  s.srho = prim + 6 * s.V;
-  s.H = prim + 7 * s.V;
-  s.mu = prim + 8 * s.V;
-  for (int d = 0; d < 3; ++d) {
-    s.F[d] = (double*)(A + oF[d]);
-    s.Fv[d] = (double*)(A + oFv[d]);
+  s.pd = PrimSet<double>{prim + 0 * s.V, prim + 1 * s.V, prim + 2 * s.V, prim + 3 * s.V, prim + 4 * s.V,
+                         prim + 5 * s.V, prim + 6 * s.V, prim + 7 * s.V, prim + 8 * s.V};
+  if (!mixed) {
+    for (int d = 0; d < 3; ++d) {
+      s.F[d] = (double*)(A + oF[d]);
+      s.Fv[d] = (double*)(A + oFv[d]);
+      s.Ff[d] = nullptr;
+      s.Fvf[d] = nullptr;
+    }
+    s.Uf = nullptr;
+    s.pf = PrimSet<float>{};
+  } else {
+    s.Uf = (float*)(A + oUf);
+    float* pfb = (float*)(A + oPf);
+    s.pf = PrimSet<float>{pfb + 0 * s.V, pfb + 1 * s.V, pfb + 2 * s.V, pfb + 3 * s.V, pfb + 4 * s.V,
+                          pfb + 5 * s.V, pfb + 6 * s.V, pfb + 7 * s.V, pfb + 8 * s.V};
+    for (int d = 0; d < 3; ++d) {
+      s.Ff[d] = (float*)(A + oFf[d]);
+      s.Fvf[d] = (float*)(A + oFvf[d]);
+      s.F[d] = nullptr;
+      s.Fv[d] = nullptr;
+    }
   }
   const cbns_params& P = h->params;
+  // Reference state of the FP32-mixed perturbation form: the reference's
+  // free stream, rho = 1, p = 1/(gamma M^2) (src/read_input.cpp:88), u = 0.
+  s.p_ref = P.p_inf;
+  s.rho_ref = P.gM2 * P.p_inf;
+  s.E_ref = P.p_inf * P.gam1_inv;
+  s.T_ref = P.gM2 * s.p_ref / s.rho_ref;
   s.gamma = P.gamma;
   s.gam1 = P.gam1;
   s.gam1_inv = P.gam1_inv;
@@ -346,8 +372,10 @@ cbns_status cbns_download_prims(cbns_handle* h, double* rho, double* u, double* 
   if (st != CBNS_OK) return st;
   const SolveDev& s = h->desc;
   const size_t bytes = sizeof(double) * (size_t)s.V;
+  // FP32-mixed solves step with binary32 primitives; form the binary64 ones of Q.
+  if (s.mixed) CBNS_CUDA(launch_prims_double(h->d_desc, h->d_tiles_pad, h->n_pad, h->stream));
   double* dst[6] = {rho, u, v, w, p, T};
-  double* src[6] = {s.rho, s.u, s.v, s.w, s.p, s.T};
+  double* src[6] = {s.pd.rho, s.pd.u, s.pd.v, s.pd.w, s.pd.p, s.pd.T};
   for (int a = 0; a < 6; ++a)
     if (dst[a]) CBNS_CUDA(cudaMemcpyAsync(dst[a], src[a], bytes, cudaMemcpyDeviceToHost, h->stream));
   CBNS_CUDA(cudaStreamSynchronize(h->stream));
@@ -358,7 +386,7 @@ cbns_status cbns_calc_dt(cbns_handle* h, double* dt) {
   cbns_status st = check_handle(h, "cbns_calc_dt");
   if (st != CBNS_OK) return st;
   if (!dt) return fail(CBNS_ERR_INVALID_ARG, "cbns_calc_dt: null output");
-  CBNS_CUDA(launch_dt_raw(h->d_desc, 0, h->d_tiles_int, h->n_int, h->d_out, h->stream, h->pf()));
+  CBNS_CUDA(launch_dt_raw(h->d_desc, 0, h->d_tiles_int, h->n_int, h->d_out, h->desc.mixed != 0, h->stream, h->pf()));
   CBNS_CUDA(cudaMemcpyAsync(h->h_out, h->d_out, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   CBNS_CUDA(cudaStreamSynchronize(h->stream));
   *dt = h->h_out[0];
@@ -366,8 +394,8 @@ cbns_status cbns_calc_dt(cbns_handle* h, double* dt) {
 }
 
 static cbns_status enqueue_stage(cbns_handle* h, int stage) {
-  CBNS_CUDA(launch_stage(h->d_desc, h->d_tiles_int, h->n_int, h->d_tiles_ring, h->n_ring, stage, 0, h->stream,
-                         h->pf()));
+  CBNS_CUDA(launch_stage(h->d_desc, h->d_tiles_int, h->n_int, h->d_tiles_ring, h->n_ring, stage, 0,
+                         h->desc.mixed != 0, h->stream, h->pf()));
   return CBNS_OK;
 }
 
@@ -382,7 +410,8 @@ cbns_status cbns_stage(cbns_handle* h, double dt, int stage) {
 }
 
 static cbns_status enqueue_step(cbns_handle* h, double t_end, bool use_t_end) {
-  CBNS_CUDA(launch_dt(h->d_desc, 1, h->d_tiles_int, h->n_int, t_end, use_t_end, h->stream, h->pf()));
+  CBNS_CUDA(launch_dt(h->d_desc, 1, h->d_tiles_int, h->n_int, t_end, use_t_end, h->desc.mixed != 0, h->stream,
+                      h->pf()));
   for (int s = 1; s <= 3; ++s) {
     cbns_status st = enqueue_stage(h, s);
     if (st != CBNS_OK) return st;

@@ -39,6 +39,23 @@ struct SolveCtl {
   int pad;
 };
 
+// Cell-centred primitive fields of a stage input.  Binary64 solves store them
+// absolute; FP32-mixed solves store rho, u, v, w, sqrt(rho), H and mu absolute
+// but p and T as perturbations p - p_ref, T - T_ref (binary32 keeps 24 bits of
+// the O(0.1) fluctuations instead of the O(70) mean pressure).
+template <typename R>
+struct PrimSet {
+  R* rho;
+  R* u;
+  R* v;
+  R* w;
+  R* p;
+  R* T;
+  R* srho;  // sqrt(rho): Roe weights
+  R* H;     // total enthalpy
+  R* mu;    // Sutherland viscosity, interior; lagged into calc_dt like the reference
+};
+
 struct SolveDev {
   int IM, JM, KM;      // interior extents
   int nx, ny, nz;      // padded extents (IM + 2*NG ...)
@@ -46,28 +63,41 @@ struct SolveDev {
   int rx, ry, rz;      // NGV-ring extents (IM + 2*NGV ...)
   long long RV;        // ring volume
   long long IV;        // interior volume
-  // conserved state (SoA, padded)
+  int mixed;           // 0: binary64 throughout; 1: FP32-mixed
+  // conserved state (SoA, padded), binary64 in both modes
   double* Q;
   double* Qp;
-  // primitives of the current stage input (padded)
-  double* rho;
-  double* u;
-  double* v;
-  double* w;
-  double* p;
-  double* T;
-  double* srho;  // sqrt(rho): Roe weights
-  double* H;     // total enthalpy
-  double* mu;    // Sutherland viscosity, interior; lagged into calc_dt like the reference
-  // face fluxes (interior, 5 components each)
+  // binary64 primitives (binary64 mode; in FP32-mixed mode filled on demand for output)
+  PrimSet<double> pd;
+  // binary64 mode: face fluxes (interior, 5 components) and viscous fluxes Ev, Fv,
+  // Gv on the NGV ring (4 components)
   double* F[3];
-  // viscous fluxes Ev, Fv, Gv on the NGV ring, 4 components each
   double* Fv[3];
+  // FP32-mixed mode: the stage input as a binary32 perturbation of the reference
+  // state (rho - rho_ref, rho*u, rho*v, rho*w, E - E_ref), its primitives, and
+  // binary32 face and viscous fluxes
+  float* Uf;
+  PrimSet<float> pf;
+  float* Ff[3];
+  float* Fvf[3];
+  // reference state of the perturbation form (u_ref = 0, E_ref = p_ref/(gamma-1))
+  double rho_ref, p_ref, E_ref, T_ref;
   // parameters (src/read_input.cpp:78-90)
   double gamma, gam1, gam1_inv, gM2, Re_inv, kappa, C_T_inf, CFL, C_dt_v;
   double dx, dy, dz, inv_dx, inv_dy, inv_dz;
   SolveCtl* ctl;
 };
+
+template <typename R>
+__host__ __device__ inline const PrimSet<R>& prims_of(const SolveDev& s);
+template <>
+__host__ __device__ inline const PrimSet<double>& prims_of<double>(const SolveDev& s) {
+  return s.pd;
+}
+template <>
+__host__ __device__ inline const PrimSet<float>& prims_of<float>(const SolveDev& s) {
+  return s.pf;
+}
 
 struct TileRef {
   uint16_t solve;

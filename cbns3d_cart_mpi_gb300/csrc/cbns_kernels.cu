@@ -53,9 +53,8 @@ __device__ __forceinline__ TileCell tile_cell(const TileRef& t, int origin) {
 }
 
 // ---------------------------------------------------------------------------
-// Start-up: ghost fill, primitives, Q_p = Q, mu = 1 (src/cbns3d.cpp:149-153 and
-// src/Block3d.cpp:265).  Over the padded domain; each cell reads only its
-// interior source, so ghosts and interior are written without races.
+// Primitive recovery (Block3d::calc_primitive, src/Block3d.cpp:359-385) of one
+// conserved state, written at padded offset o.
 
 __device__ __forceinline__ int wrap(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
 
@@ -65,14 +64,64 @@ __device__ __forceinline__ void store_prims(const SolveDev& s, long long o, doub
   double uu = ru * ir, vv = rv * ir, ww = rw * ir;
   double q2 = uu * uu + vv * vv + ww * ww;
   double pp = s.gam1 * (E - 0.5 * r * q2);
-  s.rho[o] = r;
-  s.u[o] = uu;
-  s.v[o] = vv;
-  s.w[o] = ww;
-  s.p[o] = pp;
-  s.T[o] = s.gM2 * pp * ir;
-  s.srho[o] = sqrt(r);
-  s.H[o] = s.gamma * s.gam1_inv * pp * ir + 0.5 * q2;
+  s.pd.rho[o] = r;
+  s.pd.u[o] = uu;
+  s.pd.v[o] = vv;
+  s.pd.w[o] = ww;
+  s.pd.p[o] = pp;
+  s.pd.T[o] = s.gM2 * pp * ir;
+  s.pd.srho[o] = sqrt(r);
+  s.pd.H[o] = s.gamma * s.gam1_inv * pp * ir + 0.5 * q2;
+}
+
+// FP32-mixed: the binary32 perturbation state and primitives of a binary64 state.
+// rho' = rho - rho_ref and E' = E - E_ref are formed in binary64 before rounding,
+// so binary32 keeps 24 bits of the fluctuations; p' = p - p_ref and
+// T' = T - T_ref follow from them without touching the large means.  sqrt(rho)
+// for the Roe weights is taken in binary64 where rho is below 1% of rho_ref.
+struct MixedCell {
+  float U[NEQ];
+  float rho, u, v, w, p, T, srho, H;
+};
+
+__device__ __forceinline__ MixedCell mixed_cell(const SolveDev& s, const double (&q)[NEQ]) {
+  MixedCell m;
+  const float rp = (float)(q[0] - s.rho_ref);
+  const float Ep = (float)(q[4] - s.E_ref);
+  const float r = (float)q[0];
+  m.U[0] = rp;
+  m.U[1] = (float)q[1];
+  m.U[2] = (float)q[2];
+  m.U[3] = (float)q[3];
+  m.U[4] = Ep;
+  const float ir = 1.0f / r;
+  const float uu = m.U[1] * ir, vv = m.U[2] * ir, ww = m.U[3] * ir;
+  const float q2 = uu * uu + vv * vv + ww * ww;
+  const float gam1 = (float)s.gam1;
+  const float pp = gam1 * (Ep - 0.5f * r * q2);
+  const float p_ref = (float)s.p_ref;
+  m.rho = r;
+  m.u = uu;
+  m.v = vv;
+  m.w = ww;
+  m.p = pp;
+  m.T = (float)s.gM2 * ir * (pp - (float)(s.p_ref / s.rho_ref) * rp);
+  m.srho = (q[0] < 0.01 * s.rho_ref) ? (float)sqrt(q[0]) : sqrtf(r);
+  m.H = (float)(s.gamma * s.gam1_inv) * (p_ref + pp) * ir + 0.5f * q2;
+  return m;
+}
+
+__device__ __forceinline__ void store_mixed(const SolveDev& s, long long o, const MixedCell& m) {
+#pragma unroll
+  for (int n = 0; n < NEQ; ++n) s.Uf[n * s.V + o] = m.U[n];
+  s.pf.rho[o] = m.rho;
+  s.pf.u[o] = m.u;
+  s.pf.v[o] = m.v;
+  s.pf.w[o] = m.w;
+  s.pf.p[o] = m.p;
+  s.pf.T[o] = m.T;
+  s.pf.srho[o] = m.srho;
+  s.pf.H[o] = m.H;
 }
 
 __global__ void k_aos_to_soa(const SolveDev* __restrict__ solves, int sidx, const double* __restrict__ aos,
@@ -95,6 +144,9 @@ __global__ void k_soa_to_aos(const SolveDev* __restrict__ solves, int sidx, cons
   }
 }
 
+// Start-up: ghost fill, primitives, Q_p = Q, mu = 1 (src/cbns3d.cpp:149-153 and
+// src/Block3d.cpp:265).  Over the padded domain; each cell reads only its
+// interior source, so ghosts and interior are written without races.
 __global__ void k_prepare(const SolveDev* __restrict__ solves, const TileRef* __restrict__ tiles,
                           int ntiles) {
   for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
@@ -112,8 +164,25 @@ __global__ void k_prepare(const SolveDev* __restrict__ solves, const TileRef* __
       s.Qp[n * s.V + o] = q[n];
     }
     store_prims(s, o, q[0], q[1], q[2], q[3], q[4]);
+    if (s.mixed) store_mixed(s, o, mixed_cell(s, q));
     const bool interior = tc.i >= 0 && tc.i < s.IM && tc.j >= 0 && tc.j < s.JM && tc.k >= 0 && tc.k < s.KM;
-    if (interior) s.mu[o] = 1.0;
+    if (interior) {
+      s.pd.mu[o] = 1.0;
+      if (s.mixed) s.pf.mu[o] = 1.0f;
+    }
+  }
+}
+
+// Binary64 primitives of the current Q for output (FP32-mixed solves keep
+// binary32 primitives only while stepping).
+__global__ void k_prims_double(const SolveDev* __restrict__ solves, const TileRef* __restrict__ tiles,
+                               int ntiles) {
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    TileCell tc = tile_cell(tiles[t], -NG);
+    const SolveDev& s = solves[tc.s];
+    if (tc.i >= s.IM + NG || tc.j >= s.JM + NG) continue;
+    const long long o = pad_off(s, tc.i, tc.j, tc.k);
+    store_prims(s, o, s.Q[o], s.Q[s.V + o], s.Q[2 * s.V + o], s.Q[3 * s.V + o], s.Q[4 * s.V + o]);
   }
 }
 
@@ -128,6 +197,21 @@ __device__ __forceinline__ double warp_max(double v) {
   return v;
 }
 
+template <typename R>
+__device__ __forceinline__ double dt_speed(const SolveDev& s, long long o) {
+  const PrimSet<R>& P = prims_of<R>(s);
+  const R rr = P.rho[o], uu = P.u[o], vv = P.v[o], ww = P.w[o];
+  const R pp = (sizeof(R) == 4) ? (R)s.p_ref + P.p[o] : P.p[o];
+  const R idx = (R)s.inv_dx, idy = (R)s.inv_dy, idz = (R)s.inv_dz;
+  R c = sqrt((R)s.gamma * pp / rr);
+  R fv = (R)2.0 * P.mu[o] * (R)s.C_dt_v * sqrt(uu * uu + vv * vv + ww * ww) / (c * rr);
+  R t1 = fabs(uu) + c * idx + fv * idx * idx;
+  R t2 = fabs(vv) + c * idy + fv * idy * idy;
+  R t3 = fabs(ww) + c * idz + fv * idz * idz;
+  return (double)(t1 + t2 + t3);
+}
+
+template <typename R>
 __global__ void k_dt_reduce(const SolveDev* __restrict__ solves, const TileRef* __restrict__ tiles,
                             int ntiles, double t_end, int use_t_end, int skip_finished) {
   __shared__ double red[TILE_THREADS / 32];
@@ -139,14 +223,7 @@ __global__ void k_dt_reduce(const SolveDev* __restrict__ solves, const TileRef* 
     if (skip_finished && ctl->t_cur + 1.0e-5 > te) continue;  // uniform over the tile
     double sm = 0.0;
     if (tc.i < s.IM && tc.j < s.JM) {
-      const long long o = pad_off(s, tc.i, tc.j, tc.k);
-      double rr = s.rho[o], uu = s.u[o], vv = s.v[o], ww = s.w[o], pp = s.p[o];
-      double c = sqrt(s.gamma * pp / rr);
-      double fv = 2.0 * s.mu[o] * s.C_dt_v * sqrt(uu * uu + vv * vv + ww * ww) / (c * rr);
-      double t1 = fabs(uu) + c * s.inv_dx + fv * s.inv_dx * s.inv_dx;
-      double t2 = fabs(vv) + c * s.inv_dy + fv * s.inv_dy * s.inv_dy;
-      double t3 = fabs(ww) + c * s.inv_dz + fv * s.inv_dz * s.inv_dz;
-      double sum = t1 + t2 + t3;
+      double sum = dt_speed<R>(s, pad_off(s, tc.i, tc.j, tc.k));
       sm = (sum > 0.0) ? sum : 0.0;  // a NaN is skipped, as the reference's ternary does
     }
     sm = warp_max(sm);
@@ -203,42 +280,46 @@ __global__ void k_set_dt(const SolveDev* __restrict__ solves, int sidx, double d
 // 10 * IS_1^2 IS_2^2 IS_3^2 gives the same value with one division,
 //   num = a2 a3 f1 + 6 a1 a3 f2 + 3 a1 a2 f3,  den = a2 a3 + 6 a1 a3 + 3 a1 a2,
 // a_k = IS_k^2; the division is deferred so five of them can share one.
+// (IS_k >= 1e-6, so den >= 1e-23: inside binary32's normal range too.)
 
+template <typename R>
 struct Weno {
-  double num, den;
+  R num, den;
 };
 
-__device__ __forceinline__ Weno weno5_parts(double a, double b, double c, double d, double e) {
-  const double eps = 1.0e-6;
-  const double c13 = 13.0 / 12.0;
-  double d1 = a - 2.0 * b + c;
-  double d2 = a - 4.0 * b + 3.0 * c;
-  double d3 = b - 2.0 * c + d;
-  double d4 = b - d;
-  double d5 = c - 2.0 * d + e;
-  double d6 = 3.0 * c - 4.0 * d + e;
-  double is1 = c13 * d1 * d1 + 0.25 * d2 * d2 + eps;
-  double is2 = c13 * d3 * d3 + 0.25 * d4 * d4 + eps;
-  double is3 = c13 * d5 * d5 + 0.25 * d6 * d6 + eps;
-  double a1 = is1 * is1, a2 = is2 * is2, a3 = is3 * is3;
-  double p1 = a2 * a3;
-  double p2 = (6.0 * a1) * a3;
-  double p3 = (3.0 * a1) * a2;
-  const double s6 = 1.0 / 6.0;
-  double f1 = (2.0 * s6) * a - (7.0 * s6) * b + (11.0 * s6) * c;
-  double f2 = -s6 * b + (5.0 * s6) * c + (2.0 * s6) * d;
-  double f3 = (2.0 * s6) * c + (5.0 * s6) * d - s6 * e;
-  Weno r;
+template <typename R>
+__device__ __forceinline__ Weno<R> weno5_parts(R a, R b, R c, R d, R e) {
+  const R eps = (R)1.0e-6;
+  const R c13 = (R)(13.0 / 12.0);
+  R d1 = a - (R)2 * b + c;
+  R d2 = a - (R)4 * b + (R)3 * c;
+  R d3 = b - (R)2 * c + d;
+  R d4 = b - d;
+  R d5 = c - (R)2 * d + e;
+  R d6 = (R)3 * c - (R)4 * d + e;
+  R is1 = c13 * d1 * d1 + (R)0.25 * d2 * d2 + eps;
+  R is2 = c13 * d3 * d3 + (R)0.25 * d4 * d4 + eps;
+  R is3 = c13 * d5 * d5 + (R)0.25 * d6 * d6 + eps;
+  R a1 = is1 * is1, a2 = is2 * is2, a3 = is3 * is3;
+  R p1 = a2 * a3;
+  R p2 = ((R)6 * a1) * a3;
+  R p3 = ((R)3 * a1) * a2;
+  const R s6 = (R)(1.0 / 6.0);
+  R f1 = ((R)2 * s6) * a - ((R)7 * s6) * b + ((R)11 * s6) * c;
+  R f2 = -s6 * b + ((R)5 * s6) * c + ((R)2 * s6) * d;
+  R f3 = ((R)2 * s6) * c + ((R)5 * s6) * d - s6 * e;
+  Weno<R> r;
   r.num = p1 * f1 + p2 * f2 + p3 * f3;
   r.den = p1 + p2 + p3;
   return r;
 }
 
-// r[n] = num[n] / den[n] for five parts with one division (Montgomery's
-// simultaneous inversion).  Every den lies in [1e-23, 1e61] unless a smoothness
-// indicator exceeds ~1e15; outside that the product leaves the normal range and
-// each quotient is divided on its own.
-__device__ __forceinline__ void weno_divide5(const Weno (&w)[5], double (&r)[5]) {
+// r[n] = num[n] / den[n] for five parts.  Binary64: one division (Montgomery's
+// simultaneous inversion); every den lies in [1e-23, 1e61] unless a smoothness
+// indicator exceeds ~1e15, and outside [1e-300, 1e300] each quotient is divided on
+// its own.  Binary32: a product of five dens leaves the normal range, and the
+// binary32 pipe divides cheaply, so each quotient is divided.
+__device__ __forceinline__ void weno_divide5(const Weno<double> (&w)[5], double (&r)[5]) {
   double p1 = w[0].den;
   double p2 = p1 * w[1].den;
   double p3 = p2 * w[2].den;
@@ -261,6 +342,11 @@ __device__ __forceinline__ void weno_divide5(const Weno (&w)[5], double (&r)[5])
   }
 }
 
+__device__ __forceinline__ void weno_divide5(const Weno<float> (&w)[5], float (&r)[5]) {
+#pragma unroll
+  for (int n = 0; n < 5; ++n) r[n] = w[n].num / w[n].den;
+}
+
 // ---------------------------------------------------------------------------
 // Numerical flux at one face (src/Block3d.cpp:566-616 and its y/z twins).
 //
@@ -276,45 +362,53 @@ __device__ __forceinline__ void weno_divide5(const Weno (&w)[5], double (&r)[5])
 //   E = H s + U_D c d + q^2/2 r1 + U_t1 r3 + U_t2 r4.
 // The Roe average (ratio = sqrt(rho_R/rho_L)) is formed from per-cell sqrt(rho).
 // lf_flux (src/lf_flux.cpp:32-99) takes the reconstructed conserved states.
+//
+// PERT (FP32-mixed): f is the perturbation (rho', m, E') of the reference state.
+// L and R are linear and WENO5 reproduces constants, so reconstructing the
+// perturbation and adding rho_ref, E_ref back is the same scheme; the momentum
+// flux drops the constant p_ref (it cancels in every flux difference), so every
+// binary32 flux component is O(1) instead of O(p_ref).
 
-template <int D>
-__device__ __forceinline__ void face_flux(const SolveDev& s, const double* __restrict__ U,
-                                          long long c, double (&out)[NEQ]) {
+template <int D, typename R, bool PERT>
+__device__ __forceinline__ void face_flux(const SolveDev& s, const R* __restrict__ U, long long c,
+                                          R (&out)[NEQ]) {
   constexpr int T1 = (D + 1) % 3;
   constexpr int T2 = (D + 2) % 3;
+  const PrimSet<R>& P = prims_of<R>(s);
   const long long st = D == 0 ? 1ll : (D == 1 ? (long long)s.nx : (long long)s.nx * s.ny);
   const long long V = s.V;
   const long long cl = c - st;
+  const R gam1 = (R)s.gam1, gamma = (R)s.gamma, gam1_inv = (R)s.gam1_inv;
 
   // Roe-averaged state of the two cells either side (src/eigenvectors_roe.cpp:87-106).
-  const double sL = s.srho[cl], sR = s.srho[c];
-  const double inv = 1.0 / (sL + sR);
-  double Uv[3];
-  Uv[0] = (sL * s.u[cl] + sR * s.u[c]) * inv;
-  Uv[1] = (sL * s.v[cl] + sR * s.v[c]) * inv;
-  Uv[2] = (sL * s.w[cl] + sR * s.w[c]) * inv;
-  const double HH = (sL * s.H[cl] + sR * s.H[c]) * inv;
-  const double q2 = Uv[0] * Uv[0] + Uv[1] * Uv[1] + Uv[2] * Uv[2];
-  const double hq2 = 0.5 * q2;
-  const double cc = sqrt(s.gam1 * (HH - hq2));
-  const double ic = 1.0 / cc;
-  const double K = (0.5 * s.gam1) * ic * ic;
-  const double hic = 0.5 * ic;
-  const double un = Uv[D], u1 = Uv[T1], u2 = Uv[T2];
+  const R sL = P.srho[cl], sR = P.srho[c];
+  const R inv = (R)1 / (sL + sR);
+  R Uv[3];
+  Uv[0] = (sL * P.u[cl] + sR * P.u[c]) * inv;
+  Uv[1] = (sL * P.v[cl] + sR * P.v[c]) * inv;
+  Uv[2] = (sL * P.w[cl] + sR * P.w[c]) * inv;
+  const R HH = (sL * P.H[cl] + sR * P.H[c]) * inv;
+  const R q2 = Uv[0] * Uv[0] + Uv[1] * Uv[1] + Uv[2] * Uv[2];
+  const R hq2 = (R)0.5 * q2;
+  const R cc = sqrt(gam1 * (HH - hq2));
+  const R ic = (R)1 / cc;
+  const R K = ((R)0.5 * gam1) * ic * ic;
+  const R hic = (R)0.5 * ic;
+  const R un = Uv[D], u1 = Uv[T1], u2 = Uv[T2];
 
   // Characteristic projections of the six cells c-3 .. c+2 (shared by both
   // biased stencils).
-  double w[NEQ][6];
+  R w[NEQ][6];
 #pragma unroll
   for (int m = 0; m < 6; ++m) {
     const long long o = c + (m - 3) * st;
-    const double f0 = U[o], f1 = U[V + o], f2 = U[2 * V + o], f3 = U[3 * V + o], f4 = U[4 * V + o];
-    const double fm[3] = {f1, f2, f3};
-    const double t = hq2 * f0 - (Uv[0] * f1 + Uv[1] * f2 + Uv[2] * f3) + f4;
-    const double A = K * t;
-    const double B = hic * (un * f0 - fm[D]);
+    const R f0 = U[o], f1 = U[V + o], f2 = U[2 * V + o], f3 = U[3 * V + o], f4 = U[4 * V + o];
+    const R fm[3] = {f1, f2, f3};
+    const R t = hq2 * f0 - (Uv[0] * f1 + Uv[1] * f2 + Uv[2] * f3) + f4;
+    const R A = K * t;
+    const R B = hic * (un * f0 - fm[D]);
     w[0][m] = A + B;
-    w[1][m] = f0 - 2.0 * A;
+    w[1][m] = f0 - (R)2 * A;
     w[2][m] = A - B;
     w[3][m] = fm[T1] - u1 * f0;
     w[4][m] = fm[T2] - u2 * f0;
@@ -322,24 +416,24 @@ __device__ __forceinline__ void face_flux(const SolveDev& s, const double* __res
 
   // Left-biased (cells -3..+1) and right-biased mirrored (+2..-2) reconstructions
   // (src/Block3d.cpp:591-607, src/weno.cpp:77-152).
-  double rl[NEQ], rr[NEQ];
+  R rl[NEQ], rr[NEQ];
   {
-    Weno wl[NEQ];
+    Weno<R> wl[NEQ];
 #pragma unroll
-    for (int n = 0; n < NEQ; ++n) wl[n] = weno5_parts(w[n][0], w[n][1], w[n][2], w[n][3], w[n][4]);
+    for (int n = 0; n < NEQ; ++n) wl[n] = weno5_parts<R>(w[n][0], w[n][1], w[n][2], w[n][3], w[n][4]);
     weno_divide5(wl, rl);
   }
   {
-    Weno wr[NEQ];
+    Weno<R> wr[NEQ];
 #pragma unroll
-    for (int n = 0; n < NEQ; ++n) wr[n] = weno5_parts(w[n][5], w[n][4], w[n][3], w[n][2], w[n][1]);
+    for (int n = 0; n < NEQ; ++n) wr[n] = weno5_parts<R>(w[n][5], w[n][4], w[n][3], w[n][2], w[n][1]);
     weno_divide5(wr, rr);
   }
 
-  // Back to conserved variables.
-  double rhoL, mL[3], EL, rhoR, mR[3], ER;
+  // Back to conserved variables (perturbations when PERT).
+  R rhoL, mL[3], EL, rhoR, mR[3], ER;
   {
-    double sp = rl[0] + rl[2], dm = rl[2] - rl[0];
+    R sp = rl[0] + rl[2], dm = rl[2] - rl[0];
     rhoL = sp + rl[1];
     mL[D] = un * rhoL + cc * dm;
     mL[T1] = u1 * rhoL + rl[3];
@@ -347,7 +441,7 @@ __device__ __forceinline__ void face_flux(const SolveDev& s, const double* __res
     EL = HH * sp + (un * cc) * dm + hq2 * rl[1] + u1 * rl[3] + u2 * rl[4];
   }
   {
-    double sp = rr[0] + rr[2], dm = rr[2] - rr[0];
+    R sp = rr[0] + rr[2], dm = rr[2] - rr[0];
     rhoR = sp + rr[1];
     mR[D] = un * rhoR + cc * dm;
     mR[T1] = u1 * rhoR + rr[3];
@@ -356,47 +450,61 @@ __device__ __forceinline__ void face_flux(const SolveDev& s, const double* __res
   }
 
   // Local Lax-Friedrichs flux (src/lf_flux.cpp:32-99); both 1/rho from one division.
-  const double ip = 1.0 / (rhoL * rhoR);
-  const double iL = ip * rhoR, iR = ip * rhoL;
-  double vL[3], vR[3];
+  // PERT: rhoX, EX are perturbations; dL, dR the full densities, pL, pR the
+  // pressure perturbations, pfL, pfR the full pressures.
+  const R dL = PERT ? (R)s.rho_ref + rhoL : rhoL;
+  const R dR = PERT ? (R)s.rho_ref + rhoR : rhoR;
+  const R ip = (R)1 / (dL * dR);
+  const R iL = ip * dR, iR = ip * dL;
+  R vL[3], vR[3];
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
     vL[a] = mL[a] * iL;
     vR[a] = mR[a] * iR;
   }
-  const double q2L = vL[0] * vL[0] + vL[1] * vL[1] + vL[2] * vL[2];
-  const double q2R = vR[0] * vR[0] + vR[1] * vR[1] + vR[2] * vR[2];
-  const double pL = s.gam1 * (EL - 0.5 * rhoL * q2L);
-  const double pR = s.gam1 * (ER - 0.5 * rhoR * q2R);
-  const double c2L = s.gamma * pL * iL, c2R = s.gamma * pR * iR;
-  const double cL = sqrt(c2L), cR = sqrt(c2R);
-  const double HL = c2L * s.gam1_inv + 0.5 * q2L;
-  const double HR = c2R * s.gam1_inv + 0.5 * q2R;
-  const double alpha = fmax(fabs(vR[D]) + cR, fabs(vL[D]) + cL);
-  const double fL = mL[D], fR = mR[D];  // mass fluxes rho*q_n
-  out[0] = 0.5 * (fL + fR - alpha * (rhoR - rhoL));
+  const R q2L = vL[0] * vL[0] + vL[1] * vL[1] + vL[2] * vL[2];
+  const R q2R = vR[0] * vR[0] + vR[1] * vR[1] + vR[2] * vR[2];
+  const R pL = gam1 * (EL - (R)0.5 * dL * q2L);
+  const R pR = gam1 * (ER - (R)0.5 * dR * q2R);
+  const R pfL = PERT ? (R)s.p_ref + pL : pL;
+  const R pfR = PERT ? (R)s.p_ref + pR : pR;
+  const R c2L = gamma * pfL * iL, c2R = gamma * pfR * iR;
+  const R cL = sqrt(c2L), cR = sqrt(c2R);
+  const R HL = c2L * gam1_inv + (R)0.5 * q2L;
+  const R HR = c2R * gam1_inv + (R)0.5 * q2R;
+  const R alpha = fmax(fabs(vR[D]) + cR, fabs(vL[D]) + cL);
+  const R fL = mL[D], fR = mR[D];  // mass fluxes rho*q_n
+  out[0] = (R)0.5 * (fL + fR - alpha * (rhoR - rhoL));
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
-    double pf = (a == D) ? (pL + pR) : 0.0;
-    out[1 + a] = 0.5 * (fL * vL[a] + fR * vR[a] + pf - alpha * (mR[a] - mL[a]));
+    R pf = (a == D) ? (pL + pR) : (R)0;
+    out[1 + a] = (R)0.5 * (fL * vL[a] + fR * vR[a] + pf - alpha * (mR[a] - mL[a]));
   }
-  out[4] = 0.5 * (fL * HL + fR * HR - alpha * (ER - EL));
+  out[4] = (R)0.5 * (fL * HL + fR * HR - alpha * (ER - EL));
 }
 
-template <int D>
+template <int D, typename R>
 __global__ void __launch_bounds__(TILE_THREADS) k_inviscid(const SolveDev* __restrict__ solves,
                                                            const TileRef* __restrict__ tiles, int ntiles,
                                                            int stage) {
+  constexpr bool MIXED = sizeof(R) == 4;
   for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
     TileCell tc = tile_cell(tiles[t], 0);
     const SolveDev& s = solves[tc.s];
     if (!s.ctl->active) continue;
     if (tc.i >= s.IM || tc.j >= s.JM) continue;
-    const double* U = stage == 1 ? s.Q : s.Qp;
-    double f[NEQ];
-    face_flux<D>(s, U, pad_off(s, tc.i, tc.j, tc.k), f);
+    const R* U;
+    R* F;
+    if constexpr (MIXED) {
+      U = s.Uf;
+      F = s.Ff[D];
+    } else {
+      U = stage == 1 ? s.Q : s.Qp;
+      F = s.F[D];
+    }
+    R f[NEQ];
+    face_flux<D, R, MIXED>(s, U, pad_off(s, tc.i, tc.j, tc.k), f);
     const long long fo = int_off(s, tc.i, tc.j, tc.k);
-    double* F = s.F[D];
 #pragma unroll
     for (int n = 0; n < NEQ; ++n) F[n * s.IV + fo] = f[n];
   }
@@ -405,44 +513,60 @@ __global__ void __launch_bounds__(TILE_THREADS) k_inviscid(const SolveDev* __res
 // ---------------------------------------------------------------------------
 // Viscous fluxes on the NGV ring (src/calc_gradient.cpp:17-66,
 // src/Block3d.cpp:750-868).  d/dx f = ((f[-2]-f[+2])/12 + (f[+1]-f[-1])*2/3) / dx.
+// FP32-mixed: T is stored as T - T_ref; its derivatives are the same.
 
-__device__ __forceinline__ double d4(const double* __restrict__ f, long long o, long long st, double inv_h) {
-  const double c12 = 1.0 / 12.0, c23 = 2.0 / 3.0;
+template <typename R>
+__device__ __forceinline__ R d4(const R* __restrict__ f, long long o, long long st, R inv_h) {
+  const R c12 = (R)(1.0 / 12.0), c23 = (R)(2.0 / 3.0);
   return ((f[o - 2 * st] - f[o + 2 * st]) * c12 + (f[o + st] - f[o - st]) * c23) * inv_h;
 }
 
+template <typename R>
 __global__ void __launch_bounds__(TILE_THREADS) k_viscous(const SolveDev* __restrict__ solves,
                                                           const TileRef* __restrict__ tiles, int ntiles) {
+  constexpr bool MIXED = sizeof(R) == 4;
   for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
     TileCell tc = tile_cell(tiles[t], -NGV);
     const SolveDev& s = solves[tc.s];
     if (!s.ctl->active) continue;
     if (tc.i >= s.IM + NGV || tc.j >= s.JM + NGV) continue;
+    const PrimSet<R>& P = prims_of<R>(s);
     const long long o = pad_off(s, tc.i, tc.j, tc.k);
     const long long sy = s.nx, sz = (long long)s.nx * s.ny;
-    const double ux = d4(s.u, o, 1, s.inv_dx), uy = d4(s.u, o, sy, s.inv_dy), uz = d4(s.u, o, sz, s.inv_dz);
-    const double vx = d4(s.v, o, 1, s.inv_dx), vy = d4(s.v, o, sy, s.inv_dy), vz = d4(s.v, o, sz, s.inv_dz);
-    const double wx = d4(s.w, o, 1, s.inv_dx), wy = d4(s.w, o, sy, s.inv_dy), wz = d4(s.w, o, sz, s.inv_dz);
-    const double Tx = d4(s.T, o, 1, s.inv_dx), Ty = d4(s.T, o, sy, s.inv_dy), Tz = d4(s.T, o, sz, s.inv_dz);
-    const double Tl = s.T[o];
+    const R idx = (R)s.inv_dx, idy = (R)s.inv_dy, idz = (R)s.inv_dz;
+    const R ux = d4<R>(P.u, o, 1, idx), uy = d4<R>(P.u, o, sy, idy), uz = d4<R>(P.u, o, sz, idz);
+    const R vx = d4<R>(P.v, o, 1, idx), vy = d4<R>(P.v, o, sy, idy), vz = d4<R>(P.v, o, sz, idz);
+    const R wx = d4<R>(P.w, o, 1, idx), wy = d4<R>(P.w, o, sy, idy), wz = d4<R>(P.w, o, sz, idz);
+    const R Tx = d4<R>(P.T, o, 1, idx), Ty = d4<R>(P.T, o, sy, idy), Tz = d4<R>(P.T, o, sz, idz);
+    const R Tl = MIXED ? (R)s.T_ref + P.T[o] : P.T[o];
+    const R C = (R)s.C_T_inf;
     // Sutherland's law, (1 + C) / (T + C) * T^1.5 (src/Block3d.cpp:777).
-    const double mu = (1.0 + s.C_T_inf) * Tl * sqrt(Tl) / (Tl + s.C_T_inf);
-    if (tc.i >= 0 && tc.i < s.IM && tc.j >= 0 && tc.j < s.JM && tc.k >= 0 && tc.k < s.KM) s.mu[o] = mu;
-    const double mr = mu * s.Re_inv;
-    const double m23 = (2.0 / 3.0) * mr;
-    const double txx = m23 * (2.0 * ux - vy - wz);
-    const double tyy = m23 * (2.0 * vy - ux - wz);
-    const double tzz = m23 * (2.0 * wz - ux - vy);
-    const double txy = mr * (uy + vx);
-    const double txz = mr * (uz + wx);
-    const double tyz = mr * (vz + wy);
-    const double mk = mr * s.kappa;
-    const double uu = s.u[o], vv = s.v[o], ww = s.w[o];
+    const R mu = ((R)1 + C) * Tl * sqrt(Tl) / (Tl + C);
+    if (tc.i >= 0 && tc.i < s.IM && tc.j >= 0 && tc.j < s.JM && tc.k >= 0 && tc.k < s.KM) P.mu[o] = mu;
+    const R mr = mu * (R)s.Re_inv;
+    const R m23 = (R)(2.0 / 3.0) * mr;
+    const R txx = m23 * ((R)2 * ux - vy - wz);
+    const R tyy = m23 * ((R)2 * vy - ux - wz);
+    const R tzz = m23 * ((R)2 * wz - ux - vy);
+    const R txy = mr * (uy + vx);
+    const R txz = mr * (uz + wx);
+    const R tyz = mr * (vz + wy);
+    const R mk = mr * (R)s.kappa;
+    const R uu = P.u[o], vv = P.v[o], ww = P.w[o];
     const long long r = ring_off(s, tc.i, tc.j, tc.k);
     const long long RV = s.RV;
-    double* Ev = s.Fv[0];
-    double* Fv = s.Fv[1];
-    double* Gv = s.Fv[2];
+    R* Ev;
+    R* Fv;
+    R* Gv;
+    if constexpr (MIXED) {
+      Ev = s.Fvf[0];
+      Fv = s.Fvf[1];
+      Gv = s.Fvf[2];
+    } else {
+      Ev = s.Fv[0];
+      Fv = s.Fv[1];
+      Gv = s.Fv[2];
+    }
     Ev[r] = txx;
     Ev[RV + r] = txy;
     Ev[2 * RV + r] = txz;
@@ -464,10 +588,14 @@ __global__ void __launch_bounds__(TILE_THREADS) k_viscous(const SolveDev* __rest
 // src/Block3d.cpp:359-385).  Each interior cell writes its new state and
 // primitives to itself and to every ghost cell that is its periodic image, which
 // is exactly what the reference's x, y, z halo sweeps leave there.
+// FP32-mixed: the flux differences are binary32, the RK3 accumulation of the
+// conserved state binary64.
 
+template <typename R>
 __global__ void __launch_bounds__(TILE_THREADS) k_update(const SolveDev* __restrict__ solves,
                                                          const TileRef* __restrict__ tiles, int ntiles,
                                                          int stage) {
+  constexpr bool MIXED = sizeof(R) == 4;
   for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
     TileCell tc = tile_cell(tiles[t], 0);
     const SolveDev& s = solves[tc.s];
@@ -484,42 +612,61 @@ __global__ void __launch_bounds__(TILE_THREADS) k_update(const SolveDev* __restr
     const long long r = ring_off(s, i, j, k);
     const long long ry = s.rx, rz = (long long)s.rx * s.ry;
     const long long IV = s.IV, V = s.V, RV = s.RV;
+    const R* F0;
+    const R* F1;
+    const R* F2;
+    const R* V0;
+    const R* V1;
+    const R* V2;
+    if constexpr (MIXED) {
+      F0 = s.Ff[0], F1 = s.Ff[1], F2 = s.Ff[2];
+      V0 = s.Fvf[0], V1 = s.Fvf[1], V2 = s.Fvf[2];
+    } else {
+      F0 = s.F[0], F1 = s.F[1], F2 = s.F[2];
+      V0 = s.Fv[0], V1 = s.Fv[1], V2 = s.Fv[2];
+    }
+    const R idx = (R)s.inv_dx, idy = (R)s.inv_dy, idz = (R)s.inv_dz;
 
     double qn[NEQ];
 #pragma unroll
     for (int n = 0; n < NEQ; ++n) {
-      double df = (s.F[0][n * IV + fx] - s.F[0][n * IV + fo]) * s.inv_dx +
-                  (s.F[1][n * IV + fy] - s.F[1][n * IV + fo]) * s.inv_dy +
-                  (s.F[2][n * IV + fz] - s.F[2][n * IV + fo]) * s.inv_dz;
+      R df = (F0[n * IV + fx] - F0[n * IV + fo]) * idx + (F1[n * IV + fy] - F1[n * IV + fo]) * idy +
+             (F2[n * IV + fz] - F2[n * IV + fo]) * idz;
       if (n > 0) {
-        const double* Ev = s.Fv[0] + (n - 1) * RV;
-        const double* Fv = s.Fv[1] + (n - 1) * RV;
-        const double* Gv = s.Fv[2] + (n - 1) * RV;
         // -(d/dx) of the viscous fluxes, as 4th-order central differences
         // (src/Block3d.cpp:887-910): ((f[-2]-f[+2])/12 + (f[+1]-f[-1])*2/3) / h.
-        double dv = d4(Ev, r, 1, s.inv_dx) + d4(Fv, r, ry, s.inv_dy) + d4(Gv, r, rz, s.inv_dz);
+        R dv = d4<R>(V0 + (n - 1) * RV, r, 1, idx) + d4<R>(V1 + (n - 1) * RV, r, ry, idy) +
+               d4<R>(V2 + (n - 1) * RV, r, rz, idz);
         df -= dv;
       }
+      const double dfd = (double)df;
       const double q0 = s.Q[n * V + o];
       if (stage == 1) {
-        qn[n] = q0 - dt * df;
+        qn[n] = q0 - dt * dfd;
       } else if (stage == 2) {
-        qn[n] = 0.75 * q0 + 0.25 * (s.Qp[n * V + o] - dt * df);
+        qn[n] = 0.75 * q0 + 0.25 * (s.Qp[n * V + o] - dt * dfd);
       } else {
-        qn[n] = (q0 + 2.0 * (s.Qp[n * V + o] - dt * df)) * (1.0 / 3.0);
+        qn[n] = (q0 + 2.0 * (s.Qp[n * V + o] - dt * dfd)) * (1.0 / 3.0);
       }
     }
     double* out = stage == 3 ? s.Q : s.Qp;
 
     // Primitives of the new state (once), then the cell and its ghost images.
-    const double ir = 1.0 / qn[0];
-    const double uu = qn[1] * ir, vv = qn[2] * ir, ww = qn[3] * ir;
-    const double q2 = uu * uu + vv * vv + ww * ww;
-    const double pp = s.gam1 * (qn[4] - 0.5 * qn[0] * q2);
-    const double TT = s.gM2 * pp * ir;
-    const double sr = sqrt(qn[0]);
-    const double HH = s.gamma * s.gam1_inv * pp * ir + 0.5 * q2;
-    if (!(qn[0] > 0.0) || !(pp > 0.0)) atomicOr(&ctl->status, 1);
+    double uu = 0, vv = 0, ww = 0, pp = 0, TT = 0, sr = 0, HH = 0;
+    MixedCell mc;
+    if constexpr (MIXED) {
+      mc = mixed_cell(s, qn);
+      if (!(qn[0] > 0.0) || !((float)s.p_ref + mc.p > 0.0f)) atomicOr(&ctl->status, 1);
+    } else {
+      const double ir = 1.0 / qn[0];
+      uu = qn[1] * ir, vv = qn[2] * ir, ww = qn[3] * ir;
+      const double q2 = uu * uu + vv * vv + ww * ww;
+      pp = s.gam1 * (qn[4] - 0.5 * qn[0] * q2);
+      TT = s.gM2 * pp * ir;
+      sr = sqrt(qn[0]);
+      HH = s.gamma * s.gam1_inv * pp * ir + 0.5 * q2;
+      if (!(qn[0] > 0.0) || !(pp > 0.0)) atomicOr(&ctl->status, 1);
+    }
 
     int xi[3], yi[3], zi[3];
     int nxi = 0, nyi = 0, nzi = 0;
@@ -538,14 +685,18 @@ __global__ void __launch_bounds__(TILE_THREADS) k_update(const SolveDev* __restr
           const long long d = pad_off(s, xi[a1], yi[b2], zi[c3]);
 #pragma unroll
           for (int n = 0; n < NEQ; ++n) out[n * V + d] = qn[n];
-          s.rho[d] = qn[0];
-          s.u[d] = uu;
-          s.v[d] = vv;
-          s.w[d] = ww;
-          s.p[d] = pp;
-          s.T[d] = TT;
-          s.srho[d] = sr;
-          s.H[d] = HH;
+          if constexpr (MIXED) {
+            store_mixed(s, d, mc);
+          } else {
+            s.pd.rho[d] = qn[0];
+            s.pd.u[d] = uu;
+            s.pd.v[d] = vv;
+            s.pd.w[d] = ww;
+            s.pd.p[d] = pp;
+            s.pd.T[d] = TT;
+            s.pd.srho[d] = sr;
+            s.pd.H[d] = HH;
+          }
         }
   }
 }
@@ -690,22 +841,39 @@ cudaError_t launch_layout(const SolveDev* d, int sidx, const double* src, double
   return cudaGetLastError();
 }
 
+cudaError_t launch_prims_double(const SolveDev* d, const TileRef* tiles, int ntiles, cudaStream_t st) {
+  if (ntiles == 0) return cudaSuccess;
+  k_prims_double<<<grid_for(ntiles, 0), TILE_THREADS, 0, st>>>(d, tiles, ntiles);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_dt(const SolveDev* d, int nsolves, const TileRef* tiles, int ntiles, double t_end,
-                      bool use_t_end, cudaStream_t st, Profiler* pf) {
-  if (ntiles > 0)
-    CBNS_LAUNCH(pf, KID_DT_REDUCE, st,
-                (k_dt_reduce<<<grid_for(ntiles, 0), TILE_THREADS, 0, st>>>(d, tiles, ntiles, t_end,
-                                                                           use_t_end ? 1 : 0, 1)));
+                      bool use_t_end, bool mixed, cudaStream_t st, Profiler* pf) {
+  if (ntiles > 0) {
+    if (mixed)
+      CBNS_LAUNCH(pf, KID_DT_REDUCE, st,
+                  (k_dt_reduce<float><<<grid_for(ntiles, 0), TILE_THREADS, 0, st>>>(d, tiles, ntiles, t_end,
+                                                                                    use_t_end ? 1 : 0, 1)));
+    else
+      CBNS_LAUNCH(pf, KID_DT_REDUCE, st,
+                  (k_dt_reduce<double><<<grid_for(ntiles, 0), TILE_THREADS, 0, st>>>(d, tiles, ntiles, t_end,
+                                                                                     use_t_end ? 1 : 0, 1)));
+  }
   CBNS_LAUNCH(pf, KID_DT_FINALIZE, st,
               (k_dt_finalize<<<(nsolves + 127) / 128, 128, 0, st>>>(d, nsolves, t_end, use_t_end ? 1 : 0)));
   return cudaGetLastError();
 }
 
 cudaError_t launch_dt_raw(const SolveDev* d, int sidx, const TileRef* tiles, int ntiles, double* out,
-                          cudaStream_t st, Profiler* pf) {
-  if (ntiles > 0)
-    CBNS_LAUNCH(pf, KID_DT_REDUCE, st,
-                (k_dt_reduce<<<grid_for(ntiles, 0), TILE_THREADS, 0, st>>>(d, tiles, ntiles, 0.0, 0, 0)));
+                          bool mixed, cudaStream_t st, Profiler* pf) {
+  if (ntiles > 0) {
+    if (mixed)
+      CBNS_LAUNCH(pf, KID_DT_REDUCE, st,
+                  (k_dt_reduce<float><<<grid_for(ntiles, 0), TILE_THREADS, 0, st>>>(d, tiles, ntiles, 0.0, 0, 0)));
+    else
+      CBNS_LAUNCH(pf, KID_DT_REDUCE, st,
+                  (k_dt_reduce<double><<<grid_for(ntiles, 0), TILE_THREADS, 0, st>>>(d, tiles, ntiles, 0.0, 0, 0)));
+  }
   CBNS_LAUNCH(pf, KID_DT_FINALIZE, st, (k_dt_raw<<<1, 1, 0, st>>>(d, sidx, out)));
   return cudaGetLastError();
 }
@@ -715,16 +883,23 @@ cudaError_t launch_set_dt(const SolveDev* d, int sidx, double dt, cudaStream_t s
   return cudaGetLastError();
 }
 
-cudaError_t launch_stage(const SolveDev* d, const TileRef* tiles, int ntiles, const TileRef* ring_tiles,
-                         int nring, int stage, int max_ctas, cudaStream_t st, Profiler* pf) {
-  if (ntiles == 0) return cudaSuccess;
+template <typename R>
+static void stage_launches(const SolveDev* d, const TileRef* tiles, int ntiles, const TileRef* ring_tiles,
+                           int nring, int stage, int max_ctas, cudaStream_t st, Profiler* pf) {
   const int g = grid_for(ntiles, max_ctas);
-  CBNS_LAUNCH(pf, KID_INVISCID_X, st, (k_inviscid<0><<<g, TILE_THREADS, 0, st>>>(d, tiles, ntiles, stage)));
-  CBNS_LAUNCH(pf, KID_INVISCID_Y, st, (k_inviscid<1><<<g, TILE_THREADS, 0, st>>>(d, tiles, ntiles, stage)));
-  CBNS_LAUNCH(pf, KID_INVISCID_Z, st, (k_inviscid<2><<<g, TILE_THREADS, 0, st>>>(d, tiles, ntiles, stage)));
+  CBNS_LAUNCH(pf, KID_INVISCID_X, st, (k_inviscid<0, R><<<g, TILE_THREADS, 0, st>>>(d, tiles, ntiles, stage)));
+  CBNS_LAUNCH(pf, KID_INVISCID_Y, st, (k_inviscid<1, R><<<g, TILE_THREADS, 0, st>>>(d, tiles, ntiles, stage)));
+  CBNS_LAUNCH(pf, KID_INVISCID_Z, st, (k_inviscid<2, R><<<g, TILE_THREADS, 0, st>>>(d, tiles, ntiles, stage)));
   CBNS_LAUNCH(pf, KID_VISCOUS, st,
-              (k_viscous<<<grid_for(nring, max_ctas), TILE_THREADS, 0, st>>>(d, ring_tiles, nring)));
-  CBNS_LAUNCH(pf, KID_UPDATE, st, (k_update<<<g, TILE_THREADS, 0, st>>>(d, tiles, ntiles, stage)));
+              (k_viscous<R><<<grid_for(nring, max_ctas), TILE_THREADS, 0, st>>>(d, ring_tiles, nring)));
+  CBNS_LAUNCH(pf, KID_UPDATE, st, (k_update<R><<<g, TILE_THREADS, 0, st>>>(d, tiles, ntiles, stage)));
+}
+
+cudaError_t launch_stage(const SolveDev* d, const TileRef* tiles, int ntiles, const TileRef* ring_tiles,
+                         int nring, int stage, int max_ctas, bool mixed, cudaStream_t st, Profiler* pf) {
+  if (ntiles == 0) return cudaSuccess;
+  if (mixed) stage_launches<float>(d, tiles, ntiles, ring_tiles, nring, stage, max_ctas, st, pf);
+  else stage_launches<double>(d, tiles, ntiles, ring_tiles, nring, stage, max_ctas, st, pf);
   return cudaGetLastError();
 }
 
