@@ -45,6 +45,7 @@ GPU_API = {
     "cbns_profile_begin": (c_int, [c_vp]),
     "cbns_profile_end": (c_int, [c_vp, c_vp, c_int, ctypes.POINTER(c_int)]),
     "cbns_probe_peak": (c_int, [c_int, c_dp]),
+    "cbns_diagnostics_noalloc": (c_int, [c_vp, c_u32, c_u32, c_u32, c_d, c_d, c_d, c_vp, c_vp]),
     "cbns_last_error": (ctypes.c_char_p, []),
     "cbns_version": (ctypes.c_char_p, []),
 }

@@ -68,6 +68,11 @@ size_t align_up(size_t x) { return (x + 255) & ~size_t(255); }
 
 }  // namespace
 
+namespace cbns {
+// Lets other translation units of the library report through cbns_last_error().
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+}  // namespace cbns
+
 struct cbns_handle {
   int device = 0;
   cudaStream_t stream = nullptr;

@@ -160,6 +160,27 @@ cbns_status cbns_profile_end(cbns_handle* h, cbns_kernel_time* out, int cap, int
  * binary64 when fp64 != 0 else binary32: the pipe peaks the roofline uses. */
 cbns_status cbns_probe_peak(int fp64, double* tflops);
 
+/* No counterpart in the reference.  Kinetic energy and enstrophy, as
+ * cbns_diagnostics computes them, of a conserved state the caller already holds
+ * in its own device memory, computed without allocating anything.  For callers
+ * that may not call cudaMalloc while they run: an in-situ monitor called from
+ * inside another solver's time loop that must not change the device's memory
+ * footprint, a host framework whose caching allocator owns the device budget, a
+ * real-time loop that cannot take an allocation's latency or implicit syncs.
+ *   Q_dev    device pointer, the reference's Q layout (get_idx_Q, ghosts filled)
+ *   out_dev  device pointer to 2 doubles: KE, enstrophy
+ *   stream   cudaStream_t (as void*) the two kernels are launched on; NULL = default
+ * Asynchronous on `stream`.  Scratch is a static device array of 4096 partial
+ * sums (128 KiB, held on every GPU that loads the library until exit), each
+ * covering 16384 cells, so IM*JM*KM may be at most 67,108,864 (e.g. 406^3);
+ * larger blocks are rejected with CBNS_ERR_BAD_DIMS.  The first call on a device
+ * looks up the array's device address (cudaGetSymbolAddress) with that device
+ * current; make that first call before any stream capture.  All calls share the
+ * one scratch array: calls whose kernels may overlap on the GPU (unordered
+ * streams) race and must be serialised by the caller. */
+cbns_status cbns_diagnostics_noalloc(const double* Q_dev, uint32_t IM, uint32_t JM, uint32_t KM, double dx,
+                                     double dy, double dz, double* out_dev, void* stream);
+
 /* Text of the last error on this host thread ("" if none). */
 const char* cbns_last_error(void);
 
