@@ -72,6 +72,12 @@ def reduce_max(value, world):
     return float(t.item())
 
 
+def aggregate_value(world, cells, steps, ms_max):
+    """Whole-job throughput of `world` replicas, each advancing `cells` cells by
+    `steps` steps, timed by the slowest rank (ms_max)."""
+    return world * cells * steps / (ms_max * 1e-3)
+
+
 def barrier(world):
     if world > 1:
         import torch.distributed as dist
@@ -220,7 +226,7 @@ def run_ours(args, rank, world, local):
     ms = reduce_max(ms, world)
     assert done == args.steps, "solve finished early (%d of %d steps)" % (done, args.steps)
     cells = N ** 3
-    value = world * cells * args.steps / (ms * 1e-3)
+    value = aggregate_value(world, cells, args.steps, ms)
     launches_per_step = 2 + 3 * 5
 
     line = None

@@ -16,6 +16,29 @@ HOST_LIB = os.path.join(LIB_DIR, "libcbns_host.so")
 _gpu = None
 
 
+class ServerOpts(ctypes.Structure):
+    _fields_ = [("precision", ctypes.c_int), ("memory_budget_bytes", ctypes.c_uint64),
+                ("max_active", ctypes.c_uint32), ("steps_per_round", ctypes.c_uint32),
+                ("tile_rows", ctypes.c_int), ("ctas_per_sm", ctypes.c_int)]
+
+
+class RequestInfo(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int), ("steps", ctypes.c_uint32), ("t_final", ctypes.c_double),
+                ("ke", ctypes.c_double), ("enstrophy", ctypes.c_double), ("submit_s", ctypes.c_double),
+                ("admit_s", ctypes.c_double), ("done_s", ctypes.c_double), ("device_bytes", ctypes.c_uint64)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_uint64), ("completed", ctypes.c_uint64), ("failed", ctypes.c_uint64),
+                ("rounds", ctypes.c_uint64), ("batch_builds", ctypes.c_uint64), ("cell_steps", ctypes.c_uint64),
+                ("peak_active", ctypes.c_uint32), ("queued", ctypes.c_uint32),
+                ("budget_bytes", ctypes.c_uint64), ("used_bytes", ctypes.c_uint64), ("clock_s", ctypes.c_double)]
+
+
+class LaunchConfig(ctypes.Structure):
+    _fields_ = [("tile_rows", ctypes.c_int), ("ctas_per_sm", ctypes.c_int)]
+
+
 class KernelTime(ctypes.Structure):
     _fields_ = [("name", ctypes.c_char * 32), ("launches", ctypes.c_uint32), ("total_ms", ctypes.c_double)]
 _host = None
@@ -42,6 +65,25 @@ GPU_API = {
     "cbns_check_state": (c_int, [c_vp]),
     "cbns_stream": (c_vp, [c_vp]),
     "cbns_get_info": (c_int, [c_vp, ctypes.POINTER(c_u32), ctypes.POINTER(c_u64), ctypes.POINTER(c_int)]),
+    "cbns_init_tgv": (c_int, [c_vp, c_u64, c_d, c_int, c_int, c_d]),
+    "cbns_footprint": (c_int, [c_u32, c_u32, c_u32, c_int, ctypes.POINTER(c_u64)]),
+    "cbns_server_create": (c_int, [c_vp, ctypes.POINTER(c_vp)]),
+    "cbns_server_destroy": (c_int, [c_vp]),
+    "cbns_server_submit": (c_int, [c_vp, P_params, c_u32, c_u32, c_u32, c_vp, c_int, ctypes.POINTER(c_u64)]),
+    "cbns_server_submit_tgv": (c_int, [c_vp, P_params, c_u32, c_u32, c_u32, c_u64, c_d, c_int, c_int, c_int,
+                                       ctypes.POINTER(c_u64)]),
+    "cbns_server_cancel": (c_int, [c_vp, c_u64]),
+    "cbns_server_wait": (c_int, [c_vp, c_u64, c_d, c_vp]),
+    "cbns_server_result": (c_int, [c_vp, c_u64, c_vp]),
+    "cbns_server_release": (c_int, [c_vp, c_u64]),
+    "cbns_server_get_stats": (c_int, [c_vp, c_vp]),
+    "cbns_batch_create": (c_int, [ctypes.POINTER(c_vp), c_int, ctypes.POINTER(c_vp)]),
+    "cbns_batch_destroy": (c_int, [c_vp]),
+    "cbns_batch_run": (c_int, [c_vp, c_u32, ctypes.POINTER(c_u32)]),
+    "cbns_batch_set_config": (c_int, [c_vp, c_vp]),
+    "cbns_batch_get_config": (c_int, [c_vp, c_vp]),
+    "cbns_batch_autotune": (c_int, [c_vp, c_int, c_dp, c_int, ctypes.POINTER(c_int)]),
+    "cbns_batch_stream": (c_vp, [c_vp]),
     "cbns_profile_begin": (c_int, [c_vp]),
     "cbns_profile_end": (c_int, [c_vp, c_vp, c_int, ctypes.POINTER(c_int)]),
     "cbns_probe_peak": (c_int, [c_int, c_dp]),

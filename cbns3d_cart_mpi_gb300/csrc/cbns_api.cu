@@ -13,21 +13,23 @@
 #include <vector>
 
 #include "../../include/cbns_gpu.h"
-#include "cbns_device.cuh"
-#include "cbns_prof.h"
+#include "cbns_internal.h"
+#include "cbns_modes.h"
 
 namespace cbns {
 cudaError_t launch_prepare(const SolveDev* d, const TileRef* tiles, int ntiles, cudaStream_t st, Profiler* pf);
 cudaError_t launch_layout(const SolveDev* d, int sidx, const double* src, double* dst, bool to_soa,
                           long long V, cudaStream_t st, Profiler* pf);
 cudaError_t launch_prims_double(const SolveDev* d, const TileRef* tiles, int ntiles, cudaStream_t st);
+cudaError_t launch_init_tgv(const SolveDev* d, int sidx, const TileRef* tiles, int ntiles, double p_inf,
+                            const PerturbMode* modes, int nmodes, cudaStream_t st);
 cudaError_t launch_dt(const SolveDev* d, int nsolves, const TileRef* tiles, int ntiles, double t_end,
-                      bool use_t_end, bool mixed, cudaStream_t st, Profiler* pf);
+                      bool use_t_end, bool mixed, const LaunchCfg& cfg, cudaStream_t st, Profiler* pf);
 cudaError_t launch_dt_raw(const SolveDev* d, int sidx, const TileRef* tiles, int ntiles, double* out,
-                          bool mixed, cudaStream_t st, Profiler* pf);
+                          bool mixed, const LaunchCfg& cfg, cudaStream_t st, Profiler* pf);
 cudaError_t launch_set_dt(const SolveDev* d, int sidx, double dt, cudaStream_t st);
 cudaError_t launch_stage(const SolveDev* d, const TileRef* tiles, int ntiles, const TileRef* ring_tiles,
-                         int nring, int stage, int max_ctas, bool mixed, cudaStream_t st, Profiler* pf);
+                         int nring, int stage, const LaunchCfg& cfg, bool mixed, cudaStream_t st, Profiler* pf);
 cudaError_t launch_diag(const SolveDev* d, int sidx, const TileRef* tiles, int ntiles, double* partials,
                         int nparts, double inv_n, double* out, cudaStream_t st, Profiler* pf);
 }  // namespace cbns
@@ -55,9 +57,9 @@ cbns_status cuda_fail(cudaError_t e, const char* what) {
     if (e_ != cudaSuccess) return cuda_fail(e_, #call);   \
   } while (0)
 
-// Tiles of TILE_X x TILE_Y x 1 cells over a box of extents ex, ey, ez.
-void append_tiles(std::vector<TileRef>& out, int solve, int ex, int ey, int ez) {
-  const int tx = (ex + TILE_X - 1) / TILE_X, ty = (ey + TILE_Y - 1) / TILE_Y;
+// Tiles of TILE_X x rows x 1 cells over a box of extents ex, ey, ez.
+void append_tiles(std::vector<TileRef>& out, int solve, int ex, int ey, int ez, int rows = TILE_Y) {
+  const int tx = (ex + TILE_X - 1) / TILE_X, ty = (ey + rows - 1) / rows;
   for (int k = 0; k < ez; ++k)
     for (int j = 0; j < ty; ++j)
       for (int i = 0; i < tx; ++i)
@@ -66,6 +68,66 @@ void append_tiles(std::vector<TileRef>& out, int solve, int ex, int ey, int ez) 
 
 size_t align_up(size_t x) { return (x + 255) & ~size_t(255); }
 
+size_t tile_count(long long ex, long long ey, long long ez, int rows = TILE_Y) {
+  return (size_t)((ex + TILE_X - 1) / TILE_X) * (size_t)((ey + rows - 1) / rows) * (size_t)ez;
+}
+
+// Byte offsets of everything a solve's arena holds (see cbns_create).
+struct ArenaLayout {
+  size_t oQ, oQp, oStage, oPrim, oF[3], oFv[3], oFf[3], oFvf[3], oUf, oPf, oCtl, oDesc, oTi, oTr, oTp, oPart, oOut,
+      total;
+};
+
+ArenaLayout arena_layout(const SolveDev& s, bool mixed, size_t n_int, size_t n_ring, size_t n_pad, int nparts) {
+  ArenaLayout L{};
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    size_t o = off;
+    off += align_up(bytes);
+    return o;
+  };
+  const size_t dV = sizeof(double) * (size_t)s.V, fV = sizeof(float) * (size_t)s.V;
+  L.oQ = take(NEQ * dV);
+  L.oQp = take(NEQ * dV);
+  L.oStage = take(NEQ * dV);
+  L.oPrim = take(9 * dV);
+  if (!mixed) {
+    for (int d = 0; d < 3; ++d) L.oF[d] = take(sizeof(double) * NEQ * (size_t)s.IV);
+    for (int d = 0; d < 3; ++d) L.oFv[d] = take(sizeof(double) * (NEQ - 1) * (size_t)s.RV);
+  } else {
+    L.oUf = take(NEQ * fV);
+    L.oPf = take(9 * fV);
+    for (int d = 0; d < 3; ++d) L.oFf[d] = take(sizeof(float) * NEQ * (size_t)s.IV);
+    for (int d = 0; d < 3; ++d) L.oFvf[d] = take(sizeof(float) * (NEQ - 1) * (size_t)s.RV);
+  }
+  L.oCtl = take(sizeof(SolveCtl));
+  L.oDesc = take(sizeof(SolveDev));
+  L.oTi = take(sizeof(TileRef) * n_int);
+  L.oTr = take(sizeof(TileRef) * n_ring);
+  L.oTp = take(sizeof(TileRef) * n_pad);
+  L.oPart = take(sizeof(double) * 4 * nparts);
+  L.oOut = take(sizeof(double) * 8);
+  L.total = off;
+  return L;
+}
+
+void set_extents(SolveDev& s, uint32_t IM, uint32_t JM, uint32_t KM) {
+  s.IM = IM;
+  s.JM = JM;
+  s.KM = KM;
+  s.nx = IM + 2 * NG;
+  s.ny = JM + 2 * NG;
+  s.nz = KM + 2 * NG;
+  s.V = (long long)s.nx * s.ny * s.nz;
+  s.rx = IM + 2 * NGV;
+  s.ry = JM + 2 * NGV;
+  s.rz = KM + 2 * NGV;
+  s.RV = (long long)s.rx * s.ry * s.rz;
+  s.IV = (long long)IM * JM * KM;
+}
+
+constexpr int kDiagParts = 1024;
+
 }  // namespace
 
 namespace cbns {
@@ -73,32 +135,6 @@ namespace cbns {
 void set_last_error(const std::string& msg) { g_last_error = msg; }
 }  // namespace cbns
 
-struct cbns_handle {
-  int device = 0;
-  cudaStream_t stream = nullptr;
-  int precision = CBNS_FP64;
-  cbns_params params{};
-  uint32_t IM = 0, JM = 0, KM = 0;
-  char* arena = nullptr;
-  size_t arena_bytes = 0;
-  SolveDev desc{};
-  SolveDev* d_desc = nullptr;
-  SolveCtl* d_ctl = nullptr;
-  TileRef* d_tiles_int = nullptr;
-  TileRef* d_tiles_ring = nullptr;
-  TileRef* d_tiles_pad = nullptr;
-  int n_int = 0, n_ring = 0, n_pad = 0;
-  double* d_stage = nullptr;
-  double* d_partials = nullptr;
-  int nparts = 0;
-  double* d_out = nullptr;  // small device results (diagnostics, raw dt)
-  SolveCtl* h_ctl = nullptr;  // pinned
-  double* h_out = nullptr;    // pinned
-  cudaGraphExec_t step_graph = nullptr;
-  double graph_t_end = 0.0;
-  Profiler prof;
-  Profiler* pf() { return prof.on ? &prof : nullptr; }
-};
 
 extern "C" {
 
@@ -183,18 +219,7 @@ cbns_status cbns_create(const cbns_params* p, uint32_t IM, uint32_t JM, uint32_t
     return bail(cuda_fail(cudaGetLastError(), "cudaStreamCreate"));
 
   SolveDev& s = h->desc;
-  s.IM = IM;
-  s.JM = JM;
-  s.KM = KM;
-  s.nx = IM + 2 * NG;
-  s.ny = JM + 2 * NG;
-  s.nz = KM + 2 * NG;
-  s.V = (long long)s.nx * s.ny * s.nz;
-  s.rx = IM + 2 * NGV;
-  s.ry = JM + 2 * NGV;
-  s.rz = KM + 2 * NGV;
-  s.RV = (long long)s.rx * s.ry * s.rz;
-  s.IV = (long long)IM * JM * KM;
+  set_extents(s, IM, JM, KM);
 
   std::vector<TileRef> t_int, t_ring, t_pad;
   append_tiles(t_int, 0, IM, JM, KM);
@@ -203,39 +228,19 @@ cbns_status cbns_create(const cbns_params* p, uint32_t IM, uint32_t JM, uint32_t
   h->n_int = (int)t_int.size();
   h->n_ring = (int)t_ring.size();
   h->n_pad = (int)t_pad.size();
-  h->nparts = 1024;
+  h->nparts = kDiagParts;
 
   // Arena layout.  Both modes hold the binary64 state (Q, Q_p, staging) and
   // binary64 primitives; binary64 solves add binary64 face/viscous fluxes,
   // FP32-mixed solves the binary32 perturbation state, primitives and fluxes.
   const bool mixed = precision == CBNS_FP32_MIXED;
   s.mixed = mixed ? 1 : 0;
-  size_t off = 0;
-  auto take = [&](size_t bytes) {
-    size_t o = off;
-    off += align_up(bytes);
-    return o;
-  };
-  const size_t dV = sizeof(double) * (size_t)s.V, fV = sizeof(float) * (size_t)s.V;
-  size_t oQ = take(NEQ * dV), oQp = take(NEQ * dV), oStage = take(NEQ * dV);
-  size_t oPrim = take(9 * dV);
-  size_t oF[3] = {0, 0, 0}, oFv[3] = {0, 0, 0}, oFf[3] = {0, 0, 0}, oFvf[3] = {0, 0, 0}, oUf = 0, oPf = 0;
-  if (!mixed) {
-    for (int d = 0; d < 3; ++d) oF[d] = take(sizeof(double) * NEQ * (size_t)s.IV);
-    for (int d = 0; d < 3; ++d) oFv[d] = take(sizeof(double) * (NEQ - 1) * (size_t)s.RV);
-  } else {
-    oUf = take(NEQ * fV);
-    oPf = take(9 * fV);
-    for (int d = 0; d < 3; ++d) oFf[d] = take(sizeof(float) * NEQ * (size_t)s.IV);
-    for (int d = 0; d < 3; ++d) oFvf[d] = take(sizeof(float) * (NEQ - 1) * (size_t)s.RV);
-  }
-  size_t oCtl = take(sizeof(SolveCtl));
-  size_t oDesc = take(sizeof(SolveDev));
-  size_t oTi = take(sizeof(TileRef) * t_int.size());
-  size_t oTr = take(sizeof(TileRef) * t_ring.size());
-  size_t oTp = take(sizeof(TileRef) * t_pad.size());
-  size_t oPart = take(sizeof(double) * 4 * h->nparts);
-  size_t oOut = take(sizeof(double) * 8);
+  const ArenaLayout L = arena_layout(s, mixed, t_int.size(), t_ring.size(), t_pad.size(), h->nparts);
+  const size_t off = L.total;
+  const size_t oQ = L.oQ, oQp = L.oQp, oStage = L.oStage, oPrim = L.oPrim, oUf = L.oUf, oPf = L.oPf;
+  const size_t oCtl = L.oCtl, oDesc = L.oDesc, oTi = L.oTi, oTr = L.oTr, oTp = L.oTp, oPart = L.oPart,
+               oOut = L.oOut;
+  const size_t *oF = L.oF, *oFv = L.oFv, *oFf = L.oFf, *oFvf = L.oFvf;
   h->arena_bytes = off;
   cudaError_t e = cudaMalloc(&h->arena, off);
   if (e != cudaSuccess) return bail(cuda_fail(e, "cudaMalloc(arena)"));
@@ -294,6 +299,7 @@ cbns_status cbns_create(const cbns_params* p, uint32_t IM, uint32_t JM, uint32_t
   s.inv_dx = 1.0 / s.dx;
   s.inv_dy = 1.0 / s.dy;
   s.inv_dz = 1.0 / s.dz;
+  fill_consts(s);
   h->d_ctl = (SolveCtl*)(A + oCtl);
   s.ctl = h->d_ctl;
   h->d_desc = (SolveDev*)(A + oDesc);
@@ -350,6 +356,25 @@ cbns_status cbns_upload_Q(cbns_handle* h, const double* Q, double t) {
   return CBNS_OK;
 }
 
+cbns_status cbns_init_tgv(cbns_handle* h, uint64_t seed, double amp, int nmodes, int kmax, double t) {
+  cbns_status st = check_handle(h, "cbns_init_tgv");
+  if (st != CBNS_OK) return st;
+  if (nmodes < 0 || nmodes > 64 || (nmodes > 0 && kmax < 1))
+    return fail(CBNS_ERR_INVALID_ARG, "cbns_init_tgv: nmodes must be in [0, 64] and kmax >= 1");
+  std::vector<PerturbMode> modes;
+  if (nmodes > 0) modes = draw_modes(seed, amp, nmodes, kmax);
+  CBNS_CUDA(launch_init_tgv(h->d_desc, 0, h->d_tiles_int, h->n_int, h->params.p_inf, modes.data(), nmodes,
+                            h->stream));
+  CBNS_CUDA(launch_prepare(h->d_desc, h->d_tiles_pad, h->n_pad, h->stream, h->pf()));
+  std::memset(h->h_ctl, 0, sizeof(SolveCtl));
+  h->h_ctl->t_cur = t;
+  h->h_ctl->t_end = h->params.t_end;
+  h->h_ctl->active = 1;
+  CBNS_CUDA(cudaMemcpyAsync(h->d_ctl, h->h_ctl, sizeof(SolveCtl), cudaMemcpyHostToDevice, h->stream));
+  CBNS_CUDA(cudaStreamSynchronize(h->stream));
+  return CBNS_OK;
+}
+
 static cbns_status download_state(cbns_handle* h, const double* src, double* dst, const char* fn) {
   cbns_status st = check_handle(h, fn);
   if (st != CBNS_OK) return st;
@@ -391,7 +416,8 @@ cbns_status cbns_calc_dt(cbns_handle* h, double* dt) {
   cbns_status st = check_handle(h, "cbns_calc_dt");
   if (st != CBNS_OK) return st;
   if (!dt) return fail(CBNS_ERR_INVALID_ARG, "cbns_calc_dt: null output");
-  CBNS_CUDA(launch_dt_raw(h->d_desc, 0, h->d_tiles_int, h->n_int, h->d_out, h->desc.mixed != 0, h->stream, h->pf()));
+  CBNS_CUDA(launch_dt_raw(h->d_desc, 0, h->d_tiles_int, h->n_int, h->d_out, h->desc.mixed != 0, LaunchCfg{},
+                          h->stream, h->pf()));
   CBNS_CUDA(cudaMemcpyAsync(h->h_out, h->d_out, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   CBNS_CUDA(cudaStreamSynchronize(h->stream));
   *dt = h->h_out[0];
@@ -399,7 +425,7 @@ cbns_status cbns_calc_dt(cbns_handle* h, double* dt) {
 }
 
 static cbns_status enqueue_stage(cbns_handle* h, int stage) {
-  CBNS_CUDA(launch_stage(h->d_desc, h->d_tiles_int, h->n_int, h->d_tiles_ring, h->n_ring, stage, 0,
+  CBNS_CUDA(launch_stage(h->d_desc, h->d_tiles_int, h->n_int, h->d_tiles_ring, h->n_ring, stage, LaunchCfg{},
                          h->desc.mixed != 0, h->stream, h->pf()));
   return CBNS_OK;
 }
@@ -415,8 +441,8 @@ cbns_status cbns_stage(cbns_handle* h, double dt, int stage) {
 }
 
 static cbns_status enqueue_step(cbns_handle* h, double t_end, bool use_t_end) {
-  CBNS_CUDA(launch_dt(h->d_desc, 1, h->d_tiles_int, h->n_int, t_end, use_t_end, h->desc.mixed != 0, h->stream,
-                      h->pf()));
+  CBNS_CUDA(launch_dt(h->d_desc, 1, h->d_tiles_int, h->n_int, t_end, use_t_end, h->desc.mixed != 0, LaunchCfg{},
+                      h->stream, h->pf()));
   for (int s = 1; s <= 3; ++s) {
     cbns_status st = enqueue_stage(h, s);
     if (st != CBNS_OK) return st;
@@ -546,6 +572,259 @@ cbns_status cbns_profile_end(cbns_handle* h, cbns_kernel_time* out, int cap, int
     ++k;
   }
   if (n) *n = k < cap ? k : cap;
+  return CBNS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Batches.
+
+}  // extern "C"
+
+namespace {
+constexpr int kRowsOptions[3] = {2, 4, 8};
+int rows_index(int rows) { return rows == 2 ? 0 : (rows == 8 ? 2 : 1); }
+}  // namespace
+
+
+static cbns_status batch_enqueue_step(cbns_batch* b) {
+  const int ri = rows_index(b->cfg.tile_rows);
+  const int n = (int)b->handles.size();
+  CBNS_CUDA(launch_dt(b->d_descs, n, b->d_int[ri], b->n_int[ri], 0.0, false, b->mixed, b->cfg, b->stream, nullptr));
+  for (int st = 1; st <= 3; ++st)
+    CBNS_CUDA(launch_stage(b->d_descs, b->d_int[ri], b->n_int[ri], b->d_ring[ri], b->n_ring[ri], st, b->cfg,
+                           b->mixed, b->stream, nullptr));
+  return CBNS_OK;
+}
+
+static cbns_status batch_graph(cbns_batch* b) {
+  if (b->graph && b->graph_rows == b->cfg.tile_rows && b->graph_ctas == b->cfg.max_ctas) return CBNS_OK;
+  if (b->graph) {
+    cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+  }
+  cudaGraph_t g;
+  CBNS_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+  cbns_status st = batch_enqueue_step(b);
+  cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+  if (st != CBNS_OK) return st;
+  if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture(batch)");
+  e = cudaGraphInstantiate(&b->graph, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate(batch)");
+  b->graph_rows = b->cfg.tile_rows;
+  b->graph_ctas = b->cfg.max_ctas;
+  return CBNS_OK;
+}
+
+extern "C" {
+
+cbns_status cbns_batch_destroy(cbns_batch* b) {
+  if (!b) return CBNS_OK;
+  cudaSetDevice(b->device);
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  if (b->arena) cudaFree(b->arena);
+  if (b->h_ctl) cudaFreeHost(b->h_ctl);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+  return CBNS_OK;
+}
+
+cbns_status cbns_batch_create(cbns_handle* const* handles, int n, cbns_batch** out) {
+  if (!handles || !out || n <= 0) return fail(CBNS_ERR_INVALID_ARG, "cbns_batch_create: no handles");
+  *out = nullptr;
+  if (n > 65535) return fail(CBNS_ERR_INVALID_ARG, "cbns_batch_create: at most 65535 solves");
+  for (int i = 0; i < n; ++i) {
+    if (!handles[i]) return fail(CBNS_ERR_INVALID_ARG, "cbns_batch_create: null handle");
+    if (handles[i]->device != handles[0]->device || handles[i]->precision != handles[0]->precision)
+      return fail(CBNS_ERR_INVALID_ARG, "cbns_batch_create: handles differ in device or precision");
+  }
+  cbns_batch* b = new cbns_batch();
+  auto bail = [&](cbns_status st) {
+    cbns_batch_destroy(b);
+    return st;
+  };
+  b->device = handles[0]->device;
+  b->mixed = handles[0]->precision == CBNS_FP32_MIXED;
+  b->handles.assign(handles, handles + n);
+  cudaError_t e = cudaSetDevice(b->device);
+  if (e != cudaSuccess) return bail(cuda_fail(e, "cudaSetDevice"));
+  if ((e = cudaDeviceGetAttribute(&b->sm_count, cudaDevAttrMultiProcessorCount, b->device)) != cudaSuccess)
+    return bail(cuda_fail(e, "cudaDeviceGetAttribute"));
+  if ((e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking)) != cudaSuccess)
+    return bail(cuda_fail(e, "cudaStreamCreate(batch)"));
+  std::vector<SolveDev> descs(n);
+  std::vector<TileRef> ti[3], tr[3];
+  for (int i = 0; i < n; ++i) {
+    const SolveDev& s = handles[i]->desc;
+    descs[i] = s;
+    for (int r = 0; r < 3; ++r) {
+      append_tiles(ti[r], i, s.IM, s.JM, s.KM, kRowsOptions[r]);
+      append_tiles(tr[r], i, s.rx, s.ry, s.rz, kRowsOptions[r]);
+    }
+  }
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    size_t o = off;
+    off += align_up(bytes);
+    return o;
+  };
+  size_t oD = take(sizeof(SolveDev) * n), oI[3], oR[3];
+  for (int r = 0; r < 3; ++r) {
+    oI[r] = take(sizeof(TileRef) * ti[r].size());
+    oR[r] = take(sizeof(TileRef) * tr[r].size());
+  }
+  if ((e = cudaMalloc(&b->arena, off)) != cudaSuccess) return bail(cuda_fail(e, "cudaMalloc(batch)"));
+  b->d_descs = (SolveDev*)(b->arena + oD);
+  if ((e = cudaMemcpyAsync(b->d_descs, descs.data(), sizeof(SolveDev) * n, cudaMemcpyHostToDevice, b->stream)) !=
+      cudaSuccess)
+    return bail(cuda_fail(e, "cudaMemcpyAsync(batch descs)"));
+  for (int r = 0; r < 3; ++r) {
+    b->d_int[r] = (TileRef*)(b->arena + oI[r]);
+    b->d_ring[r] = (TileRef*)(b->arena + oR[r]);
+    b->n_int[r] = (int)ti[r].size();
+    b->n_ring[r] = (int)tr[r].size();
+    if ((e = cudaMemcpyAsync(b->d_int[r], ti[r].data(), sizeof(TileRef) * ti[r].size(), cudaMemcpyHostToDevice,
+                             b->stream)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(b->d_ring[r], tr[r].data(), sizeof(TileRef) * tr[r].size(), cudaMemcpyHostToDevice,
+                             b->stream)) != cudaSuccess)
+      return bail(cuda_fail(e, "cudaMemcpyAsync(batch tiles)"));
+  }
+  if ((e = cudaMallocHost(&b->h_ctl, sizeof(SolveCtl) * n)) != cudaSuccess)
+    return bail(cuda_fail(e, "cudaMallocHost(batch)"));
+  // Work queued on the handles' own streams comes first.
+  for (int i = 0; i < n; ++i)
+    if ((e = cudaStreamSynchronize(handles[i]->stream)) != cudaSuccess) return bail(cuda_fail(e, "sync"));
+  b->start_steps.assign(n, 0);
+  for (int i = 0; i < n; ++i)
+    if ((e = cudaMemcpyAsync(&b->h_ctl[i], handles[i]->d_ctl, sizeof(SolveCtl), cudaMemcpyDeviceToHost,
+                             b->stream)) != cudaSuccess)
+      return bail(cuda_fail(e, "cudaMemcpyAsync(batch ctl)"));
+  if ((e = cudaStreamSynchronize(b->stream)) != cudaSuccess) return bail(cuda_fail(e, "sync(batch)"));
+  for (int i = 0; i < n; ++i) b->start_steps[i] = b->h_ctl[i].steps;
+  *out = b;
+  return CBNS_OK;
+}
+
+cbns_status cbns_batch_set_config(cbns_batch* b, const cbns_launch_config* cfg) {
+  if (!b || !cfg) return fail(CBNS_ERR_INVALID_ARG, "cbns_batch_set_config: null argument");
+  if (cfg->tile_rows != 2 && cfg->tile_rows != 4 && cfg->tile_rows != 8)
+    return fail(CBNS_ERR_INVALID_ARG, "cbns_batch_set_config: tile_rows must be 2, 4 or 8");
+  if (cfg->ctas_per_sm < 0 || cfg->ctas_per_sm > 64)
+    return fail(CBNS_ERR_INVALID_ARG, "cbns_batch_set_config: ctas_per_sm must be in [0, 64]");
+  b->cfg.tile_rows = cfg->tile_rows;
+  b->ctas_per_sm = cfg->ctas_per_sm;
+  b->cfg.max_ctas = cfg->ctas_per_sm * b->sm_count;
+  return CBNS_OK;
+}
+
+cbns_status cbns_batch_get_config(cbns_batch* b, cbns_launch_config* cfg) {
+  if (!b || !cfg) return fail(CBNS_ERR_INVALID_ARG, "cbns_batch_get_config: null argument");
+  cfg->tile_rows = b->cfg.tile_rows;
+  cfg->ctas_per_sm = b->ctas_per_sm;
+  return CBNS_OK;
+}
+
+void* cbns_batch_stream(cbns_batch* b) { return b ? (void*)b->stream : nullptr; }
+
+cbns_status cbns_batch_run(cbns_batch* b, uint32_t nsteps, uint32_t* steps_out) {
+  if (!b) return fail(CBNS_ERR_INVALID_ARG, "cbns_batch_run: null batch");
+  CBNS_CUDA(cudaSetDevice(b->device));
+  cbns_status st = batch_graph(b);
+  if (st != CBNS_OK) return st;
+  for (uint32_t k = 0; k < nsteps; ++k) CBNS_CUDA(cudaGraphLaunch(b->graph, b->stream));
+  const int n = (int)b->handles.size();
+  for (int i = 0; i < n; ++i)
+    CBNS_CUDA(cudaMemcpyAsync(&b->h_ctl[i], b->handles[i]->d_ctl, sizeof(SolveCtl), cudaMemcpyDeviceToHost,
+                              b->stream));
+  CBNS_CUDA(cudaStreamSynchronize(b->stream));
+  bool bad = false;
+  for (int i = 0; i < n; ++i) {
+    if (steps_out) steps_out[i] = b->h_ctl[i].steps - b->start_steps[i];
+    bad = bad || b->h_ctl[i].status != 0;
+  }
+  if (bad) return fail(CBNS_ERR_NONPHYSICAL, "cbns_batch_run: a solve met a non-physical state");
+  return CBNS_OK;
+}
+
+cbns_status cbns_batch_autotune(cbns_batch* b, int reps, double* ms_out, int cap, int* ncand) {
+  if (!b || reps < 1) return fail(CBNS_ERR_INVALID_ARG, "cbns_batch_autotune: bad arguments");
+  CBNS_CUDA(cudaSetDevice(b->device));
+  const int n = (int)b->handles.size();
+  // Snapshot every solve's whole device arena so the timing steps leave no trace.
+  std::vector<char*> snap(n, nullptr);
+  auto release = [&]() {
+    for (char* p : snap)
+      if (p) cudaFree(p);
+  };
+  for (int i = 0; i < n; ++i) {
+    cudaError_t e = cudaMalloc(&snap[i], b->handles[i]->arena_bytes);
+    if (e != cudaSuccess) {
+      release();
+      return cuda_fail(e, "cudaMalloc(autotune snapshot)");
+    }
+    e = cudaMemcpyAsync(snap[i], b->handles[i]->arena, b->handles[i]->arena_bytes, cudaMemcpyDeviceToDevice,
+                        b->stream);
+    if (e != cudaSuccess) {
+      release();
+      return cuda_fail(e, "cudaMemcpyAsync(autotune snapshot)");
+    }
+  }
+  const int cps_options[4] = {0, 2, 4, 8};
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  double best = 1e300;
+  cbns_launch_config best_cfg{b->cfg.tile_rows, b->ctas_per_sm};
+  int k = 0;
+  cbns_status st = CBNS_OK;
+  for (int r = 0; r < 3 && st == CBNS_OK; ++r)
+    for (int c = 0; c < 4 && st == CBNS_OK; ++c) {
+      cbns_launch_config cand{kRowsOptions[r], cps_options[c]};
+      cbns_batch_set_config(b, &cand);
+      if ((st = batch_graph(b)) != CBNS_OK) break;
+      cudaGraphLaunch(b->graph, b->stream);  // warm-up
+      cudaEventRecord(e0, b->stream);
+      for (int q = 0; q < reps; ++q) cudaGraphLaunch(b->graph, b->stream);
+      cudaEventRecord(e1, b->stream);
+      cudaError_t e = cudaEventSynchronize(e1);
+      if (e != cudaSuccess) {
+        st = cuda_fail(e, "autotune step");
+        break;
+      }
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      double per = ms / reps;
+      if (ms_out && k < cap) ms_out[k] = per;
+      ++k;
+      if (per < best) {
+        best = per;
+        best_cfg = cand;
+      }
+      // Restore the state before the next candidate.
+      for (int i = 0; i < n; ++i)
+        cudaMemcpyAsync(b->handles[i]->arena, snap[i], b->handles[i]->arena_bytes, cudaMemcpyDeviceToDevice,
+                        b->stream);
+    }
+  cudaError_t e = cudaStreamSynchronize(b->stream);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  release();
+  if (st != CBNS_OK) return st;
+  if (e != cudaSuccess) return cuda_fail(e, "autotune restore");
+  cbns_batch_set_config(b, &best_cfg);
+  if (ncand) *ncand = k;
+  return CBNS_OK;
+}
+
+cbns_status cbns_footprint(uint32_t IM, uint32_t JM, uint32_t KM, int precision, uint64_t* bytes) {
+  if (!bytes) return fail(CBNS_ERR_INVALID_ARG, "cbns_footprint: null output");
+  if (IM < (uint32_t)NG || JM < (uint32_t)NG || KM < (uint32_t)NG) return fail(CBNS_ERR_BAD_DIMS, "cbns_footprint");
+  SolveDev s{};
+  set_extents(s, IM, JM, KM);
+  ArenaLayout L = arena_layout(s, precision == CBNS_FP32_MIXED, tile_count(IM, JM, KM),
+                               tile_count(s.rx, s.ry, s.rz), tile_count(s.nx, s.ny, s.nz), kDiagParts);
+  *bytes = L.total;
   return CBNS_OK;
 }
 

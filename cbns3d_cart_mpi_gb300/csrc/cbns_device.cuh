@@ -56,6 +56,18 @@ struct PrimSet {
   R* mu;    // Sutherland viscosity, interior; lagged into calc_dt like the reference
 };
 
+// Per-solve constants in the precision a kernel computes in, derived once on the
+// host so no thread converts or re-derives them.
+template <typename R>
+struct Consts {
+  R gamma, gam1, gam1_inv, gM2, Re_inv, kappa, C_T_inf, C_dt_v;
+  R inv_dx, inv_dy, inv_dz;
+  R rho_ref, p_ref, E_ref, T_ref;
+  R gamma_gam1_inv;  // gamma / (gamma - 1)
+  R pref_over_rref;  // p_ref / rho_ref
+  R low_rho;         // below this density the Roe weights' sqrt is taken in binary64
+};
+
 struct SolveDev {
   int IM, JM, KM;      // interior extents
   int nx, ny, nz;      // padded extents (IM + 2*NG ...)
@@ -85,8 +97,63 @@ struct SolveDev {
   // parameters (src/read_input.cpp:78-90)
   double gamma, gam1, gam1_inv, gM2, Re_inv, kappa, C_T_inf, CFL, C_dt_v;
   double dx, dy, dz, inv_dx, inv_dy, inv_dz;
+  Consts<double> cd;
+  Consts<float> cf;
   SolveCtl* ctl;
 };
+
+template <typename R>
+__host__ __device__ inline const Consts<R>& consts_of(const SolveDev& s);
+template <>
+__host__ __device__ inline const Consts<double>& consts_of<double>(const SolveDev& s) {
+  return s.cd;
+}
+template <>
+__host__ __device__ inline const Consts<float>& consts_of<float>(const SolveDev& s) {
+  return s.cf;
+}
+
+// Fill cd and cf from the binary64 parameters (host side, once per solve).
+inline void fill_consts(SolveDev& s) {
+  Consts<double>& c = s.cd;
+  c.gamma = s.gamma;
+  c.gam1 = s.gam1;
+  c.gam1_inv = s.gam1_inv;
+  c.gM2 = s.gM2;
+  c.Re_inv = s.Re_inv;
+  c.kappa = s.kappa;
+  c.C_T_inf = s.C_T_inf;
+  c.C_dt_v = s.C_dt_v;
+  c.inv_dx = s.inv_dx;
+  c.inv_dy = s.inv_dy;
+  c.inv_dz = s.inv_dz;
+  c.rho_ref = s.rho_ref;
+  c.p_ref = s.p_ref;
+  c.E_ref = s.E_ref;
+  c.T_ref = s.T_ref;
+  c.gamma_gam1_inv = s.gamma * s.gam1_inv;
+  c.pref_over_rref = s.p_ref / s.rho_ref;
+  c.low_rho = 0.01 * s.rho_ref;
+  Consts<float>& f = s.cf;
+  f.gamma = (float)c.gamma;
+  f.gam1 = (float)c.gam1;
+  f.gam1_inv = (float)c.gam1_inv;
+  f.gM2 = (float)c.gM2;
+  f.Re_inv = (float)c.Re_inv;
+  f.kappa = (float)c.kappa;
+  f.C_T_inf = (float)c.C_T_inf;
+  f.C_dt_v = (float)c.C_dt_v;
+  f.inv_dx = (float)c.inv_dx;
+  f.inv_dy = (float)c.inv_dy;
+  f.inv_dz = (float)c.inv_dz;
+  f.rho_ref = (float)c.rho_ref;
+  f.p_ref = (float)c.p_ref;
+  f.E_ref = (float)c.E_ref;
+  f.T_ref = (float)c.T_ref;
+  f.gamma_gam1_inv = (float)c.gamma_gam1_inv;
+  f.pref_over_rref = (float)c.pref_over_rref;
+  f.low_rho = (float)c.low_rho;
+}
 
 template <typename R>
 __host__ __device__ inline const PrimSet<R>& prims_of(const SolveDev& s);
@@ -117,5 +184,12 @@ __host__ __device__ inline long long int_off(const SolveDev& s, int i, int j, in
 }
 
 enum Domain { DOM_INTERIOR = 0, DOM_RING = 1, DOM_PADDED = 2 };
+
+// Launch shape of the stage and dt kernels: tile rows (CTA = 32 x tile_rows
+// threads) and, when > 0, a persistent grid of max_ctas CTAs walking the table.
+struct LaunchCfg {
+  int tile_rows = TILE_Y;
+  int max_ctas = 0;
+};
 
 }  // namespace cbns

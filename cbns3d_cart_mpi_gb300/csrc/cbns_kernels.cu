@@ -30,6 +30,7 @@
 #include <cstdint>
 
 #include "cbns_device.cuh"
+#include "cbns_modes.h"
 #include "cbns_prof.h"
 
 namespace cbns {
@@ -43,14 +44,31 @@ struct TileCell {
   int i, j, k;
 };
 
+// A tile is TILE_X cells along i by blockDim.x/32 rows along j (one CTA).  The
+// row count is a launch-time choice (the batch autotuner picks 2, 4 or 8), not a
+// template parameter, so every launch shape runs the same compiled kernel and
+// therefore the same arithmetic: results do not depend on the launch shape.
+constexpr int kMaxThreads = 256;
+
 __device__ __forceinline__ TileCell tile_cell(const TileRef& t, int origin) {
   TileCell c;
   c.s = t.solve;
   c.i = origin + t.ti * TILE_X + (int)(threadIdx.x % TILE_X);
-  c.j = origin + t.tj * TILE_Y + (int)(threadIdx.x / TILE_X);
+  c.j = origin + t.tj * (int)(blockDim.x / TILE_X) + (int)(threadIdx.x / TILE_X);
   c.k = origin + t.tk;
   return c;
 }
+
+// ---------------------------------------------------------------------------
+// Division, reciprocal and square root by compute type.  Binary64 keeps IEEE
+// division and square root.  The binary32 paths of FP32-mixed use the fast
+// approximations (a couple of ulp): their results are stored and differenced in
+// binary32 anyway, whose rounding dominates.
+
+__device__ __forceinline__ double div_(double a, double b) { return a / b; }
+__device__ __forceinline__ float div_(float a, float b) { return __fdividef(a, b); }
+__device__ __forceinline__ double sqrt_(double a) { return sqrt(a); }
+__device__ __forceinline__ float sqrt_(float a) { return a * rsqrtf(a); }
 
 // ---------------------------------------------------------------------------
 // Primitive recovery (Block3d::calc_primitive, src/Block3d.cpp:359-385) of one
@@ -71,7 +89,7 @@ __device__ __forceinline__ void store_prims(const SolveDev& s, long long o, doub
   s.pd.p[o] = pp;
   s.pd.T[o] = s.gM2 * pp * ir;
   s.pd.srho[o] = sqrt(r);
-  s.pd.H[o] = s.gamma * s.gam1_inv * pp * ir + 0.5 * q2;
+  s.pd.H[o] = s.cd.gamma_gam1_inv * pp * ir + 0.5 * q2;
 }
 
 // FP32-mixed: the binary32 perturbation state and primitives of a binary64 state.
@@ -86,28 +104,27 @@ struct MixedCell {
 
 __device__ __forceinline__ MixedCell mixed_cell(const SolveDev& s, const double (&q)[NEQ]) {
   MixedCell m;
-  const float rp = (float)(q[0] - s.rho_ref);
-  const float Ep = (float)(q[4] - s.E_ref);
+  const Consts<float>& C = s.cf;
+  const float rp = (float)(q[0] - s.cd.rho_ref);
+  const float Ep = (float)(q[4] - s.cd.E_ref);
   const float r = (float)q[0];
   m.U[0] = rp;
   m.U[1] = (float)q[1];
   m.U[2] = (float)q[2];
   m.U[3] = (float)q[3];
   m.U[4] = Ep;
-  const float ir = 1.0f / r;
+  const float ir = div_(1.0f, r);
   const float uu = m.U[1] * ir, vv = m.U[2] * ir, ww = m.U[3] * ir;
   const float q2 = uu * uu + vv * vv + ww * ww;
-  const float gam1 = (float)s.gam1;
-  const float pp = gam1 * (Ep - 0.5f * r * q2);
-  const float p_ref = (float)s.p_ref;
+  const float pp = C.gam1 * (Ep - 0.5f * r * q2);
   m.rho = r;
   m.u = uu;
   m.v = vv;
   m.w = ww;
   m.p = pp;
-  m.T = (float)s.gM2 * ir * (pp - (float)(s.p_ref / s.rho_ref) * rp);
-  m.srho = (q[0] < 0.01 * s.rho_ref) ? (float)sqrt(q[0]) : sqrtf(r);
-  m.H = (float)(s.gamma * s.gam1_inv) * (p_ref + pp) * ir + 0.5f * q2;
+  m.T = C.gM2 * ir * (pp - C.pref_over_rref * rp);
+  m.srho = (r < C.low_rho) ? (float)sqrt(q[0]) : sqrt_(r);
+  m.H = C.gamma_gam1_inv * (C.p_ref + pp) * ir + 0.5f * q2;
   return m;
 }
 
@@ -173,6 +190,48 @@ __global__ void k_prepare(const SolveDev* __restrict__ solves, const TileRef* __
   }
 }
 
+// Device initial condition (no host state): the Taylor-Green fields of
+// Block3d::initial_condition (src/Block3d.cpp:237-271) on gen_mesh's mesh
+// (src/Block3d.cpp:208-235), plus the project's solenoidal perturbation, then
+// calc_conservative (src/Block3d.cpp:273-300), written to the interior of Q.
+// The device sin/cos differ from the host libm in the last place at most.
+constexpr int kMaxModes = 64;
+struct ModeTable {
+  int n;
+  PerturbMode m[kMaxModes];
+};
+
+__global__ void k_init_tgv(const SolveDev* __restrict__ solves, int sidx, const TileRef* __restrict__ tiles,
+                           int ntiles, double p_inf, ModeTable modes) {
+  const SolveDev& s = solves[sidx];
+  const double half_pi2 = 3.14159265358979323846;  // (2 pi) / 2, gen_mesh's offset
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    TileCell tc = tile_cell(tiles[t], 0);
+    if (tc.i >= s.IM || tc.j >= s.JM) continue;
+    const double xl = (tc.i * s.dx - half_pi2) + 0.5 * s.dx;
+    const double yl = (tc.j * s.dy - half_pi2) + 0.5 * s.dy;
+    const double zl = (tc.k * s.dz - half_pi2) + 0.5 * s.dz;
+    double u = sin(xl) * cos(yl) * cos(zl);
+    double v = -cos(xl) * sin(yl) * cos(zl);
+    double w = 0.0;
+    for (int m = 0; m < modes.n; ++m) {
+      const PerturbMode& md = modes.m[m];
+      const double c = cos(md.k[0] * xl + md.k[1] * yl + md.k[2] * zl + md.phase);
+      u += md.a[0] * c;
+      v += md.a[1] * c;
+      w += md.a[2] * c;
+    }
+    const double p = p_inf + (cos(2.0 * xl) + cos(2.0 * yl)) * (cos(2.0 * zl) + 2.0) / 16.0;
+    const double r = s.gM2 * p;
+    const long long o = pad_off(s, tc.i, tc.j, tc.k);
+    s.Q[o] = r;
+    s.Q[s.V + o] = r * u;
+    s.Q[2 * s.V + o] = r * v;
+    s.Q[3 * s.V + o] = r * w;
+    s.Q[4 * s.V + o] = p / s.gam1 + 0.5 * r * (u * u + v * v + w * w);
+  }
+}
+
 // Binary64 primitives of the current Q for output (FP32-mixed solves keep
 // binary32 primitives only while stepping).
 __global__ void k_prims_double(const SolveDev* __restrict__ solves, const TileRef* __restrict__ tiles,
@@ -201,10 +260,11 @@ template <typename R>
 __device__ __forceinline__ double dt_speed(const SolveDev& s, long long o) {
   const PrimSet<R>& P = prims_of<R>(s);
   const R rr = P.rho[o], uu = P.u[o], vv = P.v[o], ww = P.w[o];
-  const R pp = (sizeof(R) == 4) ? (R)s.p_ref + P.p[o] : P.p[o];
-  const R idx = (R)s.inv_dx, idy = (R)s.inv_dy, idz = (R)s.inv_dz;
-  R c = sqrt((R)s.gamma * pp / rr);
-  R fv = (R)2.0 * P.mu[o] * (R)s.C_dt_v * sqrt(uu * uu + vv * vv + ww * ww) / (c * rr);
+  const Consts<R>& C = consts_of<R>(s);
+  const R pp = (sizeof(R) == 4) ? C.p_ref + P.p[o] : P.p[o];
+  const R idx = C.inv_dx, idy = C.inv_dy, idz = C.inv_dz;
+  R c = sqrt_(div_(C.gamma * pp, rr));
+  R fv = div_((R)2.0 * P.mu[o] * C.C_dt_v * sqrt_(uu * uu + vv * vv + ww * ww), c * rr);
   R t1 = fabs(uu) + c * idx + fv * idx * idx;
   R t2 = fabs(vv) + c * idy + fv * idy * idy;
   R t3 = fabs(ww) + c * idz + fv * idz * idz;
@@ -212,9 +272,11 @@ __device__ __forceinline__ double dt_speed(const SolveDev& s, long long o) {
 }
 
 template <typename R>
-__global__ void k_dt_reduce(const SolveDev* __restrict__ solves, const TileRef* __restrict__ tiles,
-                            int ntiles, double t_end, int use_t_end, int skip_finished) {
-  __shared__ double red[TILE_THREADS / 32];
+__global__ void __launch_bounds__(kMaxThreads) k_dt_reduce(const SolveDev* __restrict__ solves,
+                                                           const TileRef* __restrict__ tiles, int ntiles,
+                                                           double t_end, int use_t_end, int skip_finished) {
+  __shared__ double red[kMaxThreads / 32];
+  const int nwarps = (int)(blockDim.x / 32);
   for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
     TileCell tc = tile_cell(tiles[t], 0);
     const SolveDev& s = solves[tc.s];
@@ -232,7 +294,7 @@ __global__ void k_dt_reduce(const SolveDev* __restrict__ solves, const TileRef* 
     if (threadIdx.x == 0) {
       double m = red[0];
 #pragma unroll
-      for (int a = 1; a < TILE_THREADS / 32; ++a) m = fmax(m, red[a]);
+      for (int a = 1; a < nwarps; ++a) m = fmax(m, red[a]);
       // Positive doubles order like their bit patterns.
       atomicMax(&s.ctl->smax_bits, (unsigned long long)__double_as_longlong(m));
     }
@@ -344,7 +406,7 @@ __device__ __forceinline__ void weno_divide5(const Weno<double> (&w)[5], double 
 
 __device__ __forceinline__ void weno_divide5(const Weno<float> (&w)[5], float (&r)[5]) {
 #pragma unroll
-  for (int n = 0; n < 5; ++n) r[n] = w[n].num / w[n].den;
+  for (int n = 0; n < 5; ++n) r[n] = div_(w[n].num, w[n].den);
 }
 
 // ---------------------------------------------------------------------------
@@ -378,11 +440,12 @@ __device__ __forceinline__ void face_flux(const SolveDev& s, const R* __restrict
   const long long st = D == 0 ? 1ll : (D == 1 ? (long long)s.nx : (long long)s.nx * s.ny);
   const long long V = s.V;
   const long long cl = c - st;
-  const R gam1 = (R)s.gam1, gamma = (R)s.gamma, gam1_inv = (R)s.gam1_inv;
+  const Consts<R>& C = consts_of<R>(s);
+  const R gam1 = C.gam1, gamma = C.gamma, gam1_inv = C.gam1_inv;
 
   // Roe-averaged state of the two cells either side (src/eigenvectors_roe.cpp:87-106).
   const R sL = P.srho[cl], sR = P.srho[c];
-  const R inv = (R)1 / (sL + sR);
+  const R inv = div_((R)1, sL + sR);
   R Uv[3];
   Uv[0] = (sL * P.u[cl] + sR * P.u[c]) * inv;
   Uv[1] = (sL * P.v[cl] + sR * P.v[c]) * inv;
@@ -390,8 +453,8 @@ __device__ __forceinline__ void face_flux(const SolveDev& s, const R* __restrict
   const R HH = (sL * P.H[cl] + sR * P.H[c]) * inv;
   const R q2 = Uv[0] * Uv[0] + Uv[1] * Uv[1] + Uv[2] * Uv[2];
   const R hq2 = (R)0.5 * q2;
-  const R cc = sqrt(gam1 * (HH - hq2));
-  const R ic = (R)1 / cc;
+  const R cc = sqrt_(gam1 * (HH - hq2));
+  const R ic = div_((R)1, cc);
   const R K = ((R)0.5 * gam1) * ic * ic;
   const R hic = (R)0.5 * ic;
   const R un = Uv[D], u1 = Uv[T1], u2 = Uv[T2];
@@ -452,9 +515,9 @@ __device__ __forceinline__ void face_flux(const SolveDev& s, const R* __restrict
   // Local Lax-Friedrichs flux (src/lf_flux.cpp:32-99); both 1/rho from one division.
   // PERT: rhoX, EX are perturbations; dL, dR the full densities, pL, pR the
   // pressure perturbations, pfL, pfR the full pressures.
-  const R dL = PERT ? (R)s.rho_ref + rhoL : rhoL;
-  const R dR = PERT ? (R)s.rho_ref + rhoR : rhoR;
-  const R ip = (R)1 / (dL * dR);
+  const R dL = PERT ? C.rho_ref + rhoL : rhoL;
+  const R dR = PERT ? C.rho_ref + rhoR : rhoR;
+  const R ip = div_((R)1, dL * dR);
   const R iL = ip * dR, iR = ip * dL;
   R vL[3], vR[3];
 #pragma unroll
@@ -466,10 +529,10 @@ __device__ __forceinline__ void face_flux(const SolveDev& s, const R* __restrict
   const R q2R = vR[0] * vR[0] + vR[1] * vR[1] + vR[2] * vR[2];
   const R pL = gam1 * (EL - (R)0.5 * dL * q2L);
   const R pR = gam1 * (ER - (R)0.5 * dR * q2R);
-  const R pfL = PERT ? (R)s.p_ref + pL : pL;
-  const R pfR = PERT ? (R)s.p_ref + pR : pR;
+  const R pfL = PERT ? C.p_ref + pL : pL;
+  const R pfR = PERT ? C.p_ref + pR : pR;
   const R c2L = gamma * pfL * iL, c2R = gamma * pfR * iR;
-  const R cL = sqrt(c2L), cR = sqrt(c2R);
+  const R cL = sqrt_(c2L), cR = sqrt_(c2R);
   const R HL = c2L * gam1_inv + (R)0.5 * q2L;
   const R HR = c2R * gam1_inv + (R)0.5 * q2R;
   const R alpha = fmax(fabs(vR[D]) + cR, fabs(vL[D]) + cL);
@@ -484,9 +547,8 @@ __device__ __forceinline__ void face_flux(const SolveDev& s, const R* __restrict
 }
 
 template <int D, typename R>
-__global__ void __launch_bounds__(TILE_THREADS) k_inviscid(const SolveDev* __restrict__ solves,
-                                                           const TileRef* __restrict__ tiles, int ntiles,
-                                                           int stage) {
+__global__ void __launch_bounds__(kMaxThreads) k_inviscid(const SolveDev* __restrict__ solves,
+                                                          const TileRef* __restrict__ tiles, int ntiles, int stage) {
   constexpr bool MIXED = sizeof(R) == 4;
   for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
     TileCell tc = tile_cell(tiles[t], 0);
@@ -522,8 +584,8 @@ __device__ __forceinline__ R d4(const R* __restrict__ f, long long o, long long 
 }
 
 template <typename R>
-__global__ void __launch_bounds__(TILE_THREADS) k_viscous(const SolveDev* __restrict__ solves,
-                                                          const TileRef* __restrict__ tiles, int ntiles) {
+__global__ void __launch_bounds__(kMaxThreads) k_viscous(const SolveDev* __restrict__ solves,
+                                                         const TileRef* __restrict__ tiles, int ntiles) {
   constexpr bool MIXED = sizeof(R) == 4;
   for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
     TileCell tc = tile_cell(tiles[t], -NGV);
@@ -533,17 +595,18 @@ __global__ void __launch_bounds__(TILE_THREADS) k_viscous(const SolveDev* __rest
     const PrimSet<R>& P = prims_of<R>(s);
     const long long o = pad_off(s, tc.i, tc.j, tc.k);
     const long long sy = s.nx, sz = (long long)s.nx * s.ny;
-    const R idx = (R)s.inv_dx, idy = (R)s.inv_dy, idz = (R)s.inv_dz;
+    const Consts<R>& CS = consts_of<R>(s);
+    const R idx = CS.inv_dx, idy = CS.inv_dy, idz = CS.inv_dz;
     const R ux = d4<R>(P.u, o, 1, idx), uy = d4<R>(P.u, o, sy, idy), uz = d4<R>(P.u, o, sz, idz);
     const R vx = d4<R>(P.v, o, 1, idx), vy = d4<R>(P.v, o, sy, idy), vz = d4<R>(P.v, o, sz, idz);
     const R wx = d4<R>(P.w, o, 1, idx), wy = d4<R>(P.w, o, sy, idy), wz = d4<R>(P.w, o, sz, idz);
     const R Tx = d4<R>(P.T, o, 1, idx), Ty = d4<R>(P.T, o, sy, idy), Tz = d4<R>(P.T, o, sz, idz);
-    const R Tl = MIXED ? (R)s.T_ref + P.T[o] : P.T[o];
-    const R C = (R)s.C_T_inf;
+    const R Tl = MIXED ? CS.T_ref + P.T[o] : P.T[o];
+    const R C = CS.C_T_inf;
     // Sutherland's law, (1 + C) / (T + C) * T^1.5 (src/Block3d.cpp:777).
-    const R mu = ((R)1 + C) * Tl * sqrt(Tl) / (Tl + C);
+    const R mu = div_(((R)1 + C) * Tl * sqrt_(Tl), Tl + C);
     if (tc.i >= 0 && tc.i < s.IM && tc.j >= 0 && tc.j < s.JM && tc.k >= 0 && tc.k < s.KM) P.mu[o] = mu;
-    const R mr = mu * (R)s.Re_inv;
+    const R mr = mu * CS.Re_inv;
     const R m23 = (R)(2.0 / 3.0) * mr;
     const R txx = m23 * ((R)2 * ux - vy - wz);
     const R tyy = m23 * ((R)2 * vy - ux - wz);
@@ -551,7 +614,7 @@ __global__ void __launch_bounds__(TILE_THREADS) k_viscous(const SolveDev* __rest
     const R txy = mr * (uy + vx);
     const R txz = mr * (uz + wx);
     const R tyz = mr * (vz + wy);
-    const R mk = mr * (R)s.kappa;
+    const R mk = mr * CS.kappa;
     const R uu = P.u[o], vv = P.v[o], ww = P.w[o];
     const long long r = ring_off(s, tc.i, tc.j, tc.k);
     const long long RV = s.RV;
@@ -592,9 +655,8 @@ __global__ void __launch_bounds__(TILE_THREADS) k_viscous(const SolveDev* __rest
 // conserved state binary64.
 
 template <typename R>
-__global__ void __launch_bounds__(TILE_THREADS) k_update(const SolveDev* __restrict__ solves,
-                                                         const TileRef* __restrict__ tiles, int ntiles,
-                                                         int stage) {
+__global__ void __launch_bounds__(kMaxThreads) k_update(const SolveDev* __restrict__ solves,
+                                                        const TileRef* __restrict__ tiles, int ntiles, int stage) {
   constexpr bool MIXED = sizeof(R) == 4;
   for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
     TileCell tc = tile_cell(tiles[t], 0);
@@ -625,7 +687,7 @@ __global__ void __launch_bounds__(TILE_THREADS) k_update(const SolveDev* __restr
       F0 = s.F[0], F1 = s.F[1], F2 = s.F[2];
       V0 = s.Fv[0], V1 = s.Fv[1], V2 = s.Fv[2];
     }
-    const R idx = (R)s.inv_dx, idy = (R)s.inv_dy, idz = (R)s.inv_dz;
+    const R idx = consts_of<R>(s).inv_dx, idy = consts_of<R>(s).inv_dy, idz = consts_of<R>(s).inv_dz;
 
     double qn[NEQ];
 #pragma unroll
@@ -656,7 +718,7 @@ __global__ void __launch_bounds__(TILE_THREADS) k_update(const SolveDev* __restr
     MixedCell mc;
     if constexpr (MIXED) {
       mc = mixed_cell(s, qn);
-      if (!(qn[0] > 0.0) || !((float)s.p_ref + mc.p > 0.0f)) atomicOr(&ctl->status, 1);
+      if (!(qn[0] > 0.0) || !(s.cf.p_ref + mc.p > 0.0f)) atomicOr(&ctl->status, 1);
     } else {
       const double ir = 1.0 / qn[0];
       uu = qn[1] * ir, vv = qn[2] * ir, ww = qn[3] * ir;
@@ -664,7 +726,7 @@ __global__ void __launch_bounds__(TILE_THREADS) k_update(const SolveDev* __restr
       pp = s.gam1 * (qn[4] - 0.5 * qn[0] * q2);
       TT = s.gM2 * pp * ir;
       sr = sqrt(qn[0]);
-      HH = s.gamma * s.gam1_inv * pp * ir + 0.5 * q2;
+      HH = s.cd.gamma_gam1_inv * pp * ir + 0.5 * q2;
       if (!(qn[0] > 0.0) || !(pp > 0.0)) atomicOr(&ctl->status, 1);
     }
 
@@ -841,23 +903,35 @@ cudaError_t launch_layout(const SolveDev* d, int sidx, const double* src, double
   return cudaGetLastError();
 }
 
+cudaError_t launch_init_tgv(const SolveDev* d, int sidx, const TileRef* tiles, int ntiles, double p_inf,
+                            const PerturbMode* modes, int nmodes, cudaStream_t st) {
+  if (nmodes < 0 || nmodes > kMaxModes) return cudaErrorInvalidValue;
+  ModeTable mt;
+  mt.n = nmodes;
+  for (int m = 0; m < nmodes; ++m) mt.m[m] = modes[m];
+  k_init_tgv<<<grid_for(ntiles, 0), TILE_THREADS, 0, st>>>(d, sidx, tiles, ntiles, p_inf, mt);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_prims_double(const SolveDev* d, const TileRef* tiles, int ntiles, cudaStream_t st) {
   if (ntiles == 0) return cudaSuccess;
   k_prims_double<<<grid_for(ntiles, 0), TILE_THREADS, 0, st>>>(d, tiles, ntiles);
   return cudaGetLastError();
 }
 
+template <typename R>
+static void dt_reduce_ty(const SolveDev* d, const TileRef* tiles, int ntiles, double t_end, int use_t_end, int skip,
+                         const LaunchCfg& cfg, cudaStream_t st, Profiler* pf) {
+  CBNS_LAUNCH(pf, KID_DT_REDUCE, st,
+              (k_dt_reduce<R><<<grid_for(ntiles, cfg.max_ctas), 32 * cfg.tile_rows, 0, st>>>(d, tiles, ntiles, t_end,
+                                                                                             use_t_end, skip)));
+}
+
 cudaError_t launch_dt(const SolveDev* d, int nsolves, const TileRef* tiles, int ntiles, double t_end,
-                      bool use_t_end, bool mixed, cudaStream_t st, Profiler* pf) {
+                      bool use_t_end, bool mixed, const LaunchCfg& cfg, cudaStream_t st, Profiler* pf) {
   if (ntiles > 0) {
-    if (mixed)
-      CBNS_LAUNCH(pf, KID_DT_REDUCE, st,
-                  (k_dt_reduce<float><<<grid_for(ntiles, 0), TILE_THREADS, 0, st>>>(d, tiles, ntiles, t_end,
-                                                                                    use_t_end ? 1 : 0, 1)));
-    else
-      CBNS_LAUNCH(pf, KID_DT_REDUCE, st,
-                  (k_dt_reduce<double><<<grid_for(ntiles, 0), TILE_THREADS, 0, st>>>(d, tiles, ntiles, t_end,
-                                                                                     use_t_end ? 1 : 0, 1)));
+    if (mixed) dt_reduce_ty<float>(d, tiles, ntiles, t_end, use_t_end ? 1 : 0, 1, cfg, st, pf);
+    else dt_reduce_ty<double>(d, tiles, ntiles, t_end, use_t_end ? 1 : 0, 1, cfg, st, pf);
   }
   CBNS_LAUNCH(pf, KID_DT_FINALIZE, st,
               (k_dt_finalize<<<(nsolves + 127) / 128, 128, 0, st>>>(d, nsolves, t_end, use_t_end ? 1 : 0)));
@@ -865,14 +939,10 @@ cudaError_t launch_dt(const SolveDev* d, int nsolves, const TileRef* tiles, int 
 }
 
 cudaError_t launch_dt_raw(const SolveDev* d, int sidx, const TileRef* tiles, int ntiles, double* out,
-                          bool mixed, cudaStream_t st, Profiler* pf) {
+                          bool mixed, const LaunchCfg& cfg, cudaStream_t st, Profiler* pf) {
   if (ntiles > 0) {
-    if (mixed)
-      CBNS_LAUNCH(pf, KID_DT_REDUCE, st,
-                  (k_dt_reduce<float><<<grid_for(ntiles, 0), TILE_THREADS, 0, st>>>(d, tiles, ntiles, 0.0, 0, 0)));
-    else
-      CBNS_LAUNCH(pf, KID_DT_REDUCE, st,
-                  (k_dt_reduce<double><<<grid_for(ntiles, 0), TILE_THREADS, 0, st>>>(d, tiles, ntiles, 0.0, 0, 0)));
+    if (mixed) dt_reduce_ty<float>(d, tiles, ntiles, 0.0, 0, 0, cfg, st, pf);
+    else dt_reduce_ty<double>(d, tiles, ntiles, 0.0, 0, 0, cfg, st, pf);
   }
   CBNS_LAUNCH(pf, KID_DT_FINALIZE, st, (k_dt_raw<<<1, 1, 0, st>>>(d, sidx, out)));
   return cudaGetLastError();
@@ -884,22 +954,23 @@ cudaError_t launch_set_dt(const SolveDev* d, int sidx, double dt, cudaStream_t s
 }
 
 template <typename R>
-static void stage_launches(const SolveDev* d, const TileRef* tiles, int ntiles, const TileRef* ring_tiles,
-                           int nring, int stage, int max_ctas, cudaStream_t st, Profiler* pf) {
-  const int g = grid_for(ntiles, max_ctas);
-  CBNS_LAUNCH(pf, KID_INVISCID_X, st, (k_inviscid<0, R><<<g, TILE_THREADS, 0, st>>>(d, tiles, ntiles, stage)));
-  CBNS_LAUNCH(pf, KID_INVISCID_Y, st, (k_inviscid<1, R><<<g, TILE_THREADS, 0, st>>>(d, tiles, ntiles, stage)));
-  CBNS_LAUNCH(pf, KID_INVISCID_Z, st, (k_inviscid<2, R><<<g, TILE_THREADS, 0, st>>>(d, tiles, ntiles, stage)));
+static void stage_ty(const SolveDev* d, const TileRef* tiles, int ntiles, const TileRef* ring_tiles, int nring,
+                     int stage, const LaunchCfg& cfg, cudaStream_t st, Profiler* pf) {
+  const int g = grid_for(ntiles, cfg.max_ctas);
+  const int nt = 32 * cfg.tile_rows;
+  CBNS_LAUNCH(pf, KID_INVISCID_X, st, (k_inviscid<0, R><<<g, nt, 0, st>>>(d, tiles, ntiles, stage)));
+  CBNS_LAUNCH(pf, KID_INVISCID_Y, st, (k_inviscid<1, R><<<g, nt, 0, st>>>(d, tiles, ntiles, stage)));
+  CBNS_LAUNCH(pf, KID_INVISCID_Z, st, (k_inviscid<2, R><<<g, nt, 0, st>>>(d, tiles, ntiles, stage)));
   CBNS_LAUNCH(pf, KID_VISCOUS, st,
-              (k_viscous<R><<<grid_for(nring, max_ctas), TILE_THREADS, 0, st>>>(d, ring_tiles, nring)));
-  CBNS_LAUNCH(pf, KID_UPDATE, st, (k_update<R><<<g, TILE_THREADS, 0, st>>>(d, tiles, ntiles, stage)));
+              (k_viscous<R><<<grid_for(nring, cfg.max_ctas), nt, 0, st>>>(d, ring_tiles, nring)));
+  CBNS_LAUNCH(pf, KID_UPDATE, st, (k_update<R><<<g, nt, 0, st>>>(d, tiles, ntiles, stage)));
 }
 
 cudaError_t launch_stage(const SolveDev* d, const TileRef* tiles, int ntiles, const TileRef* ring_tiles,
-                         int nring, int stage, int max_ctas, bool mixed, cudaStream_t st, Profiler* pf) {
+                         int nring, int stage, const LaunchCfg& cfg, bool mixed, cudaStream_t st, Profiler* pf) {
   if (ntiles == 0) return cudaSuccess;
-  if (mixed) stage_launches<float>(d, tiles, ntiles, ring_tiles, nring, stage, max_ctas, st, pf);
-  else stage_launches<double>(d, tiles, ntiles, ring_tiles, nring, stage, max_ctas, st, pf);
+  if (mixed) stage_ty<float>(d, tiles, ntiles, ring_tiles, nring, stage, cfg, st, pf);
+  else stage_ty<double>(d, tiles, ntiles, ring_tiles, nring, stage, cfg, st, pf);
   return cudaGetLastError();
 }
 

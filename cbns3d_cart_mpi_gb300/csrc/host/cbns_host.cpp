@@ -1,5 +1,6 @@
 // cbns_host.cpp — host-side pieces of the solver kept on the CPU (include/cbns_host.h).
 #include "../../../include/cbns_host.h"
+#include "../cbns_modes.h"
 
 #include <cmath>
 #include <cstdint>
@@ -85,14 +86,6 @@ void derive(cbns_params* p) {
   p->C_dt_v = (a < g ? g : a) * p->Re_inv;
 }
 
-uint64_t splitmix64(uint64_t& s) {
-  uint64_t z = (s += 0x9E3779B97F4A7C15ull);
-  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
-  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
-  return z ^ (z >> 31);
-}
-double uniform01(uint64_t& s) { return (double)(splitmix64(s) >> 11) * (1.0 / 9007199254740992.0); }
-
 }  // namespace
 
 extern "C" {
@@ -152,33 +145,7 @@ cbns_status cbns_host_initial_condition_perturbed(const cbns_params* p, uint32_t
   if (IM == 0 || JM == 0 || KM == 0) return CBNS_ERR_BAD_DIMS;
   std::vector<double> u, v, w, pr, rho;
   tgv_state(p, IM, JM, KM, 0, 0, 0, u, v, w, pr, rho);
-  // Modes: integer k with 1 <= |k| <= kmax, a random unit direction a
-  // perpendicular to k (so the mode is divergence-free), a random phase and a
-  // random weight; the weights are normalised so their sum is amp.
-  uint64_t s = seed;
-  struct Mode {
-    double k[3], a[3], phase, weight;
-  };
-  std::vector<Mode> modes;
-  double wsum = 0.0;
-  while ((int)modes.size() < nmodes) {
-    Mode m;
-    for (int d = 0; d < 3; ++d) m.k[d] = std::floor(uniform01(s) * (2 * kmax + 1)) - kmax;
-    double k2 = m.k[0] * m.k[0] + m.k[1] * m.k[1] + m.k[2] * m.k[2];
-    if (k2 < 1.0 || k2 > (double)kmax * kmax) continue;
-    double r[3], a2 = 0.0;
-    for (int d = 0; d < 3; ++d) r[d] = uniform01(s) * 2.0 - 1.0;
-    m.a[0] = m.k[1] * r[2] - m.k[2] * r[1];
-    m.a[1] = m.k[2] * r[0] - m.k[0] * r[2];
-    m.a[2] = m.k[0] * r[1] - m.k[1] * r[0];
-    for (int d = 0; d < 3; ++d) a2 += m.a[d] * m.a[d];
-    if (a2 < 1e-12) continue;
-    for (int d = 0; d < 3; ++d) m.a[d] /= std::sqrt(a2);
-    m.phase = uniform01(s) * 2.0 * PI;
-    m.weight = 0.5 + uniform01(s);
-    wsum += m.weight;
-    modes.push_back(m);
-  }
+  const std::vector<cbns::PerturbMode> modes = cbns::draw_modes(seed, amp, nmodes, kmax);
   std::vector<double> x(IM + 1), y(JM + 1), z(KM + 1);
   cbns_host_gen_mesh(p, IM, JM, KM, 0, 0, 0, x.data(), y.data(), z.data());
   const double dx = 2.0 * PI / p->IM, dy = 2.0 * PI / p->JM, dz = 2.0 * PI / p->KM;
@@ -187,10 +154,9 @@ cbns_status cbns_host_initial_condition_perturbed(const cbns_params* p, uint32_t
       for (uint32_t i = 0; i < IM; i++) {
         double xc[3] = {x[i] + 0.5 * dx, y[j] + 0.5 * dy, z[k] + 0.5 * dz};
         size_t c = i + (size_t)IM * (j + (size_t)JM * k);
-        for (const Mode& m : modes) {
-          double amp_m = amp * m.weight / wsum;
+        for (const cbns::PerturbMode& m : modes) {
           double ph = m.k[0] * xc[0] + m.k[1] * xc[1] + m.k[2] * xc[2] + m.phase;
-          double cph = std::cos(ph) * amp_m;
+          double cph = std::cos(ph);
           u[c] += m.a[0] * cph;
           v[c] += m.a[1] * cph;
           w[c] += m.a[2] * cph;

@@ -79,6 +79,12 @@ class Solver:
             raise ValueError("Q has %d values, %d expected" % (Q.size, int(np.prod(self.shape))))
         _check(_lib.gpu().cbns_upload_Q(self._h, _ptr(Q), self.params.t_cur if t is None else t), "cbns_upload_Q")
 
+    def init_tgv(self, seed=0, amp=0.0, nmodes=0, kmax=4, t=None):
+        """Build the Taylor-Green state (plus the seeded perturbation when nmodes > 0)
+        on the device, then the start-up fill (cbns_init_tgv)."""
+        _check(_lib.gpu().cbns_init_tgv(self._h, int(seed), float(amp), int(nmodes), int(kmax),
+                                        self.params.t_cur if t is None else t), "cbns_init_tgv")
+
     def download_Q(self, out=None):
         out = np.empty(self.shape) if out is None else out
         _check(_lib.gpu().cbns_download_Q(self._h, _ptr(out)), "cbns_download_Q")
@@ -149,6 +155,128 @@ class Solver:
         nbytes, prec = ctypes.c_uint64(), ctypes.c_int()
         _check(_lib.gpu().cbns_get_info(self._h, dims, ctypes.byref(nbytes), ctypes.byref(prec)), "cbns_get_info")
         return {"dims": tuple(dims), "device_bytes": nbytes.value, "precision": prec.value}
+
+
+class Batch:
+    """Many independent solves stepped together (include/cbns_gpu.h, cbns_batch_*):
+    one launch per kernel over the flattened tiles of every solve, a batch step
+    replayed as one CUDA graph, each solve stopping at its own t_end."""
+
+    def __init__(self, solvers):
+        self.solvers = list(solvers)
+        arr = (ctypes.c_void_p * len(self.solvers))(*[s._h.value for s in self.solvers])
+        b = ctypes.c_void_p()
+        _check(_lib.gpu().cbns_batch_create(arr, len(self.solvers), ctypes.byref(b)), "cbns_batch_create")
+        self._b = b
+
+    def close(self):
+        if getattr(self, "_b", None) is not None and self._b.value:
+            _lib.gpu().cbns_batch_destroy(self._b)
+            self._b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def run(self, nsteps):
+        """nsteps batch steps; returns the steps each solve has taken since creation."""
+        out = (ctypes.c_uint32 * len(self.solvers))()
+        _check(_lib.gpu().cbns_batch_run(self._b, int(nsteps), out), "cbns_batch_run")
+        return list(out)
+
+    @property
+    def config(self):
+        c = _lib.LaunchConfig()
+        _check(_lib.gpu().cbns_batch_get_config(self._b, ctypes.byref(c)), "cbns_batch_get_config")
+        return {"tile_rows": c.tile_rows, "ctas_per_sm": c.ctas_per_sm}
+
+    def set_config(self, tile_rows=4, ctas_per_sm=0):
+        c = _lib.LaunchConfig(tile_rows, ctas_per_sm)
+        _check(_lib.gpu().cbns_batch_set_config(self._b, ctypes.byref(c)), "cbns_batch_set_config")
+
+    def autotune(self, reps=2):
+        """Time every candidate launch shape over `reps` steps, keep the fastest, and
+        restore the solves' state; returns [(tile_rows, ctas_per_sm, ms/step)]."""
+        ms = (ctypes.c_double * 64)()
+        n = ctypes.c_int()
+        _check(_lib.gpu().cbns_batch_autotune(self._b, int(reps), ms, 64, ctypes.byref(n)), "cbns_batch_autotune")
+        cands = [(r, c) for r in (2, 4, 8) for c in (0, 2, 4, 8)]
+        return [(r, c, ms[i]) for i, (r, c) in enumerate(cands[:n.value])]
+
+    @property
+    def stream(self):
+        return _lib.gpu().cbns_batch_stream(self._b)
+
+
+def footprint(IM, JM, KM, precision="fp64"):
+    """Device bytes a solve of these extents holds (cbns_footprint)."""
+    b = ctypes.c_uint64()
+    _check(_lib.gpu().cbns_footprint(IM, JM, KM, PRECISIONS[precision], ctypes.byref(b)), "cbns_footprint")
+    return b.value
+
+
+class Server:
+    """Continuous-batching request loop (include/cbns_gpu.h, cbns_server_*)."""
+
+    def __init__(self, precision="fp64", memory_budget_bytes=0, max_active=0, steps_per_round=10, tile_rows=0,
+                 ctas_per_sm=0):
+        opts = _lib.ServerOpts(PRECISIONS[precision], int(memory_budget_bytes), int(max_active),
+                               int(steps_per_round), int(tile_rows), int(ctas_per_sm))
+        sv = ctypes.c_void_p()
+        _check(_lib.gpu().cbns_server_create(ctypes.byref(opts), ctypes.byref(sv)), "cbns_server_create")
+        self._s = sv
+        self.precision = precision
+
+    def close(self):
+        if getattr(self, "_s", None) is not None and self._s.value:
+            _lib.gpu().cbns_server_destroy(self._s)
+            self._s = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit(self, params, Q0, keep_state=False):
+        rid = ctypes.c_uint64()
+        Q0 = np.ascontiguousarray(Q0, dtype=np.float64)
+        _check(_lib.gpu().cbns_server_submit(self._s, ctypes.byref(params), params.IM, params.JM, params.KM,
+                                             _ptr(Q0), int(keep_state), ctypes.byref(rid)), "cbns_server_submit")
+        return rid.value
+
+    def submit_tgv(self, params, seed=0, amp=0.0, nmodes=0, kmax=4, keep_state=False):
+        rid = ctypes.c_uint64()
+        _check(_lib.gpu().cbns_server_submit_tgv(self._s, ctypes.byref(params), params.IM, params.JM, params.KM,
+                                                 int(seed), float(amp), int(nmodes), int(kmax), int(keep_state),
+                                                 ctypes.byref(rid)), "cbns_server_submit_tgv")
+        return rid.value
+
+    def cancel(self, rid):
+        _check(_lib.gpu().cbns_server_cancel(self._s, int(rid)), "cbns_server_cancel")
+
+    def wait(self, rid, timeout=-1.0):
+        """Block until the request finishes; returns its info dict (status included)."""
+        info = _lib.RequestInfo()
+        st = _lib.gpu().cbns_server_wait(self._s, int(rid), float(timeout), ctypes.byref(info))
+        out = {f: getattr(info, f) for f, _ in _lib.RequestInfo._fields_}
+        out["status"] = st
+        return out
+
+    def result(self, rid, shape):
+        Q = np.empty(shape)
+        _check(_lib.gpu().cbns_server_result(self._s, int(rid), _ptr(Q)), "cbns_server_result")
+        return Q
+
+    def release(self, rid):
+        _check(_lib.gpu().cbns_server_release(self._s, int(rid)), "cbns_server_release")
+
+    def stats(self):
+        st = _lib.ServerStats()
+        _check(_lib.gpu().cbns_server_get_stats(self._s, ctypes.byref(st)), "cbns_server_get_stats")
+        return {f: getattr(st, f) for f, _ in _lib.ServerStats._fields_}
 
 
 def probe_peak(fp64=True):

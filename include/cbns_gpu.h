@@ -42,7 +42,8 @@ typedef enum cbns_status {
   CBNS_ERR_TIMEOUT = -6,          /* a bounded device-side wait gave up */
   CBNS_ERR_NO_DEVICE = -7,        /* no CUDA device, or not an sm_103 device */
   CBNS_ERR_IO = -8,               /* host file could not be read or written */
-  CBNS_ERR_FORMAT = -9            /* host file is truncated or its dimensions do not match */
+  CBNS_ERR_FORMAT = -9,           /* host file is truncated or its dimensions do not match */
+  CBNS_ERR_CANCELLED = -10        /* a serving request was cancelled or its server stopped */
 } cbns_status;
 
 typedef enum cbns_precision {
@@ -94,6 +95,14 @@ cbns_status cbns_destroy(cbns_handle* h);
  * Block3d::initial_condition gives it (src/Block3d.cpp:265).  Sets t_cur = t. */
 cbns_status cbns_upload_Q(cbns_handle* h, const double* Q, double t);
 
+/* Device-side initial condition (no host state): the Taylor-Green state of
+ * Block3d::initial_condition + calc_conservative (src/Block3d.cpp:237-300),
+ * plus, when nmodes > 0 (at most 64), the project-defined solenoidal velocity
+ * perturbation that cbns_host_initial_condition_perturbed draws from the same
+ * seed; then the start-up sequence of cbns_upload_Q.  Equal to uploading the
+ * host-built state up to the last-place differences of device sin/cos. */
+cbns_status cbns_init_tgv(cbns_handle* h, uint64_t seed, double amp, int nmodes, int kmax, double t);
+
 /* Block3d::get_Q / get_Q_p (src/Block3d.cpp:302-316): copy Q or Q_p, ghosts
  * included, into a host array of NEQ*IM_G*JM_G*KM_G doubles. */
 cbns_status cbns_download_Q(cbns_handle* h, double* Q);
@@ -140,9 +149,103 @@ cbns_status cbns_check_state(cbns_handle* h);
 /* The handle's cudaStream_t (as void*), for callers that time or order work. */
 void* cbns_stream(cbns_handle* h);
 
+/* Device bytes cbns_create would allocate for a block of these extents (the
+ * admission test of the serving loop). */
+cbns_status cbns_footprint(uint32_t IM, uint32_t JM, uint32_t KM, int precision, uint64_t* bytes);
+
 /* Block extents and device bytes the handle holds. */
 cbns_status cbns_get_info(cbns_handle* h, uint32_t dims[3], uint64_t* device_bytes,
                           int* precision);
+
+/* ---- Batched ensembles ---------------------------------------------------
+ * A batch steps many independent solves (uneven grid sizes and parameters)
+ * together: each kernel of a step is one launch over a flattened table of the
+ * tiles of every solve, optionally persistent (a fixed number of CTAs per SM
+ * walking the table), and a step of the whole batch is one replayed CUDA graph.
+ * Every solve keeps its own t_cur, t_end, dt and is_finished test on the
+ * device, so solves that finish early stop while the others go on.  The handles
+ * keep their state; the batch owns only descriptor and tile tables.  All handles
+ * must be on one device and share one precision.  Results are bitwise those of
+ * stepping each handle alone. */
+typedef struct cbns_batch cbns_batch;
+
+typedef struct cbns_launch_config {
+  int tile_rows;     /* rows of 32 cells per tile (CTA of 32*tile_rows threads): 2, 4 or 8 */
+  int ctas_per_sm;   /* persistent CTAs per SM; 0 = one CTA per tile (not persistent) */
+} cbns_launch_config;
+
+cbns_status cbns_batch_create(cbns_handle* const* handles, int n, cbns_batch** out);
+cbns_status cbns_batch_destroy(cbns_batch* b);
+/* nsteps batch steps (each solve stops at its own t_end); per-solve steps taken
+ * since the batch was created go to steps_out[n] (may be NULL). */
+cbns_status cbns_batch_run(cbns_batch* b, uint32_t nsteps, uint32_t* steps_out);
+cbns_status cbns_batch_set_config(cbns_batch* b, const cbns_launch_config* cfg);
+cbns_status cbns_batch_get_config(cbns_batch* b, cbns_launch_config* cfg);
+/* Project autotuner: times `reps` steps of the batch for each candidate launch
+ * configuration, keeps the fastest, and restores every solve's device state
+ * (the timing steps leave no trace).  ms_out[i] receives the time per step of
+ * candidate i (up to cap entries), *ncand their count; both may be NULL. */
+cbns_status cbns_batch_autotune(cbns_batch* b, int reps, double* ms_out, int cap, int* ncand);
+void* cbns_batch_stream(cbns_batch* b);
+
+/* ---- Serving ---------------------------------------------------------------
+ * A continuous-batching request loop.  A worker thread admits queued requests
+ * (first come, first served among those that fit) while their device footprint
+ * (cbns_footprint) fits the memory budget and fewer than max_active run; each
+ * admitted request's state is created on, and stays resident on, the device;
+ * all running requests step together as one batch for steps_per_round steps;
+ * requests that reach their t_end (or fail, or are cancelled) are retired and
+ * their memory goes to the next ones, so requests arriving while others run
+ * join at the next round.  Each request's result is bitwise the one stepping it
+ * alone gives.  Times in cbns_request_info are seconds on the server's clock. */
+typedef struct cbns_server cbns_server;
+
+typedef struct cbns_server_opts {
+  int precision;                /* CBNS_FP64 or CBNS_FP32_MIXED */
+  uint64_t memory_budget_bytes; /* device bytes for request state; 0 = 80% of free memory */
+  uint32_t max_active;          /* most requests stepped together; 0 = no limit */
+  uint32_t steps_per_round;     /* batch steps between scheduling rounds; 0 = 10 */
+  int tile_rows;                /* batch launch shape (cbns_launch_config); 0 = default */
+  int ctas_per_sm;
+} cbns_server_opts;
+
+typedef struct cbns_request_info {
+  int status;        /* CBNS_OK, or the error that retired the request */
+  uint32_t steps;    /* RK3 steps taken */
+  double t_final;    /* simulated time reached */
+  double ke, enstrophy;  /* diagnostics of the final state (status CBNS_OK) */
+  double submit_s, admit_s, done_s;
+  uint64_t device_bytes;
+} cbns_request_info;
+
+typedef struct cbns_server_stats {
+  uint64_t submitted, completed, failed;
+  uint64_t rounds, batch_builds, cell_steps;
+  uint32_t peak_active, queued;
+  uint64_t budget_bytes, used_bytes;
+  double clock_s;
+} cbns_server_stats;
+
+cbns_status cbns_server_create(const cbns_server_opts* opts, cbns_server** out);
+/* Cancels queued and running requests and joins the worker. */
+cbns_status cbns_server_destroy(cbns_server* s);
+/* A request with a host initial state (get_idx_Q layout, copied at submit).
+ * p->t_cur and p->t_end give its start and end time.  keep_state != 0 keeps the
+ * final state for cbns_server_result. */
+cbns_status cbns_server_submit(cbns_server* s, const cbns_params* p, uint32_t IM, uint32_t JM, uint32_t KM,
+                               const double* Q0, int keep_state, uint64_t* id);
+/* A request whose initial state is built on the device (cbns_init_tgv). */
+cbns_status cbns_server_submit_tgv(cbns_server* s, const cbns_params* p, uint32_t IM, uint32_t JM, uint32_t KM,
+                                   uint64_t seed, double amp, int nmodes, int kmax, int keep_state,
+                                   uint64_t* id);
+cbns_status cbns_server_cancel(cbns_server* s, uint64_t id);
+/* Waits for a request (timeout_s < 0: no limit; CBNS_ERR_TIMEOUT if it runs out)
+ * and returns its final status. */
+cbns_status cbns_server_wait(cbns_server* s, uint64_t id, double timeout_s, cbns_request_info* info);
+cbns_status cbns_server_result(cbns_server* s, uint64_t id, double* Q_out);
+/* Forgets a finished request (frees its stored result). */
+cbns_status cbns_server_release(cbns_server* s, uint64_t id);
+cbns_status cbns_server_get_stats(cbns_server* s, cbns_server_stats* out);
 
 /* Per-kernel timing.  Between cbns_profile_begin and cbns_profile_end every kernel
  * the handle launches is bracketed by CUDA events on its stream and launched
