@@ -87,7 +87,8 @@ def build(verbose=False, extra_nvcc=()):
         path = os.path.join(CSRC, src)
         obj = os.path.join(objdir, os.path.basename(src) + ".o")
         if _stale(obj, [path] + hdrs + [__file__]):
-            _atomic(lambda out: ["g++", "-O2", "-std=c++17", "-fPIC", "-Wall", "-c", path, "-o", out], obj)
+            _atomic(lambda out: ["g++", "-O2", "-std=c++17", "-fPIC", "-Wall", "-pthread", "-c", path, "-o", out],
+                    obj)
         return obj
 
     with ThreadPoolExecutor(max_workers=max(2, os.cpu_count() or 2)) as ex:
@@ -105,7 +106,7 @@ def build(verbose=False, extra_nvcc=()):
         _atomic(lambda out: ["g++", "-shared", "-o", out] + host_objs, HOST_LIB)
     if _stale(DRIVER, [drv_obj, GPU_LIB, HOST_LIB]):
         _atomic(lambda out: ["g++", "-o", out, drv_obj, "-L" + LIB, "-lcbns_gpu", "-lcbns_host",
-                             "-L" + cudalib, "-lcudart", "-Wl,-rpath,$ORIGIN", "-Wl,-rpath," + cudalib],
+                             "-L" + cudalib, "-lcudart", "-pthread", "-Wl,-rpath,$ORIGIN", "-Wl,-rpath," + cudalib],
                 DRIVER)
     if verbose:
         for p in (GPU_LIB, HOST_LIB, DRIVER):

@@ -271,34 +271,42 @@ __device__ __forceinline__ double dt_speed(const SolveDev& s, long long o) {
   return (double)(t1 + t2 + t3);
 }
 
+// Each CTA walks its tiles (grid stride) keeping a running per-thread maximum,
+// and folds it into the solve's control block (one block reduction and one
+// atomicMax) only when the next tile belongs to another solve or the walk ends.
+// Tiles of one solve are contiguous in the table, so a bounded grid issues
+// about one atomic per CTA instead of one per tile.
 template <typename R>
 __global__ void __launch_bounds__(kMaxThreads) k_dt_reduce(const SolveDev* __restrict__ solves,
                                                            const TileRef* __restrict__ tiles, int ntiles,
                                                            double t_end, int use_t_end, int skip_finished) {
   __shared__ double red[kMaxThreads / 32];
   const int nwarps = (int)(blockDim.x / 32);
+  double run = 0.0;
   for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
     TileCell tc = tile_cell(tiles[t], 0);
     const SolveDev& s = solves[tc.s];
     const SolveCtl* ctl = s.ctl;
     const double te = use_t_end ? t_end : ctl->t_end;
-    if (skip_finished && ctl->t_cur + 1.0e-5 > te) continue;  // uniform over the tile
-    double sm = 0.0;
-    if (tc.i < s.IM && tc.j < s.JM) {
+    const bool live = !(skip_finished && ctl->t_cur + 1.0e-5 > te);  // uniform over the tile
+    if (live && tc.i < s.IM && tc.j < s.JM) {
       double sum = dt_speed<R>(s, pad_off(s, tc.i, tc.j, tc.k));
-      sm = (sum > 0.0) ? sum : 0.0;  // a NaN is skipped, as the reference's ternary does
+      if (sum > run) run = sum;  // a NaN is skipped, as the reference's ternary does
     }
-    sm = warp_max(sm);
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = sm;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      double m = red[0];
-#pragma unroll
-      for (int a = 1; a < nwarps; ++a) m = fmax(m, red[a]);
-      // Positive doubles order like their bit patterns.
-      atomicMax(&s.ctl->smax_bits, (unsigned long long)__double_as_longlong(m));
+    const int tn = t + (int)gridDim.x;
+    const bool flush = tn >= ntiles || tiles[tn].solve != tiles[t].solve;  // uniform over the CTA
+    if (flush) {
+      double m = warp_max(run);
+      if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        for (int a = 1; a < nwarps; ++a) m = fmax(m, red[a]);
+        // Positive doubles order like their bit patterns.
+        if (m > 0.0) atomicMax(&s.ctl->smax_bits, (unsigned long long)__double_as_longlong(m));
+      }
+      __syncthreads();
+      run = 0.0;
     }
-    __syncthreads();
   }
 }
 
@@ -341,7 +349,7 @@ __global__ void k_set_dt(const SolveDev* __restrict__ solves, int sidx, double d
 // (sum w_k f_k) / (sum w_k).  Multiplying numerator and denominator by
 // 10 * IS_1^2 IS_2^2 IS_3^2 gives the same value with one division,
 //   num = a2 a3 f1 + 6 a1 a3 f2 + 3 a1 a2 f3,  den = a2 a3 + 6 a1 a3 + 3 a1 a2,
-// a_k = IS_k^2; the division is deferred so five of them can share one.
+// a_k = IS_k^2; the division is deferred so the ten of a face can share one.
 // (IS_k >= 1e-6, so den >= 1e-23: inside binary32's normal range too.)
 
 template <typename R>
@@ -349,64 +357,80 @@ struct Weno {
   R num, den;
 };
 
+// Both reconstructions of one characteristic field at a face: the left-biased
+// stencil (v0..v4) and the mirrored right-biased one (v5..v1), v = cells c-3..c+2.
+// The mirrored stencil's second and third smoothness indicators use the same
+// second differences as the left one's third and second, so 13/12*D is formed
+// once for the four distinct D; otherwise the formulas above, applied twice.
 template <typename R>
-__device__ __forceinline__ Weno<R> weno5_parts(R a, R b, R c, R d, R e) {
+__device__ __forceinline__ void weno5_pair(const R (&v)[6], Weno<R>& L, Weno<R>& Rt) {
   const R eps = (R)1.0e-6;
   const R c13 = (R)(13.0 / 12.0);
-  R d1 = a - (R)2 * b + c;
-  R d2 = a - (R)4 * b + (R)3 * c;
-  R d3 = b - (R)2 * c + d;
-  R d4 = b - d;
-  R d5 = c - (R)2 * d + e;
-  R d6 = (R)3 * c - (R)4 * d + e;
-  R is1 = c13 * d1 * d1 + (R)0.25 * d2 * d2 + eps;
-  R is2 = c13 * d3 * d3 + (R)0.25 * d4 * d4 + eps;
-  R is3 = c13 * d5 * d5 + (R)0.25 * d6 * d6 + eps;
-  R a1 = is1 * is1, a2 = is2 * is2, a3 = is3 * is3;
-  R p1 = a2 * a3;
-  R p2 = ((R)6 * a1) * a3;
-  R p3 = ((R)3 * a1) * a2;
+  const R D1 = v[0] - (R)2 * v[1] + v[2];
+  const R D2 = v[1] - (R)2 * v[2] + v[3];
+  const R D3 = v[2] - (R)2 * v[3] + v[4];
+  const R D4 = v[3] - (R)2 * v[4] + v[5];
+  const R C1 = c13 * D1, C2 = c13 * D2, C3 = c13 * D3, C4 = c13 * D4;
   const R s6 = (R)(1.0 / 6.0);
-  R f1 = ((R)2 * s6) * a - ((R)7 * s6) * b + ((R)11 * s6) * c;
-  R f2 = -s6 * b + ((R)5 * s6) * c + ((R)2 * s6) * d;
-  R f3 = ((R)2 * s6) * c + ((R)5 * s6) * d - s6 * e;
-  Weno<R> r;
-  r.num = p1 * f1 + p2 * f2 + p3 * f3;
-  r.den = p1 + p2 + p3;
-  return r;
-}
-
-// r[n] = num[n] / den[n] for five parts.  Binary64: one division (Montgomery's
-// simultaneous inversion); every den lies in [1e-23, 1e61] unless a smoothness
-// indicator exceeds ~1e15, and outside [1e-300, 1e300] each quotient is divided on
-// its own.  Binary32: a product of five dens leaves the normal range, and the
-// binary32 pipe divides cheaply, so each quotient is divided.
-__device__ __forceinline__ void weno_divide5(const Weno<double> (&w)[5], double (&r)[5]) {
-  double p1 = w[0].den;
-  double p2 = p1 * w[1].den;
-  double p3 = p2 * w[2].den;
-  double p4 = p3 * w[3].den;
-  double p5 = p4 * w[4].den;
-  if (p5 > 1.0e-300 && p5 < 1.0e300) {
-    double inv = 1.0 / p5;
-    r[4] = w[4].num * (inv * p4);
-    inv *= w[4].den;
-    r[3] = w[3].num * (inv * p3);
-    inv *= w[3].den;
-    r[2] = w[2].num * (inv * p2);
-    inv *= w[2].den;
-    r[1] = w[1].num * (inv * p1);
-    inv *= w[1].den;
-    r[0] = w[0].num * inv;
-  } else {
-#pragma unroll
-    for (int n = 0; n < 5; ++n) r[n] = w[n].num / w[n].den;
+  {
+    const R e1 = v[0] - (R)4 * v[1] + (R)3 * v[2];
+    const R e2 = v[1] - v[3];
+    const R e3 = (R)3 * v[2] - (R)4 * v[3] + v[4];
+    const R is1 = C1 * D1 + (R)0.25 * e1 * e1 + eps;
+    const R is2 = C2 * D2 + (R)0.25 * e2 * e2 + eps;
+    const R is3 = C3 * D3 + (R)0.25 * e3 * e3 + eps;
+    const R a1 = is1 * is1, a2 = is2 * is2, a3 = is3 * is3;
+    const R p1 = a2 * a3, p2 = ((R)6 * a1) * a3, p3 = ((R)3 * a1) * a2;
+    const R f1 = ((R)2 * s6) * v[0] - ((R)7 * s6) * v[1] + ((R)11 * s6) * v[2];
+    const R f2 = -s6 * v[1] + ((R)5 * s6) * v[2] + ((R)2 * s6) * v[3];
+    const R f3 = ((R)2 * s6) * v[2] + ((R)5 * s6) * v[3] - s6 * v[4];
+    L.num = p1 * f1 + p2 * f2 + p3 * f3;
+    L.den = p1 + p2 + p3;
+  }
+  {
+    const R e1 = v[5] - (R)4 * v[4] + (R)3 * v[3];
+    const R e2 = v[4] - v[2];
+    const R e3 = (R)3 * v[3] - (R)4 * v[2] + v[1];
+    const R is1 = C4 * D4 + (R)0.25 * e1 * e1 + eps;
+    const R is2 = C3 * D3 + (R)0.25 * e2 * e2 + eps;
+    const R is3 = C2 * D2 + (R)0.25 * e3 * e3 + eps;
+    const R a1 = is1 * is1, a2 = is2 * is2, a3 = is3 * is3;
+    const R p1 = a2 * a3, p2 = ((R)6 * a1) * a3, p3 = ((R)3 * a1) * a2;
+    const R f1 = ((R)2 * s6) * v[5] - ((R)7 * s6) * v[4] + ((R)11 * s6) * v[3];
+    const R f2 = -s6 * v[4] + ((R)5 * s6) * v[3] + ((R)2 * s6) * v[2];
+    const R f3 = ((R)2 * s6) * v[3] + ((R)5 * s6) * v[2] - s6 * v[1];
+    Rt.num = p1 * f1 + p2 * f2 + p3 * f3;
+    Rt.den = p1 + p2 + p3;
   }
 }
 
-__device__ __forceinline__ void weno_divide5(const Weno<float> (&w)[5], float (&r)[5]) {
+// r[n] = num[n] / den[n] for ten parts (both states of a face).  Binary64: one
+// division (Montgomery's simultaneous inversion); every den lies in
+// [1e-23, 1e30] unless a smoothness indicator exceeds ~1e7, and outside
+// [1e-300, 1e300] for the product each quotient is divided on its own.
+// Binary32: each quotient is divided (the binary32 pipe divides cheaply).
+__device__ __forceinline__ void weno_divide10(const Weno<double> (&w)[10], double (&r)[10]) {
+  double pre[10];
+  pre[0] = w[0].den;
 #pragma unroll
-  for (int n = 0; n < 5; ++n) r[n] = div_(w[n].num, w[n].den);
+  for (int n = 1; n < 10; ++n) pre[n] = pre[n - 1] * w[n].den;
+  if (pre[9] > 1.0e-300 && pre[9] < 1.0e300) {
+    double inv = 1.0 / pre[9];
+#pragma unroll
+    for (int n = 9; n > 0; --n) {
+      r[n] = w[n].num * (inv * pre[n - 1]);
+      inv *= w[n].den;
+    }
+    r[0] = w[0].num * inv;
+  } else {
+#pragma unroll
+    for (int n = 0; n < 10; ++n) r[n] = w[n].num / w[n].den;
+  }
+}
+
+__device__ __forceinline__ void weno_divide10(const Weno<float> (&w)[10], float (&r)[10]) {
+#pragma unroll
+  for (int n = 0; n < 10; ++n) r[n] = div_(w[n].num, w[n].den);
 }
 
 // ---------------------------------------------------------------------------
@@ -453,8 +477,9 @@ __device__ __forceinline__ void face_flux(const SolveDev& s, const R* __restrict
   const R HH = (sL * P.H[cl] + sR * P.H[c]) * inv;
   const R q2 = Uv[0] * Uv[0] + Uv[1] * Uv[1] + Uv[2] * Uv[2];
   const R hq2 = (R)0.5 * q2;
-  const R cc = sqrt_(gam1 * (HH - hq2));
-  const R ic = div_((R)1, cc);
+  const R c2 = gam1 * (HH - hq2);
+  const R ic = rsqrt(c2);  // 1/c; c = c^2 * (1/c)
+  const R cc = c2 * ic;
   const R K = ((R)0.5 * gam1) * ic * ic;
   const R hic = (R)0.5 * ic;
   const R un = Uv[D], u1 = Uv[T1], u2 = Uv[T2];
@@ -481,16 +506,16 @@ __device__ __forceinline__ void face_flux(const SolveDev& s, const R* __restrict
   // (src/Block3d.cpp:591-607, src/weno.cpp:77-152).
   R rl[NEQ], rr[NEQ];
   {
-    Weno<R> wl[NEQ];
+    Weno<R> wp[2 * NEQ];
 #pragma unroll
-    for (int n = 0; n < NEQ; ++n) wl[n] = weno5_parts<R>(w[n][0], w[n][1], w[n][2], w[n][3], w[n][4]);
-    weno_divide5(wl, rl);
-  }
-  {
-    Weno<R> wr[NEQ];
+    for (int n = 0; n < NEQ; ++n) weno5_pair<R>(w[n], wp[n], wp[NEQ + n]);
+    R q[2 * NEQ];
+    weno_divide10(wp, q);
 #pragma unroll
-    for (int n = 0; n < NEQ; ++n) wr[n] = weno5_parts<R>(w[n][5], w[n][4], w[n][3], w[n][2], w[n][1]);
-    weno_divide5(wr, rr);
+    for (int n = 0; n < NEQ; ++n) {
+      rl[n] = q[n];
+      rr[n] = q[NEQ + n];
+    }
   }
 
   // Back to conserved variables (perturbations when PERT).
@@ -730,36 +755,43 @@ __global__ void __launch_bounds__(kMaxThreads) k_update(const SolveDev* __restri
       if (!(qn[0] > 0.0) || !(pp > 0.0)) atomicOr(&ctl->status, 1);
     }
 
-    int xi[3], yi[3], zi[3];
-    int nxi = 0, nyi = 0, nzi = 0;
-    xi[nxi++] = i;
-    if (i < NG) xi[nxi++] = i + s.IM;
-    if (i >= s.IM - NG) xi[nxi++] = i - s.IM;
-    yi[nyi++] = j;
-    if (j < NG) yi[nyi++] = j + s.JM;
-    if (j >= s.JM - NG) yi[nyi++] = j - s.JM;
-    zi[nzi++] = k;
-    if (k < NG) zi[nzi++] = k + s.KM;
-    if (k >= s.KM - NG) zi[nzi++] = k - s.KM;
-    for (int c3 = 0; c3 < nzi; ++c3)
-      for (int b2 = 0; b2 < nyi; ++b2)
-        for (int a1 = 0; a1 < nxi; ++a1) {
-          const long long d = pad_off(s, xi[a1], yi[b2], zi[c3]);
+    // The cell itself, then its periodic images in the ghost layers: along each
+    // axis a cell within NG of either end has one image (two when the extent is
+    // below 2*NG).  Most cells have none, and take the first branch only.
+    auto store = [&](long long d) {
 #pragma unroll
-          for (int n = 0; n < NEQ; ++n) out[n * V + d] = qn[n];
-          if constexpr (MIXED) {
-            store_mixed(s, d, mc);
-          } else {
-            s.pd.rho[d] = qn[0];
-            s.pd.u[d] = uu;
-            s.pd.v[d] = vv;
-            s.pd.w[d] = ww;
-            s.pd.p[d] = pp;
-            s.pd.T[d] = TT;
-            s.pd.srho[d] = sr;
-            s.pd.H[d] = HH;
-          }
-        }
+      for (int n = 0; n < NEQ; ++n) out[n * V + d] = qn[n];
+      if constexpr (MIXED) {
+        store_mixed(s, d, mc);
+      } else {
+        s.pd.rho[d] = qn[0];
+        s.pd.u[d] = uu;
+        s.pd.v[d] = vv;
+        s.pd.w[d] = ww;
+        s.pd.p[d] = pp;
+        s.pd.T[d] = TT;
+        s.pd.srho[d] = sr;
+        s.pd.H[d] = HH;
+      }
+    };
+    store(o);
+    const bool xl = i < NG, xh = i >= s.IM - NG, yl = j < NG, yh = j >= s.JM - NG, zl = k < NG,
+               zh = k >= s.KM - NG;
+    if (xl || xh || yl || yh || zl || zh) {
+      // Image offsets per axis: slot 0 = the cell, 1 = +extent, 2 = -extent.
+      const long long sy = s.nx, sz = (long long)s.nx * s.ny;
+      const long long dx3[3] = {0, (long long)s.IM, -(long long)s.IM};
+      const long long dy3[3] = {0, (long long)s.JM * sy, -(long long)s.JM * sy};
+      const long long dz3[3] = {0, (long long)s.KM * sz, -(long long)s.KM * sz};
+      const bool ux[3] = {true, xl, xh}, uy[3] = {true, yl, yh}, uz[3] = {true, zl, zh};
+#pragma unroll
+      for (int c3 = 0; c3 < 3; ++c3)
+#pragma unroll
+        for (int b2 = 0; b2 < 3; ++b2)
+#pragma unroll
+          for (int a1 = 0; a1 < 3; ++a1)
+            if ((a1 | b2 | c3) && ux[a1] && uy[b2] && uz[c3]) store(o + dx3[a1] + dy3[b2] + dz3[c3]);
+    }
   }
 }
 
@@ -919,12 +951,16 @@ cudaError_t launch_prims_double(const SolveDev* d, const TileRef* tiles, int nti
   return cudaGetLastError();
 }
 
+// The reduction runs persistent whatever the stage kernels do: a few CTAs per SM
+// keep the atomics on the control block few.
+constexpr int kDtReduceCtas = 152 * 8;
+
 template <typename R>
 static void dt_reduce_ty(const SolveDev* d, const TileRef* tiles, int ntiles, double t_end, int use_t_end, int skip,
                          const LaunchCfg& cfg, cudaStream_t st, Profiler* pf) {
+  const int g = grid_for(ntiles, (cfg.max_ctas > 0 && cfg.max_ctas < kDtReduceCtas) ? cfg.max_ctas : kDtReduceCtas);
   CBNS_LAUNCH(pf, KID_DT_REDUCE, st,
-              (k_dt_reduce<R><<<grid_for(ntiles, cfg.max_ctas), 32 * cfg.tile_rows, 0, st>>>(d, tiles, ntiles, t_end,
-                                                                                             use_t_end, skip)));
+              (k_dt_reduce<R><<<g, 32 * cfg.tile_rows, 0, st>>>(d, tiles, ntiles, t_end, use_t_end, skip)));
 }
 
 cudaError_t launch_dt(const SolveDev* d, int nsolves, const TileRef* tiles, int ntiles, double t_end,

@@ -18,26 +18,59 @@
 #include <iostream>
 #include <sstream>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../../include/cbns_gpu.h"
 #include "../../../include/cbns_host.h"
 
-static int write_output(cbns_handle* h, const cbns_params& sp, unsigned cnt) {
-  const uint32_t IM = sp.IM, JM = sp.JM, KM = sp.KM;
-  const size_t n = (size_t)(IM + 2 * CBNS_NG) * (JM + 2 * CBNS_NG) * (KM + 2 * CBNS_NG);
-  std::vector<double> rho(n), u(n), v(n), w(n), p(n), x(IM + 1), y(JM + 1), z(KM + 1);
-  if (cbns_download_prims(h, rho.data(), u.data(), v.data(), w.data(), p.data(), nullptr) != CBNS_OK) return -1;
-  cbns_host_gen_mesh(&sp, IM, JM, KM, 0, 0, 0, x.data(), y.data(), z.data());
-  std::ostringstream dir;
-  dir << "output" << std::setw(3) << std::setfill('0') << cnt;
-  if (cbns_host_output_vtk_xml(dir.str().c_str(), "output", 0, 1, IM, JM, KM, x.data(), y.data(), z.data(),
-                               rho.data(), u.data(), v.data(), w.data(), p.data()) != CBNS_OK) {
-    std::cerr << "Unable to open the .vtr file by process 0\n";
-    return -1;
+// Output staging: the primitives of the current state are downloaded once
+// (cbns_download_prims), then the ASCII VTK writer — the slow part at large
+// grids — runs on a host thread while the GPU keeps stepping.  One writer at a
+// time; the next output waits for the previous one before reusing the buffers.
+class OutputStager {
+ public:
+  explicit OutputStager(const cbns_params& sp) : sp_(sp) {
+    const size_t n = (size_t)(sp.IM + 2 * CBNS_NG) * (sp.JM + 2 * CBNS_NG) * (sp.KM + 2 * CBNS_NG);
+    for (auto& a : f_) a.resize(n);
+    x_.resize(sp.IM + 1);
+    y_.resize(sp.JM + 1);
+    z_.resize(sp.KM + 1);
+    cbns_host_gen_mesh(&sp, sp.IM, sp.JM, sp.KM, 0, 0, 0, x_.data(), y_.data(), z_.data());
   }
-  return 0;
-}
+  ~OutputStager() { wait(); }
+
+  // Returns 0, or -1 if the download failed; a failed write is reported by wait().
+  int submit(cbns_handle* h, unsigned cnt) {
+    if (wait() != 0) return -1;
+    if (cbns_download_prims(h, f_[0].data(), f_[1].data(), f_[2].data(), f_[3].data(), f_[4].data(), nullptr) !=
+        CBNS_OK)
+      return -1;
+    std::ostringstream dir;
+    dir << "output" << std::setw(3) << std::setfill('0') << cnt;
+    writer_ = std::thread([this, d = dir.str()] {
+      status_ = cbns_host_output_vtk_xml(d.c_str(), "output", 0, 1, sp_.IM, sp_.JM, sp_.KM, x_.data(), y_.data(),
+                                         z_.data(), f_[0].data(), f_[1].data(), f_[2].data(), f_[3].data(),
+                                         f_[4].data());
+    });
+    return 0;
+  }
+
+  int wait() {
+    if (writer_.joinable()) writer_.join();
+    if (status_ != CBNS_OK) {
+      std::cerr << "Unable to open the .vtr file by process 0\n";
+      return -1;
+    }
+    return 0;
+  }
+
+ private:
+  cbns_params sp_;
+  std::vector<double> f_[5], x_, y_, z_;
+  std::thread writer_;
+  cbns_status status_ = CBNS_OK;
+};
 
 int main(int argc, char** argv) {
   if (4 > argc) {
@@ -87,7 +120,8 @@ int main(int argc, char** argv) {
     return 1;
   }
   unsigned cnt_out = 0;
-  if (write_output(h, sp, cnt_out) != 0) return 1;
+  OutputStager out(sp);
+  if (out.submit(h, cnt_out) != 0) return 1;
   double dt_out = sp.t_end / sp.num_output;
   double t_out = ((int)(sp.t_cur / dt_out) + 1) * dt_out;
 
@@ -114,7 +148,7 @@ int main(int argc, char** argv) {
     }
     if (t_out < sp.t_cur) {
       cnt_out++;
-      if (write_output(h, sp, cnt_out) != 0) return 1;
+      if (out.submit(h, cnt_out) != 0) return 1;
       t_out += dt_out;
     }
   }
@@ -123,7 +157,7 @@ int main(int argc, char** argv) {
   std::cout << "  Wall time: " << wall << " seconds\n"
             << "  CPU time: " << wall << " seconds\n";
   cnt_out++;
-  if (write_output(h, sp, cnt_out) != 0) return 1;
+  if (out.submit(h, cnt_out) != 0 || out.wait() != 0) return 1;
   cbns_destroy(h);
   return 0;
 }

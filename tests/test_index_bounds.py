@@ -1,0 +1,110 @@
+"""Index arithmetic of every kernel, checked on the CPU against the buffers.
+
+The kernels address padded arrays (NG = 4 ghost layers), the NGV = 2 ring and
+interior arrays.  Each offset formula below restates the one in
+csrc/cbns_device.cuh / cbns_kernels.cu / cbns_noalloc.cu; offsets are monotone in
+i, j, k, so the extreme offsets a launch can touch are reached at the corners of
+its index box plus the stencil reach.  Every one must lie inside its buffer for
+every block shape the library accepts (each extent >= NG), including the
+smallest and odd ones.
+"""
+import itertools
+
+import pytest
+
+NG, NGV, NEQ = 4, 2, 5
+SHAPES = [(4, 4, 4), (4, 5, 6), (5, 4, 7), (7, 9, 4), (12, 16, 20), (33, 17, 9), (64, 64, 64), (256, 256, 256),
+          (1000, 8, 8)]
+
+
+def geom(IM, JM, KM):
+    nx, ny, nz = IM + 2 * NG, JM + 2 * NG, KM + 2 * NG
+    rx, ry, rz = IM + 2 * NGV, JM + 2 * NGV, KM + 2 * NGV
+    return dict(V=nx * ny * nz, RV=rx * ry * rz, IV=IM * JM * KM, nx=nx, ny=ny, rx=rx, ry=ry)
+
+
+def pad_off(g, i, j, k):
+    return (i + NG) + g["nx"] * ((j + NG) + g["ny"] * (k + NG))
+
+
+def ring_off(g, i, j, k):
+    return (i + NGV) + g["rx"] * ((j + NGV) + g["ry"] * (k + NGV))
+
+
+def int_off(IM, JM, i, j, k):
+    return i + IM * (j + JM * k)
+
+
+def corners(lo, hi):
+    """Corners of the box lo <= (i, j, k) < hi."""
+    return itertools.product(*[(lo[d], hi[d] - 1) for d in range(3)])
+
+
+def span(f, lo, hi, reach):
+    vals = [f(*c) + r for c in corners(lo, hi) for r in reach]
+    return min(vals), max(vals)
+
+
+@pytest.mark.parametrize("shape", SHAPES)
+def test_stage_kernels_stay_in_bounds(shape):
+    IM, JM, KM = shape
+    g = geom(IM, JM, KM)
+    strides = [1, g["nx"], g["nx"] * g["ny"]]
+    interior = ((0, 0, 0), (IM, JM, KM))
+    # k_inviscid<D>: Q/U at c + m*st, m in -3..2 (SoA, per component n*V + off); prims at c, c - st.
+    for st in strides:
+        lo, hi = span(lambda i, j, k: pad_off(g, i, j, k), *interior, [m * st for m in range(-3, 3)])
+        assert lo >= 0 and hi < g["V"]
+    # face fluxes: interior offsets and the periodic neighbour (wrapped)
+    lo, hi = span(lambda i, j, k: int_off(IM, JM, i, j, k), *interior, [0])
+    assert lo >= 0 and hi < g["IV"]
+    # k_viscous: ring points i in [-NGV, IM+NGV); derivatives reach +-2 in each direction
+    ring = ((-NGV, -NGV, -NGV), (IM + NGV, JM + NGV, KM + NGV))
+    for st in strides:
+        lo, hi = span(lambda i, j, k: pad_off(g, i, j, k), *ring, [-2 * st, 2 * st])
+        assert lo >= 0 and hi < g["V"]
+    lo, hi = span(lambda i, j, k: ring_off(g, i, j, k), *ring, [0])
+    assert lo >= 0 and hi < g["RV"]
+    # k_update: viscous flux stencil at interior cells, +-2 ring strides
+    for st in [1, g["rx"], g["rx"] * g["ry"]]:
+        lo, hi = span(lambda i, j, k: ring_off(g, i, j, k), *interior, [-2 * st, 2 * st])
+        assert lo >= 0 and hi < g["RV"]
+    # k_update ghost images: i + IM when i < NG, i - IM when i >= IM - NG (per axis)
+    for i in range(IM):
+        for img in [i] + ([i + IM] if i < NG else []) + ([i - IM] if i >= IM - NG else []):
+            assert -NG <= img < IM + NG
+    # every ghost cell is the image of exactly one interior cell (x axis; y, z alike)
+    for gi in list(range(-NG, 0)) + list(range(IM, IM + NG)):
+        sources = [i for i in range(IM) if (i < NG and i + IM == gi) or (i >= IM - NG and i - IM == gi)]
+        assert len(sources) == 1
+    # k_prepare: the padded box, sources wrapped into the interior
+    lo, hi = span(lambda i, j, k: pad_off(g, i, j, k), (-NG, -NG, -NG), (IM + NG, JM + NG, KM + NG), [0])
+    assert lo == 0 and hi == g["V"] - 1
+    # SoA component bases
+    assert (NEQ - 1) * g["V"] + g["V"] - 1 < NEQ * g["V"]
+
+
+@pytest.mark.parametrize("shape", SHAPES)
+def test_diagnostics_and_noalloc_stay_in_bounds(shape):
+    IM, JM, KM = shape
+    g = geom(IM, JM, KM)
+    strides = [1, g["nx"], g["nx"] * g["ny"]]
+    for st in strides:
+        lo, hi = span(lambda i, j, k: pad_off(g, i, j, k), (0, 0, 0), (IM, JM, KM), [-2 * st, 2 * st])
+        assert lo >= 0 and hi < g["V"]
+        # the allocation-free entry point reads the reference's AoS layout: 5*c + n
+        assert NEQ * lo >= 0 and NEQ * hi + NEQ - 1 < NEQ * g["V"]
+
+
+def test_tiles_cover_each_domain_exactly():
+    """Tiles of 32 x rows cells: guards drop the overhang, nothing is missed."""
+    for (ex, ey, ez), rows in itertools.product([(4, 5, 6), (33, 17, 9), (260, 260, 3)], (2, 4, 8)):
+        tx, ty = -(-ex // 32), -(-ey // rows)
+        covered = set()
+        for tk, tj, ti in itertools.product(range(ez), range(ty), range(tx)):
+            for t in range(32 * rows):
+                i, j = ti * 32 + t % 32, tj * rows + t // 32
+                if i < ex and j < ey:
+                    covered.add((i, j, tk))
+        assert len(covered) == ex * ey * ez
+        assert tx < 2 ** 16 and ty < 2 ** 16 and ez < 2 ** 16  # TileRef fields are 16-bit
