@@ -62,6 +62,9 @@ template <typename R>
 struct Consts {
   R gamma, gam1, gam1_inv, gM2, Re_inv, kappa, C_T_inf, C_dt_v;
   R inv_dx, inv_dy, inv_dz;
+  // 4th-order central difference weights with 1/h folded in:
+  // d/dx f = (f[-2] - f[+2]) * c12x + (f[+1] - f[-1]) * c23x
+  R c12x, c23x, c12y, c23y, c12z, c23z;
   R rho_ref, p_ref, E_ref, T_ref;
   R gamma_gam1_inv;  // gamma / (gamma - 1)
   R pref_over_rref;  // p_ref / rho_ref
@@ -127,6 +130,12 @@ inline void fill_consts(SolveDev& s) {
   c.inv_dx = s.inv_dx;
   c.inv_dy = s.inv_dy;
   c.inv_dz = s.inv_dz;
+  c.c12x = (1.0 / 12.0) * s.inv_dx;
+  c.c23x = (2.0 / 3.0) * s.inv_dx;
+  c.c12y = (1.0 / 12.0) * s.inv_dy;
+  c.c23y = (2.0 / 3.0) * s.inv_dy;
+  c.c12z = (1.0 / 12.0) * s.inv_dz;
+  c.c23z = (2.0 / 3.0) * s.inv_dz;
   c.rho_ref = s.rho_ref;
   c.p_ref = s.p_ref;
   c.E_ref = s.E_ref;
@@ -146,6 +155,12 @@ inline void fill_consts(SolveDev& s) {
   f.inv_dx = (float)c.inv_dx;
   f.inv_dy = (float)c.inv_dy;
   f.inv_dz = (float)c.inv_dz;
+  f.c12x = (float)c.c12x;
+  f.c23x = (float)c.c23x;
+  f.c12y = (float)c.c12y;
+  f.c23y = (float)c.c23y;
+  f.c12z = (float)c.c12z;
+  f.c23z = (float)c.c23z;
   f.rho_ref = (float)c.rho_ref;
   f.p_ref = (float)c.p_ref;
   f.E_ref = (float)c.E_ref;

@@ -599,15 +599,14 @@ __global__ void __launch_bounds__(kMaxThreads) k_inviscid(const SolveDev* __rest
 
 // ---------------------------------------------------------------------------
 // Viscous fluxes on the NGV ring (src/calc_gradient.cpp:17-66,
-// src/Block3d.cpp:750-868).  d/dx f = ((f[-2]-f[+2])/12 + (f[+1]-f[-1])*2/3) / dx.
+// src/Block3d.cpp:750-868).  d/dx f = ((f[-2]-f[+2])/12 + (f[+1]-f[-1])*2/3) / dx,
+// evaluated with the 1/dx folded into the two weights.
 // FP32-mixed: T is stored as T - T_ref; its derivatives are the same.
 
 template <typename R>
-__device__ __forceinline__ R d4(const R* __restrict__ f, long long o, long long st, R inv_h) {
-  const R c12 = (R)(1.0 / 12.0), c23 = (R)(2.0 / 3.0);
-  return ((f[o - 2 * st] - f[o + 2 * st]) * c12 + (f[o + st] - f[o - st]) * c23) * inv_h;
+__device__ __forceinline__ R d4(const R* __restrict__ f, long long o, long long st, R c12h, R c23h) {
+  return (f[o - 2 * st] - f[o + 2 * st]) * c12h + (f[o + st] - f[o - st]) * c23h;
 }
-
 template <typename R>
 __global__ void __launch_bounds__(kMaxThreads) k_viscous(const SolveDev* __restrict__ solves,
                                                          const TileRef* __restrict__ tiles, int ntiles) {
@@ -621,11 +620,11 @@ __global__ void __launch_bounds__(kMaxThreads) k_viscous(const SolveDev* __restr
     const long long o = pad_off(s, tc.i, tc.j, tc.k);
     const long long sy = s.nx, sz = (long long)s.nx * s.ny;
     const Consts<R>& CS = consts_of<R>(s);
-    const R idx = CS.inv_dx, idy = CS.inv_dy, idz = CS.inv_dz;
-    const R ux = d4<R>(P.u, o, 1, idx), uy = d4<R>(P.u, o, sy, idy), uz = d4<R>(P.u, o, sz, idz);
-    const R vx = d4<R>(P.v, o, 1, idx), vy = d4<R>(P.v, o, sy, idy), vz = d4<R>(P.v, o, sz, idz);
-    const R wx = d4<R>(P.w, o, 1, idx), wy = d4<R>(P.w, o, sy, idy), wz = d4<R>(P.w, o, sz, idz);
-    const R Tx = d4<R>(P.T, o, 1, idx), Ty = d4<R>(P.T, o, sy, idy), Tz = d4<R>(P.T, o, sz, idz);
+    const R ax = CS.c12x, bx = CS.c23x, ay = CS.c12y, by = CS.c23y, az = CS.c12z, bz = CS.c23z;
+    const R ux = d4<R>(P.u, o, 1, ax, bx), uy = d4<R>(P.u, o, sy, ay, by), uz = d4<R>(P.u, o, sz, az, bz);
+    const R vx = d4<R>(P.v, o, 1, ax, bx), vy = d4<R>(P.v, o, sy, ay, by), vz = d4<R>(P.v, o, sz, az, bz);
+    const R wx = d4<R>(P.w, o, 1, ax, bx), wy = d4<R>(P.w, o, sy, ay, by), wz = d4<R>(P.w, o, sz, az, bz);
+    const R Tx = d4<R>(P.T, o, 1, ax, bx), Ty = d4<R>(P.T, o, sy, ay, by), Tz = d4<R>(P.T, o, sz, az, bz);
     const R Tl = MIXED ? CS.T_ref + P.T[o] : P.T[o];
     const R C = CS.C_T_inf;
     // Sutherland's law, (1 + C) / (T + C) * T^1.5 (src/Block3d.cpp:777).
@@ -722,8 +721,9 @@ __global__ void __launch_bounds__(kMaxThreads) k_update(const SolveDev* __restri
       if (n > 0) {
         // -(d/dx) of the viscous fluxes, as 4th-order central differences
         // (src/Block3d.cpp:887-910): ((f[-2]-f[+2])/12 + (f[+1]-f[-1])*2/3) / h.
-        R dv = d4<R>(V0 + (n - 1) * RV, r, 1, idx) + d4<R>(V1 + (n - 1) * RV, r, ry, idy) +
-               d4<R>(V2 + (n - 1) * RV, r, rz, idz);
+        const Consts<R>& CS = consts_of<R>(s);
+        R dv = d4<R>(V0 + (n - 1) * RV, r, 1, CS.c12x, CS.c23x) + d4<R>(V1 + (n - 1) * RV, r, ry, CS.c12y, CS.c23y) +
+               d4<R>(V2 + (n - 1) * RV, r, rz, CS.c12z, CS.c23z);
         df -= dv;
       }
       const double dfd = (double)df;
