@@ -65,6 +65,8 @@ __device__ __forceinline__ TileCell tile_cell(const TileRef& t, int origin) {
 // approximations (a couple of ulp): their results are stored and differenced in
 // binary32 anyway, whose rounding dominates.
 
+__device__ __forceinline__ double fma_(double a, double b, double c) { return fma(a, b, c); }
+__device__ __forceinline__ float fma_(float a, float b, float c) { return fmaf(a, b, c); }
 __device__ __forceinline__ double div_(double a, double b) { return a / b; }
 __device__ __forceinline__ float div_(float a, float b) { return __fdividef(a, b); }
 __device__ __forceinline__ double sqrt_(double a) { return sqrt(a); }
@@ -363,45 +365,39 @@ struct Weno {
 // second differences as the left one's third and second, so 13/12*D is formed
 // once for the four distinct D; otherwise the formulas above, applied twice.
 template <typename R>
-__device__ __forceinline__ void weno5_pair(const R (&v)[6], Weno<R>& L, Weno<R>& Rt) {
+__device__ __forceinline__ void weno5_side(R D1, R C1, R D2, R C2, R D3, R C3, R e1, R e2, R e3, R f1, R f2,
+                                           R f3, Weno<R>& out) {
   const R eps = (R)1.0e-6;
+  // IS_k = 13/12 D_k^2 + 1/4 e_k^2 + eps, as two fused multiply-adds each.
+  const R is1 = fma_(C1, D1, fma_((R)0.25 * e1, e1, eps));
+  const R is2 = fma_(C2, D2, fma_((R)0.25 * e2, e2, eps));
+  const R is3 = fma_(C3, D3, fma_((R)0.25 * e3, e3, eps));
+  const R a1 = is1 * is1, a2 = is2 * is2, a3 = is3 * is3;
+  // den = a2 a3 + 6 a1 a3 + 3 a1 a2 and num = a2 a3 f1 + 6 a1 a3 f2 + 3 a1 a2 f3,
+  // with the linear weights 0.1 : 0.6 : 0.3 (times 10) inside the multiply-adds.
+  const R p1 = a2 * a3, q2 = a1 * a3, q3 = a1 * a2;
+  out.den = fma_((R)6, q2, fma_((R)3, q3, p1));
+  out.num = fma_((R)6 * q2, f2, fma_((R)3 * q3, f3, p1 * f1));
+}
+
+template <typename R>
+__device__ __forceinline__ void weno5_pair(const R (&v)[6], Weno<R>& L, Weno<R>& Rt) {
   const R c13 = (R)(13.0 / 12.0);
-  const R D1 = v[0] - (R)2 * v[1] + v[2];
-  const R D2 = v[1] - (R)2 * v[2] + v[3];
-  const R D3 = v[2] - (R)2 * v[3] + v[4];
-  const R D4 = v[3] - (R)2 * v[4] + v[5];
+  const R D1 = fma_((R)-2, v[1], v[0]) + v[2];
+  const R D2 = fma_((R)-2, v[2], v[1]) + v[3];
+  const R D3 = fma_((R)-2, v[3], v[2]) + v[4];
+  const R D4 = fma_((R)-2, v[4], v[3]) + v[5];
   const R C1 = c13 * D1, C2 = c13 * D2, C3 = c13 * D3, C4 = c13 * D4;
   const R s6 = (R)(1.0 / 6.0);
-  {
-    const R e1 = v[0] - (R)4 * v[1] + (R)3 * v[2];
-    const R e2 = v[1] - v[3];
-    const R e3 = (R)3 * v[2] - (R)4 * v[3] + v[4];
-    const R is1 = C1 * D1 + (R)0.25 * e1 * e1 + eps;
-    const R is2 = C2 * D2 + (R)0.25 * e2 * e2 + eps;
-    const R is3 = C3 * D3 + (R)0.25 * e3 * e3 + eps;
-    const R a1 = is1 * is1, a2 = is2 * is2, a3 = is3 * is3;
-    const R p1 = a2 * a3, p2 = ((R)6 * a1) * a3, p3 = ((R)3 * a1) * a2;
-    const R f1 = ((R)2 * s6) * v[0] - ((R)7 * s6) * v[1] + ((R)11 * s6) * v[2];
-    const R f2 = -s6 * v[1] + ((R)5 * s6) * v[2] + ((R)2 * s6) * v[3];
-    const R f3 = ((R)2 * s6) * v[2] + ((R)5 * s6) * v[3] - s6 * v[4];
-    L.num = p1 * f1 + p2 * f2 + p3 * f3;
-    L.den = p1 + p2 + p3;
-  }
-  {
-    const R e1 = v[5] - (R)4 * v[4] + (R)3 * v[3];
-    const R e2 = v[4] - v[2];
-    const R e3 = (R)3 * v[3] - (R)4 * v[2] + v[1];
-    const R is1 = C4 * D4 + (R)0.25 * e1 * e1 + eps;
-    const R is2 = C3 * D3 + (R)0.25 * e2 * e2 + eps;
-    const R is3 = C2 * D2 + (R)0.25 * e3 * e3 + eps;
-    const R a1 = is1 * is1, a2 = is2 * is2, a3 = is3 * is3;
-    const R p1 = a2 * a3, p2 = ((R)6 * a1) * a3, p3 = ((R)3 * a1) * a2;
-    const R f1 = ((R)2 * s6) * v[5] - ((R)7 * s6) * v[4] + ((R)11 * s6) * v[3];
-    const R f2 = -s6 * v[4] + ((R)5 * s6) * v[3] + ((R)2 * s6) * v[2];
-    const R f3 = ((R)2 * s6) * v[3] + ((R)5 * s6) * v[2] - s6 * v[1];
-    Rt.num = p1 * f1 + p2 * f2 + p3 * f3;
-    Rt.den = p1 + p2 + p3;
-  }
+  const R k2 = (R)2 * s6, k5 = (R)5 * s6, k7 = (R)7 * s6, k11 = (R)11 * s6;
+  // Left-biased stencil v0..v4.
+  weno5_side<R>(D1, C1, D2, C2, D3, C3, fma_((R)3, v[2], fma_((R)-4, v[1], v[0])), v[1] - v[3],
+                fma_((R)-4, v[3], fma_((R)3, v[2], v[4])), fma_(k11, v[2], fma_(-k7, v[1], k2 * v[0])),
+                fma_(k2, v[3], fma_(k5, v[2], -s6 * v[1])), fma_(-s6, v[4], fma_(k5, v[3], k2 * v[2])), L);
+  // Mirrored right-biased stencil v5..v1: its D's are D4, D3, D2.
+  weno5_side<R>(D4, C4, D3, C3, D2, C2, fma_((R)3, v[3], fma_((R)-4, v[4], v[5])), v[4] - v[2],
+                fma_((R)-4, v[2], fma_((R)3, v[3], v[1])), fma_(k11, v[3], fma_(-k7, v[4], k2 * v[5])),
+                fma_(k2, v[2], fma_(k5, v[3], -s6 * v[4])), fma_(-s6, v[1], fma_(k5, v[2], k2 * v[3])), Rt);
 }
 
 // r[n] = num[n] / den[n] for ten parts (both states of a face).  Binary64: one
@@ -468,13 +464,14 @@ __device__ __forceinline__ void face_flux(const SolveDev& s, const R* __restrict
   const R gam1 = C.gam1, gamma = C.gamma, gam1_inv = C.gam1_inv;
 
   // Roe-averaged state of the two cells either side (src/eigenvectors_roe.cpp:87-106).
+  // (sqrt(rho_L) f_L + sqrt(rho_R) f_R) / (sqrt(rho_L) + sqrt(rho_R)) = f_R + wL (f_L - f_R).
   const R sL = P.srho[cl], sR = P.srho[c];
-  const R inv = div_((R)1, sL + sR);
+  const R wL = div_(sL, sL + sR);
   R Uv[3];
-  Uv[0] = (sL * P.u[cl] + sR * P.u[c]) * inv;
-  Uv[1] = (sL * P.v[cl] + sR * P.v[c]) * inv;
-  Uv[2] = (sL * P.w[cl] + sR * P.w[c]) * inv;
-  const R HH = (sL * P.H[cl] + sR * P.H[c]) * inv;
+  Uv[0] = fma_(wL, P.u[cl] - P.u[c], P.u[c]);
+  Uv[1] = fma_(wL, P.v[cl] - P.v[c], P.v[c]);
+  Uv[2] = fma_(wL, P.w[cl] - P.w[c], P.w[c]);
+  const R HH = fma_(wL, P.H[cl] - P.H[c], P.H[c]);
   const R q2 = Uv[0] * Uv[0] + Uv[1] * Uv[1] + Uv[2] * Uv[2];
   const R hq2 = (R)0.5 * q2;
   const R c2 = gam1 * (HH - hq2);
@@ -492,14 +489,14 @@ __device__ __forceinline__ void face_flux(const SolveDev& s, const R* __restrict
     const long long o = c + (m - 3) * st;
     const R f0 = U[o], f1 = U[V + o], f2 = U[2 * V + o], f3 = U[3 * V + o], f4 = U[4 * V + o];
     const R fm[3] = {f1, f2, f3};
-    const R t = hq2 * f0 - (Uv[0] * f1 + Uv[1] * f2 + Uv[2] * f3) + f4;
+    const R t = fma_(-Uv[2], f3, fma_(-Uv[1], f2, fma_(-Uv[0], f1, fma_(hq2, f0, f4))));
     const R A = K * t;
-    const R B = hic * (un * f0 - fm[D]);
-    w[0][m] = A + B;
-    w[1][m] = f0 - (R)2 * A;
-    w[2][m] = A - B;
-    w[3][m] = fm[T1] - u1 * f0;
-    w[4][m] = fm[T2] - u2 * f0;
+    const R g = fma_(un, f0, -fm[D]);  // B = g / (2c)
+    w[0][m] = fma_(hic, g, A);
+    w[1][m] = fma_((R)-2, A, f0);
+    w[2][m] = fma_(-hic, g, A);
+    w[3][m] = fma_(-u1, f0, fm[T1]);
+    w[4][m] = fma_(-u2, f0, fm[T2]);
   }
 
   // Left-biased (cells -3..+1) and right-biased mirrored (+2..-2) reconstructions

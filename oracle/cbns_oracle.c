@@ -9,7 +9,7 @@
  * FP64 arithmetic of chenbei102/cbns3d_cart_mpi (each function cites the file:line
  * it follows), so that on the same input it reproduces the reference's binary64
  * results bit for bit.  That claim is pinned: tests compare this port against
- * the reference itself, compiled unmodified (oracle/build_ref.py), and against
+ * the reference itself, compiled unmodified (oracle/build.py), and against
  * the golden states made from it (tests/golden/).  Build with
  * -ffp-contract=off and without -ffast-math so no multiply-add is fused.
  *
@@ -679,4 +679,17 @@ int oracle_num_threads(void) {
 #else
   return 1;
 #endif
+}
+
+/* Hooks for property tests of the restated reference functions (test use only). */
+void oracle_eigenvectors(double gamma, const double* pL, const double* pR, const double* n, double* R25,
+                         double* L25) {
+  double R[5][5], L[5][5];
+  eigenvectors(gamma, pL[0], pL[1], pL[2], pL[3], pL[4], pR[0], pR[1], pR[2], pR[3], pR[4], n[0], n[1], n[2], R, L);
+  memcpy(R25, R, sizeof R);
+  memcpy(L25, L, sizeof L);
+}
+double oracle_weno5(const double* v) { return weno5(v[0], v[1], v[2], v[3], v[4]); }
+void oracle_lf_flux(double gamma, const double* pR, const double* pL, const double* n, double* flux) {
+  lf_flux(gamma, pR[0], pR[1], pR[2], pR[3], pR[4], pL[0], pL[1], pL[2], pL[3], pL[4], n[0], n[1], n[2], flux);
 }
