@@ -364,9 +364,11 @@ struct Weno {
 // The mirrored stencil's second and third smoothness indicators use the same
 // second differences as the left one's third and second, so 13/12*D is formed
 // once for the four distinct D; otherwise the formulas above, applied twice.
+// f1 is the first candidate; f2s = 6 f2 and f3s = 3 f3 carry their linear
+// weights, so their coefficients are (-1, 5, 2) and (1, 2.5, -0.5).
 template <typename R>
-__device__ __forceinline__ void weno5_side(R D1, R C1, R D2, R C2, R D3, R C3, R e1, R e2, R e3, R f1, R f2,
-                                           R f3, Weno<R>& out) {
+__device__ __forceinline__ void weno5_side(R D1, R C1, R D2, R C2, R D3, R C3, R e1, R e2, R e3, R f1, R f2s,
+                                           R f3s, Weno<R>& out) {
   const R eps = (R)1.0e-6;
   // IS_k = 13/12 D_k^2 + 1/4 e_k^2 + eps, as two fused multiply-adds each.
   const R is1 = fma_(C1, D1, fma_((R)0.25 * e1, e1, eps));
@@ -377,7 +379,7 @@ __device__ __forceinline__ void weno5_side(R D1, R C1, R D2, R C2, R D3, R C3, R
   // with the linear weights 0.1 : 0.6 : 0.3 (times 10) inside the multiply-adds.
   const R p1 = a2 * a3, q2 = a1 * a3, q3 = a1 * a2;
   out.den = fma_((R)6, q2, fma_((R)3, q3, p1));
-  out.num = fma_((R)6 * q2, f2, fma_((R)3 * q3, f3, p1 * f1));
+  out.num = fma_(q2, f2s, fma_(q3, f3s, p1 * f1));
 }
 
 template <typename R>
@@ -389,15 +391,15 @@ __device__ __forceinline__ void weno5_pair(const R (&v)[6], Weno<R>& L, Weno<R>&
   const R D4 = fma_((R)-2, v[4], v[3]) + v[5];
   const R C1 = c13 * D1, C2 = c13 * D2, C3 = c13 * D3, C4 = c13 * D4;
   const R s6 = (R)(1.0 / 6.0);
-  const R k2 = (R)2 * s6, k5 = (R)5 * s6, k7 = (R)7 * s6, k11 = (R)11 * s6;
+  const R k2 = (R)2 * s6, k7 = (R)7 * s6, k11 = (R)11 * s6;
   // Left-biased stencil v0..v4.
   weno5_side<R>(D1, C1, D2, C2, D3, C3, fma_((R)3, v[2], fma_((R)-4, v[1], v[0])), v[1] - v[3],
                 fma_((R)-4, v[3], fma_((R)3, v[2], v[4])), fma_(k11, v[2], fma_(-k7, v[1], k2 * v[0])),
-                fma_(k2, v[3], fma_(k5, v[2], -s6 * v[1])), fma_(-s6, v[4], fma_(k5, v[3], k2 * v[2])), L);
+                fma_((R)2, v[3], fma_((R)5, v[2], -v[1])), fma_((R)-0.5, v[4], fma_((R)2.5, v[3], v[2])), L);
   // Mirrored right-biased stencil v5..v1: its D's are D4, D3, D2.
   weno5_side<R>(D4, C4, D3, C3, D2, C2, fma_((R)3, v[3], fma_((R)-4, v[4], v[5])), v[4] - v[2],
                 fma_((R)-4, v[2], fma_((R)3, v[3], v[1])), fma_(k11, v[3], fma_(-k7, v[4], k2 * v[5])),
-                fma_(k2, v[2], fma_(k5, v[3], -s6 * v[4])), fma_(-s6, v[1], fma_(k5, v[2], k2 * v[3])), Rt);
+                fma_((R)2, v[2], fma_((R)5, v[3], -v[4])), fma_((R)-0.5, v[1], fma_((R)2.5, v[2], v[3])), Rt);
 }
 
 // r[n] = num[n] / den[n] for ten parts (both states of a face).  Binary64: one
@@ -554,7 +556,7 @@ __device__ __forceinline__ void face_flux(const SolveDev& s, const R* __restrict
   const R pfL = PERT ? C.p_ref + pL : pL;
   const R pfR = PERT ? C.p_ref + pR : pR;
   const R c2L = gamma * pfL * iL, c2R = gamma * pfR * iR;
-  const R cL = sqrt_(c2L), cR = sqrt_(c2R);
+  const R cL = c2L * rsqrt(c2L), cR = c2R * rsqrt(c2R);
   const R HL = c2L * gam1_inv + (R)0.5 * q2L;
   const R HR = c2R * gam1_inv + (R)0.5 * q2R;
   const R alpha = fmax(fabs(vR[D]) + cR, fabs(vL[D]) + cL);
