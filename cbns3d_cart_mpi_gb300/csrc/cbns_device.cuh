@@ -62,6 +62,9 @@ template <typename R>
 struct Consts {
   R gamma, gam1, gam1_inv, gM2, Re_inv, kappa, C_T_inf, C_dt_v;
   R inv_dx, inv_dy, inv_dz;
+  R hfx, hfy, hfz;  // 0.5 / h: the inviscid face fluxes are stored doubled
+  R sum_ih, sum_ih2;  // 1/hx + 1/hy + 1/hz and 1/hx^2 + 1/hy^2 + 1/hz^2 (time step)
+  R C_dt_v2;          // 2 C_dt_v
   // 4th-order central difference weights with 1/h folded in:
   // d/dx f = (f[-2] - f[+2]) * c12x + (f[+1] - f[-1]) * c23x
   R c12x, c23x, c12y, c23y, c12z, c23z;
@@ -130,6 +133,12 @@ inline void fill_consts(SolveDev& s) {
   c.inv_dx = s.inv_dx;
   c.inv_dy = s.inv_dy;
   c.inv_dz = s.inv_dz;
+  c.hfx = 0.5 * s.inv_dx;
+  c.hfy = 0.5 * s.inv_dy;
+  c.hfz = 0.5 * s.inv_dz;
+  c.sum_ih = s.inv_dx + s.inv_dy + s.inv_dz;
+  c.sum_ih2 = s.inv_dx * s.inv_dx + s.inv_dy * s.inv_dy + s.inv_dz * s.inv_dz;
+  c.C_dt_v2 = 2.0 * s.C_dt_v;
   c.c12x = (1.0 / 12.0) * s.inv_dx;
   c.c23x = (2.0 / 3.0) * s.inv_dx;
   c.c12y = (1.0 / 12.0) * s.inv_dy;
@@ -155,6 +164,12 @@ inline void fill_consts(SolveDev& s) {
   f.inv_dx = (float)c.inv_dx;
   f.inv_dy = (float)c.inv_dy;
   f.inv_dz = (float)c.inv_dz;
+  f.hfx = (float)c.hfx;
+  f.hfy = (float)c.hfy;
+  f.hfz = (float)c.hfz;
+  f.sum_ih = (float)c.sum_ih;
+  f.sum_ih2 = (float)c.sum_ih2;
+  f.C_dt_v2 = (float)c.C_dt_v2;
   f.c12x = (float)c.c12x;
   f.c23x = (float)c.c23x;
   f.c12y = (float)c.c12y;

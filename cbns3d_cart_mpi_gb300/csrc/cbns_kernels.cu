@@ -258,19 +258,24 @@ __device__ __forceinline__ double warp_max(double v) {
   return v;
 }
 
+// The reference's per-cell sum over x, y, z of |u_d| + c/h_d + fv/h_d^2 with
+// fv = 2 mu C_dt_v |u| / (rho c), regrouped as
+//   (|u| + |v| + |w|) + c (1/hx + 1/hy + 1/hz) + fv (1/hx^2 + 1/hy^2 + 1/hz^2)
+// with one reciprocal of rho and one reciprocal square root (c = c^2 / c).
 template <typename R>
 __device__ __forceinline__ double dt_speed(const SolveDev& s, long long o) {
   const PrimSet<R>& P = prims_of<R>(s);
   const R rr = P.rho[o], uu = P.u[o], vv = P.v[o], ww = P.w[o];
   const Consts<R>& C = consts_of<R>(s);
   const R pp = (sizeof(R) == 4) ? C.p_ref + P.p[o] : P.p[o];
-  const R idx = C.inv_dx, idy = C.inv_dy, idz = C.inv_dz;
-  R c = sqrt_(div_(C.gamma * pp, rr));
-  R fv = div_((R)2.0 * P.mu[o] * C.C_dt_v * sqrt_(uu * uu + vv * vv + ww * ww), c * rr);
-  R t1 = fabs(uu) + c * idx + fv * idx * idx;
-  R t2 = fabs(vv) + c * idy + fv * idy * idy;
-  R t3 = fabs(ww) + c * idz + fv * idz * idz;
-  return (double)(t1 + t2 + t3);
+  const R ir = div_((R)1, rr);
+  const R c2 = (C.gamma * pp) * ir;
+  const R ic = rsqrt(c2);
+  const R c = c2 * ic;
+  const R q2 = fma_(ww, ww, fma_(vv, vv, uu * uu));
+  const R q = (sizeof(R) == 4 && !(q2 > (R)0)) ? (R)0 : sqrt_(q2);  // binary32 sqrt_ is q2 * rsqrt(q2)
+  const R fv = (C.C_dt_v2 * P.mu[o]) * q * (ir * ic);
+  return (double)((fabs(uu) + fabs(vv) + fabs(ww)) + fma_(c, C.sum_ih, fv * C.sum_ih2));
 }
 
 // Each CTA walks its tiles (grid stride) keeping a running per-thread maximum,
@@ -347,88 +352,95 @@ __global__ void k_set_dt(const SolveDev* __restrict__ solves, int sidx, double d
 }
 
 // ---------------------------------------------------------------------------
-// WENO5 (src/weno.cpp:25-56).  The reference forms w_k = d_k / IS_k^2 and returns
-// (sum w_k f_k) / (sum w_k).  Multiplying numerator and denominator by
-// 10 * IS_1^2 IS_2^2 IS_3^2 gives the same value with one division,
-//   num = a2 a3 f1 + 6 a1 a3 f2 + 3 a1 a2 f3,  den = a2 a3 + 6 a1 a3 + 3 a1 a2,
-// a_k = IS_k^2; the division is deferred so the ten of a face can share one.
-// (IS_k >= 1e-6, so den >= 1e-23: inside binary32's normal range too.)
+// WENO5 (src/weno.cpp:25-56).  The reference forms w_k = d_k / (eps + IS_k)^2
+// and returns (sum w_k f_k) / (sum w_k).  Here:
+// * every quantity is written in the first differences d_m = v_{m+1} - v_m of
+//   the six values v0..v5 of a face (cells c-3 .. c+2);
+// * the result is v2 + (sum w_k g_k) / (sum w_k) with g_k = f_k - v2 (the
+//   candidates' deviations are two-term combinations of the d_m);
+// * the indicators are taken four times over, 4 (eps + IS_k) =
+//   13/3 D_k^2 + e_k^2 + 4 eps (exact: a power-of-two scaling that cancels in
+//   the ratio);
+// * numerator and denominator are multiplied by 10 a1 a2 a3, a_k = (4 (eps + IS_k))^2,
+//     num = a2 a3 g1 + 6 a1 a3 g2 + 3 a1 a2 g3,  den = a2 a3 + 6 a1 a3 + 3 a1 a2,
+//   and the division is deferred so the ten of a face share one.
+// (4 (eps + IS_k) >= 4e-6, so den >= 2.56e-22: inside binary32's normal range.)
 
 template <typename R>
 struct Weno {
   R num, den;
 };
 
-// Both reconstructions of one characteristic field at a face: the left-biased
-// stencil (v0..v4) and the mirrored right-biased one (v5..v1), v = cells c-3..c+2.
-// The mirrored stencil's second and third smoothness indicators use the same
-// second differences as the left one's third and second, so 13/12*D is formed
-// once for the four distinct D; otherwise the formulas above, applied twice.
-// f1 is the first candidate; f2s = 6 f2 and f3s = 3 f3 carry their linear
-// weights, so their coefficients are (-1, 5, 2) and (1, 2.5, -0.5).
+// One biased stencil: D_k the second differences (C_k = 13/3 D_k), e_k the
+// one-sided differences of the indicators, g1 = f1 - v2, g2s = 6 (f2 - v2) and
+// g3s = 3 (f3 - v2) (the linear weights 0.1 : 0.6 : 0.3, times 10, folded in).
 template <typename R>
-__device__ __forceinline__ void weno5_side(R D1, R C1, R D2, R C2, R D3, R C3, R e1, R e2, R e3, R f1, R f2s,
-                                           R f3s, Weno<R>& out) {
-  const R eps = (R)1.0e-6;
-  // IS_k = 13/12 D_k^2 + 1/4 e_k^2 + eps, as two fused multiply-adds each.
-  const R is1 = fma_(C1, D1, fma_((R)0.25 * e1, e1, eps));
-  const R is2 = fma_(C2, D2, fma_((R)0.25 * e2, e2, eps));
-  const R is3 = fma_(C3, D3, fma_((R)0.25 * e3, e3, eps));
+__device__ __forceinline__ void weno5_side(R D1, R C1, R D2, R C2, R D3, R C3, R e1, R e2, R e3, R g1, R g2s,
+                                           R g3s, Weno<R>& out) {
+  const R eps4 = (R)4.0e-6;
+  const R is1 = fma_(C1, D1, fma_(e1, e1, eps4));
+  const R is2 = fma_(C2, D2, fma_(e2, e2, eps4));
+  const R is3 = fma_(C3, D3, fma_(e3, e3, eps4));
   const R a1 = is1 * is1, a2 = is2 * is2, a3 = is3 * is3;
-  // den = a2 a3 + 6 a1 a3 + 3 a1 a2 and num = a2 a3 f1 + 6 a1 a3 f2 + 3 a1 a2 f3,
-  // with the linear weights 0.1 : 0.6 : 0.3 (times 10) inside the multiply-adds.
   const R p1 = a2 * a3, q2 = a1 * a3, q3 = a1 * a2;
   out.den = fma_((R)6, q2, fma_((R)3, q3, p1));
-  out.num = fma_(q2, f2s, fma_(q3, f3s, p1 * f1));
+  out.num = fma_(q2, g2s, fma_(q3, g3s, p1 * g1));
 }
 
+// Both reconstructions of one characteristic field at a face: the left-biased
+// stencil (v0..v4, result v2 + num/den) and the mirrored right-biased one
+// (v5..v1, result v3 + num/den).  With d_m as above,
+//   left:  D = d1-d0, d2-d1, d3-d2;  e = 3 d1 - d0, d1 + d2, d3 - 3 d2;
+//          6 g1 = 5 d1 - 2 d0,  6 g2 = d1 + 2 d2,  6 g3 = 4 d2 - d3;
+//   right: D = d4-d3, d3-d2, d2-d1;  e = d4 - 3 d3, d2 + d3, 3 d2 - d1;
+//          6 g1 = 2 d4 - 5 d3,  6 g2 = -(d3 + 2 d2),  6 g3 = d1 - 4 d2
+// (the sign of an e_k is immaterial: it is squared).  The middle second
+// differences D2, D3 serve both stencils.
 template <typename R>
 __device__ __forceinline__ void weno5_pair(const R (&v)[6], Weno<R>& L, Weno<R>& Rt) {
-  const R c13 = (R)(13.0 / 12.0);
-  const R D1 = fma_((R)-2, v[1], v[0]) + v[2];
-  const R D2 = fma_((R)-2, v[2], v[1]) + v[3];
-  const R D3 = fma_((R)-2, v[3], v[2]) + v[4];
-  const R D4 = fma_((R)-2, v[4], v[3]) + v[5];
+  const R d0 = v[1] - v[0], d1 = v[2] - v[1], d2 = v[3] - v[2], d3 = v[4] - v[3], d4 = v[5] - v[4];
+  const R D1 = d1 - d0, D2 = d2 - d1, D3 = d3 - d2, D4 = d4 - d3;
+  const R c13 = (R)(13.0 / 3.0);
   const R C1 = c13 * D1, C2 = c13 * D2, C3 = c13 * D3, C4 = c13 * D4;
-  const R s6 = (R)(1.0 / 6.0);
-  const R k2 = (R)2 * s6, k7 = (R)7 * s6, k11 = (R)11 * s6;
-  // Left-biased stencil v0..v4.
-  weno5_side<R>(D1, C1, D2, C2, D3, C3, fma_((R)3, v[2], fma_((R)-4, v[1], v[0])), v[1] - v[3],
-                fma_((R)-4, v[3], fma_((R)3, v[2], v[4])), fma_(k11, v[2], fma_(-k7, v[1], k2 * v[0])),
-                fma_((R)2, v[3], fma_((R)5, v[2], -v[1])), fma_((R)-0.5, v[4], fma_((R)2.5, v[3], v[2])), L);
-  // Mirrored right-biased stencil v5..v1: its D's are D4, D3, D2.
-  weno5_side<R>(D4, C4, D3, C3, D2, C2, fma_((R)3, v[3], fma_((R)-4, v[4], v[5])), v[4] - v[2],
-                fma_((R)-4, v[2], fma_((R)3, v[3], v[1])), fma_(k11, v[3], fma_(-k7, v[4], k2 * v[5])),
-                fma_((R)2, v[2], fma_((R)5, v[3], -v[4])), fma_((R)-0.5, v[1], fma_((R)2.5, v[2], v[3])), Rt);
+  const R k56 = (R)(5.0 / 6.0), k13 = (R)(1.0 / 3.0);
+  weno5_side<R>(D1, C1, D2, C2, D3, C3, fma_((R)3, d1, -d0), d1 + d2, fma_((R)-3, d2, d3),
+                fma_(k56, d1, -k13 * d0), fma_((R)2, d2, d1), fma_((R)2, d2, (R)-0.5 * d3), L);
+  weno5_side<R>(D4, C4, D3, C3, D2, C2, fma_((R)-3, d3, d4), d2 + d3, fma_((R)3, d2, -d1),
+                fma_(-k56, d3, k13 * d4), fma_((R)-2, d2, -d3), fma_((R)-2, d2, (R)0.5 * d1), Rt);
 }
 
-// r[n] = num[n] / den[n] for ten parts (both states of a face).  Binary64: one
-// division (Montgomery's simultaneous inversion); every den lies in
-// [1e-23, 1e30] unless a smoothness indicator exceeds ~1e7, and outside
-// [1e-300, 1e300] for the product each quotient is divided on its own.
+// r[n] = base[n] + num[n] / den[n] for ten parts (both states of a face).
+// Binary64: one division (Montgomery's simultaneous inversion).  Every den is
+// positive and at least 2.56e-22, so no prefix product underflows, and one that
+// overflows makes the last one infinite; the batch is used while that product
+// lies in about [1e-300, 1e300] (biased exponent 27 .. 2019, tested on the
+// integer pipe), otherwise each quotient is divided on its own.
 // Binary32: each quotient is divided (the binary32 pipe divides cheaply).
-__device__ __forceinline__ void weno_divide10(const Weno<double> (&w)[10], double (&r)[10]) {
+__device__ __forceinline__ void weno_divide10(const Weno<double> (&w)[10], const double (&base)[10],
+                                              double (&r)[10]) {
   double pre[10];
   pre[0] = w[0].den;
 #pragma unroll
   for (int n = 1; n < 10; ++n) pre[n] = pre[n - 1] * w[n].den;
-  if (pre[9] > 1.0e-300 && pre[9] < 1.0e300) {
+  const unsigned bexp = (unsigned)((unsigned long long)__double_as_longlong(pre[9]) >> 52);
+  if (bexp - 27u < 1993u) {
     double inv = 1.0 / pre[9];
 #pragma unroll
     for (int n = 9; n > 0; --n) {
-      r[n] = w[n].num * (inv * pre[n - 1]);
+      r[n] = fma(w[n].num, inv * pre[n - 1], base[n]);
       inv *= w[n].den;
     }
-    r[0] = w[0].num * inv;
+    r[0] = fma(w[0].num, inv, base[0]);
   } else {
 #pragma unroll
-    for (int n = 0; n < 10; ++n) r[n] = w[n].num / w[n].den;
+    for (int n = 0; n < 10; ++n) r[n] = base[n] + w[n].num / w[n].den;
   }
 }
 
-__device__ __forceinline__ void weno_divide10(const Weno<float> (&w)[10], float (&r)[10]) {
+__device__ __forceinline__ void weno_divide10(const Weno<float> (&w)[10], const float (&base)[10],
+                                              float (&r)[10]) {
 #pragma unroll
-  for (int n = 0; n < 10; ++n) r[n] = div_(w[n].num, w[n].den);
+  for (int n = 0; n < 10; ++n) r[n] = base[n] + div_(w[n].num, w[n].den);
 }
 
 // ---------------------------------------------------------------------------
@@ -508,8 +520,13 @@ __device__ __forceinline__ void face_flux(const SolveDev& s, const R* __restrict
     Weno<R> wp[2 * NEQ];
 #pragma unroll
     for (int n = 0; n < NEQ; ++n) weno5_pair<R>(w[n], wp[n], wp[NEQ + n]);
-    R q[2 * NEQ];
-    weno_divide10(wp, q);
+    R base[2 * NEQ], q[2 * NEQ];
+#pragma unroll
+    for (int n = 0; n < NEQ; ++n) {
+      base[n] = w[n][2];
+      base[NEQ + n] = w[n][3];
+    }
+    weno_divide10(wp, base, q);
 #pragma unroll
     for (int n = 0; n < NEQ; ++n) {
       rl[n] = q[n];
@@ -539,6 +556,8 @@ __device__ __forceinline__ void face_flux(const SolveDev& s, const R* __restrict
   // Local Lax-Friedrichs flux (src/lf_flux.cpp:32-99); both 1/rho from one division.
   // PERT: rhoX, EX are perturbations; dL, dR the full densities, pL, pR the
   // pressure perturbations, pfL, pfR the full pressures.
+  // The stored flux is twice the reference's: the halves are folded into the
+  // flux difference's 0.5/h (an exact power-of-two scaling).
   const R dL = PERT ? C.rho_ref + rhoL : rhoL;
   const R dR = PERT ? C.rho_ref + rhoR : rhoR;
   const R ip = div_((R)1, dL * dR);
@@ -549,25 +568,32 @@ __device__ __forceinline__ void face_flux(const SolveDev& s, const R* __restrict
     vL[a] = mL[a] * iL;
     vR[a] = mR[a] * iR;
   }
-  const R q2L = vL[0] * vL[0] + vL[1] * vL[1] + vL[2] * vL[2];
-  const R q2R = vR[0] * vR[0] + vR[1] * vR[1] + vR[2] * vR[2];
-  const R pL = gam1 * (EL - (R)0.5 * dL * q2L);
-  const R pR = gam1 * (ER - (R)0.5 * dR * q2R);
+  // rho q^2 = m . v; p = (gamma - 1) (E - rho q^2 / 2).
+  const R kL = fma_(mL[2], vL[2], fma_(mL[1], vL[1], mL[0] * vL[0]));
+  const R kR = fma_(mR[2], vR[2], fma_(mR[1], vR[1], mR[0] * vR[0]));
+  const R pL = gam1 * fma_((R)-0.5, kL, EL);
+  const R pR = gam1 * fma_((R)-0.5, kR, ER);
   const R pfL = PERT ? C.p_ref + pL : pL;
   const R pfR = PERT ? C.p_ref + pR : pR;
-  const R c2L = gamma * pfL * iL, c2R = gamma * pfR * iR;
+  const R c2L = (gamma * iL) * pfL, c2R = (gamma * iR) * pfR;
   const R cL = c2L * rsqrt(c2L), cR = c2R * rsqrt(c2R);
-  const R HL = c2L * gam1_inv + (R)0.5 * q2L;
-  const R HR = c2R * gam1_inv + (R)0.5 * q2R;
   const R alpha = fmax(fabs(vR[D]) + cR, fabs(vL[D]) + cL);
   const R fL = mL[D], fR = mR[D];  // mass fluxes rho*q_n
-  out[0] = (R)0.5 * (fL + fR - alpha * (rhoR - rhoL));
+  out[0] = fma_(-alpha, rhoR - rhoL, fL + fR);
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
-    R pf = (a == D) ? (pL + pR) : (R)0;
-    out[1 + a] = (R)0.5 * (fL * vL[a] + fR * vR[a] + pf - alpha * (mR[a] - mL[a]));
+    const R fLa = (a == D) ? fma_(fL, vL[a], pL + pR) : fL * vL[a];
+    out[1 + a] = fma_(-alpha, mR[a] - mL[a], fma_(fR, vR[a], fLa));
   }
-  out[4] = (R)0.5 * (fL * HL + fR * HR - alpha * (ER - EL));
+  if constexpr (PERT) {
+    // rho q_n H with H = c^2/(gamma-1) + q^2/2 from the full sound speed.
+    const R HL = fma_(c2L, gam1_inv, (R)0.5 * (kL * iL));
+    const R HR = fma_(c2R, gam1_inv, (R)0.5 * (kR * iR));
+    out[4] = fma_(-alpha, ER - EL, fma_(fR, HR, fL * HL));
+  } else {
+    // rho q_n H = q_n (E + p).
+    out[4] = fma_(-alpha, ER - EL, fma_(vR[D], ER + pR, vL[D] * (EL + pL)));
+  }
 }
 
 template <int D, typename R>
@@ -710,7 +736,8 @@ __global__ void __launch_bounds__(kMaxThreads) k_update(const SolveDev* __restri
       F0 = s.F[0], F1 = s.F[1], F2 = s.F[2];
       V0 = s.Fv[0], V1 = s.Fv[1], V2 = s.Fv[2];
     }
-    const R idx = consts_of<R>(s).inv_dx, idy = consts_of<R>(s).inv_dy, idz = consts_of<R>(s).inv_dz;
+    // The face fluxes are stored doubled: hf = 0.5 / h.
+    const R idx = consts_of<R>(s).hfx, idy = consts_of<R>(s).hfy, idz = consts_of<R>(s).hfz;
 
     double qn[NEQ];
 #pragma unroll
