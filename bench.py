@@ -272,6 +272,9 @@ def run_ours(args, rank, world, local):
                            "MEASURED_PEAKS.json holds no FP64 figure",
             "algorithmic_flops_per_launch": flops,
             "flop_count": "reference's own op count per face/cell (tests/golden/opcount.txt)",
+            "note": "achieved counts the reference's FLOPs; the kernel issues fewer binary64 instructions "
+                    "than that count, so frac can exceed 1; its FP64-pipe utilisation (ncu) is in "
+                    "profiles/inviscid_fp64_tgv160.md",
         }
         step_ms = ms / args.steps
         line["kernels"] = kernels
