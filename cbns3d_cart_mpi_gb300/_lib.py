@@ -56,6 +56,8 @@ GPU_API = {
     "cbns_download_Q": (c_int, [c_vp, c_vp]),
     "cbns_download_Q_p": (c_int, [c_vp, c_vp]),
     "cbns_download_prims": (c_int, [c_vp] + [c_vp] * 6),
+    "cbns_load_checkpoint": (c_int, [c_vp, ctypes.c_char_p, c_dp]),
+    "cbns_save_checkpoint": (c_int, [c_vp, ctypes.c_char_p]),
     "cbns_calc_dt": (c_int, [c_vp, c_dp]),
     "cbns_stage": (c_int, [c_vp, c_d, c_int]),
     "cbns_step": (c_int, [c_vp, c_d, c_dp, c_dp]),
@@ -72,6 +74,8 @@ GPU_API = {
     "cbns_server_submit": (c_int, [c_vp, P_params, c_u32, c_u32, c_u32, c_vp, c_int, ctypes.POINTER(c_u64)]),
     "cbns_server_submit_tgv": (c_int, [c_vp, P_params, c_u32, c_u32, c_u32, c_u64, c_d, c_int, c_int, c_int,
                                        ctypes.POINTER(c_u64)]),
+    "cbns_server_submit_checkpoint": (c_int, [c_vp, P_params, c_u32, c_u32, c_u32, ctypes.c_char_p, c_int,
+                                              ctypes.POINTER(c_u64)]),
     "cbns_server_cancel": (c_int, [c_vp, c_u64]),
     "cbns_server_wait": (c_int, [c_vp, c_u64, c_d, c_vp]),
     "cbns_server_result": (c_int, [c_vp, c_u64, c_vp]),

@@ -18,7 +18,8 @@ CSRC = os.path.join(PKG, "csrc")
 LIB = os.path.join(PKG, "lib")
 INCLUDE = os.path.join(ROOT, "include")
 
-GPU_SOURCES = ["cbns_kernels.cu", "cbns_api.cu", "cbns_probe.cu", "cbns_noalloc.cu", "cbns_serve.cu"]
+GPU_SOURCES = ["cbns_kernels.cu", "cbns_api.cu", "cbns_probe.cu", "cbns_noalloc.cu", "cbns_serve.cu",
+               "cbns_ckpt.cu"]
 HOST_SOURCES = ["host/cbns_host.cpp"]
 DRIVER_SOURCE = "host/cbns3d_gb300.cpp"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

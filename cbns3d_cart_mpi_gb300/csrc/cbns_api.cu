@@ -136,6 +136,7 @@ void set_last_error(const std::string& msg) { g_last_error = msg; }
 }  // namespace cbns
 
 
+
 extern "C" {
 
 const char* cbns_last_error(void) { return g_last_error.c_str(); }
@@ -165,6 +166,10 @@ cbns_status cbns_destroy(cbns_handle* h) {
   if (h->arena) cudaFree(h->arena);
   if (h->h_ctl) cudaFreeHost(h->h_ctl);
   if (h->h_out) cudaFreeHost(h->h_out);
+  for (int b = 0; b < 2; ++b) {
+    if (h->h_chunk[b]) cudaFreeHost(h->h_chunk[b]);
+    if (h->ev_chunk[b]) cudaEventDestroy(h->ev_chunk[b]);
+  }
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
   return CBNS_OK;
@@ -209,7 +214,6 @@ cbns_status cbns_create(const cbns_params* p, uint32_t IM, uint32_t JM, uint32_t
   h->IM = IM;
   h->JM = JM;
   h->KM = KM;
-  cbns_status st = CBNS_OK;
   auto bail = [&](cbns_status s) {
     cbns_destroy(h);
     return s;
@@ -325,7 +329,6 @@ cbns_status cbns_create(const cbns_params* p, uint32_t IM, uint32_t JM, uint32_t
       (e = cudaMemcpyAsync(h->d_ctl, h->h_ctl, sizeof(SolveCtl), cudaMemcpyHostToDevice, h->stream)) != cudaSuccess)
     return bail(cuda_fail(e, "cudaMemcpyAsync(setup)"));
   if ((e = cudaStreamSynchronize(h->stream)) != cudaSuccess) return bail(cuda_fail(e, "cudaStreamSynchronize"));
-  (void)st;
   *out = h;
   return CBNS_OK;
 }
@@ -341,19 +344,10 @@ cbns_status cbns_upload_Q(cbns_handle* h, const double* Q, double t) {
   cbns_status st = check_handle(h, "cbns_upload_Q");
   if (st != CBNS_OK) return st;
   if (!Q) return fail(CBNS_ERR_INVALID_ARG, "cbns_upload_Q: null Q");
-  const SolveDev& s = h->desc;
-  // The host array goes to the staging buffer as-is, is transposed into Q (SoA),
-  // then the start-up kernel fills ghosts, primitives, Q_p and mu.
-  CBNS_CUDA(cudaMemcpyAsync(h->d_stage, Q, sizeof(double) * NEQ * (size_t)s.V, cudaMemcpyHostToDevice, h->stream));
-  CBNS_CUDA(launch_layout(h->d_desc, 0, h->d_stage, s.Q, true, s.V, h->stream, h->pf()));
-  CBNS_CUDA(launch_prepare(h->d_desc, h->d_tiles_pad, h->n_pad, h->stream, h->pf()));
-  std::memset(h->h_ctl, 0, sizeof(SolveCtl));
-  h->h_ctl->t_cur = t;
-  h->h_ctl->t_end = h->params.t_end;
-  h->h_ctl->active = 1;
-  CBNS_CUDA(cudaMemcpyAsync(h->d_ctl, h->h_ctl, sizeof(SolveCtl), cudaMemcpyHostToDevice, h->stream));
-  CBNS_CUDA(cudaStreamSynchronize(h->stream));
-  return CBNS_OK;
+  // The host array goes to the staging buffer as-is, then becomes the state.
+  CBNS_CUDA(cudaMemcpyAsync(h->d_stage, Q, sizeof(double) * NEQ * (size_t)h->desc.V, cudaMemcpyHostToDevice,
+                            h->stream));
+  return cbns::adopt_staged(h, t);
 }
 
 cbns_status cbns_init_tgv(cbns_handle* h, uint64_t seed, double amp, int nmodes, int kmax, double t) {
@@ -841,3 +835,31 @@ cbns_status cbns_get_info(cbns_handle* h, uint32_t dims[3], uint64_t* device_byt
 }
 
 }  // extern "C"
+
+namespace cbns {
+cbns_status enter(cbns_handle* h, const char* fn) { return check_handle(h, fn); }
+
+cbns_status cuda_error(cudaError_t e, const char* what) { return cuda_fail(e, what); }
+
+// The AoS state in h->d_stage becomes the solve's state at time t: transposed
+// into Q (SoA), then the start-up kernel fills ghosts, primitives, Q_p and mu
+// (src/cbns3d.cpp:149-153), and the control block restarts at t.
+cbns_status adopt_staged(cbns_handle* h, double t) {
+  const SolveDev& s = h->desc;
+  CBNS_CUDA(launch_layout(h->d_desc, 0, h->d_stage, s.Q, true, s.V, h->stream, h->pf()));
+  CBNS_CUDA(launch_prepare(h->d_desc, h->d_tiles_pad, h->n_pad, h->stream, h->pf()));
+  std::memset(h->h_ctl, 0, sizeof(SolveCtl));
+  h->h_ctl->t_cur = t;
+  h->h_ctl->t_end = h->params.t_end;
+  h->h_ctl->active = 1;
+  CBNS_CUDA(cudaMemcpyAsync(h->d_ctl, h->h_ctl, sizeof(SolveCtl), cudaMemcpyHostToDevice, h->stream));
+  CBNS_CUDA(cudaStreamSynchronize(h->stream));
+  return CBNS_OK;
+}
+
+// Q in the reference's AoS layout in h->d_stage, enqueued on h->stream.
+cbns_status stage_state(cbns_handle* h) {
+  CBNS_CUDA(launch_layout(h->d_desc, 0, h->desc.Q, h->d_stage, false, h->desc.V, h->stream, h->pf()));
+  return CBNS_OK;
+}
+}  // namespace cbns

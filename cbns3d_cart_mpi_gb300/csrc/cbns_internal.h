@@ -15,6 +15,15 @@ namespace cbns {
 void set_last_error(const std::string& msg);
 }  // namespace cbns
 
+struct cbns_handle;
+namespace cbns {
+// Helpers shared by the translation units of the library (cbns_api.cu).
+cbns_status enter(cbns_handle* h, const char* fn);           // null check, cudaSetDevice
+cbns_status cuda_error(cudaError_t e, const char* what);     // records the error text
+cbns_status adopt_staged(cbns_handle* h, double t);          // staged AoS state -> the solve's state
+cbns_status stage_state(cbns_handle* h);                     // Q -> staged AoS (enqueued)
+}  // namespace cbns
+
 struct cbns_handle {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -36,6 +45,8 @@ struct cbns_handle {
   double* d_out = nullptr;  // small device results (diagnostics, raw dt)
   cbns::SolveCtl* h_ctl = nullptr;  // pinned
   double* h_out = nullptr;    // pinned
+  char* h_chunk[2] = {nullptr, nullptr};           // pinned checkpoint chunks (cbns_ckpt.cu)
+  cudaEvent_t ev_chunk[2] = {nullptr, nullptr};
   cudaGraphExec_t step_graph = nullptr;
   double graph_t_end = 0.0;
   cbns::Profiler prof;

@@ -41,6 +41,7 @@ struct Request {
   cbns_params params{};
   uint32_t IM = 0, JM = 0, KM = 0;
   std::vector<double> Q0;  // host state, or empty for the device initial condition
+  std::string ckpt;        // checkpoint file read at admission, if not empty
   uint64_t seed = 0;
   double amp = 0.0;
   int nmodes = 0, kmax = 1;
@@ -146,8 +147,12 @@ void worker_loop(cbns_server* sv) {
     for (Request* r : admit) {
       cbns_status st = cbns_create(&r->params, r->IM, r->JM, r->KM, sv->opts.precision, &r->h);
       if (st == CBNS_OK) {
-        st = r->Q0.empty() ? cbns_init_tgv(r->h, r->seed, r->amp, r->nmodes, r->kmax, r->params.t_cur)
-                           : cbns_upload_Q(r->h, r->Q0.data(), r->params.t_cur);
+        if (!r->ckpt.empty())
+          st = cbns_load_checkpoint(r->h, r->ckpt.c_str(), nullptr);
+        else if (r->Q0.empty())
+          st = cbns_init_tgv(r->h, r->seed, r->amp, r->nmodes, r->kmax, r->params.t_cur);
+        else
+          st = cbns_upload_Q(r->h, r->Q0.data(), r->params.t_cur);
         std::vector<double>().swap(r->Q0);
       }
       if (st != CBNS_OK) {
@@ -334,6 +339,20 @@ cbns_status cbns_server_submit_tgv(cbns_server* sv, const cbns_params* p, uint32
   r->amp = amp;
   r->nmodes = nmodes;
   r->kmax = kmax;
+  r->keep_state = keep_state;
+  return submit(sv, r, id);
+}
+
+cbns_status cbns_server_submit_checkpoint(cbns_server* sv, const cbns_params* p, uint32_t IM, uint32_t JM,
+                                          uint32_t KM, const char* path, int keep_state, uint64_t* id) {
+  if (!sv || !p || !path) return serve_fail(CBNS_ERR_INVALID_ARG, "cbns_server_submit_checkpoint: null argument");
+  Request* r = new Request();
+  r->params = *p;
+  cbns_params_derive(&r->params);
+  r->IM = IM;
+  r->JM = JM;
+  r->KM = KM;
+  r->ckpt = path;
   r->keep_state = keep_state;
   return submit(sv, r, id);
 }

@@ -100,24 +100,28 @@ int main(int argc, char** argv) {
     mkdir(name, 0755);
   }
   const uint32_t IM = sp.IM, JM = sp.JM, KM = sp.KM;
-  std::vector<double> Q((size_t)CBNS_NEQ * (IM + 2 * CBNS_NG) * (JM + 2 * CBNS_NG) * (KM + 2 * CBNS_NG));
   std::string ckpt = std::string(sp.checkpoint_fname) + "000.dat";
-  double t0 = sp.t_cur;
-  if (sp.is_restart) {
-    cbns_host_initial_condition(&sp, IM, JM, KM, 0, 0, 0, Q.data());
-  } else if (cbns_host_read_bin(ckpt.c_str(), IM, JM, KM, Q.data(), &t0) != CBNS_OK) {
-    std::cerr << "Unable to open the checkpoint file by process 0\n";
-    return 1;
-  }
-  sp.t_cur = t0;
   cbns_handle* h = nullptr;
   if ((st = cbns_create(&sp, IM, JM, KM, CBNS_FP64, &h)) != CBNS_OK) {
     std::cerr << "cbns_create failed: " << cbns_last_error() << "\n";
     return 1;
   }
-  if ((st = cbns_upload_Q(h, Q.data(), sp.t_cur)) != CBNS_OK) {
-    std::cerr << "cbns_upload_Q failed: " << cbns_last_error() << "\n";
-    return 1;
+  if (sp.is_restart) {
+    // The reference's initial condition on the host (its libm sin/cos), uploaded.
+    std::vector<double> Q((size_t)CBNS_NEQ * (IM + 2 * CBNS_NG) * (JM + 2 * CBNS_NG) * (KM + 2 * CBNS_NG));
+    cbns_host_initial_condition(&sp, IM, JM, KM, 0, 0, 0, Q.data());
+    if ((st = cbns_upload_Q(h, Q.data(), sp.t_cur)) != CBNS_OK) {
+      std::cerr << "cbns_upload_Q failed: " << cbns_last_error() << "\n";
+      return 1;
+    }
+  } else {
+    // The checkpoint streams from the file to the device.
+    double t0 = sp.t_cur;
+    if (cbns_load_checkpoint(h, ckpt.c_str(), &t0) != CBNS_OK) {
+      std::cerr << "Unable to open the checkpoint file by process 0\n" << cbns_last_error() << "\n";
+      return 1;
+    }
+    sp.t_cur = t0;
   }
   unsigned cnt_out = 0;
   OutputStager out(sp);
@@ -140,8 +144,7 @@ int main(int argc, char** argv) {
     sp.t_cur = t;
     std::cout << n_t << ", " << dt << ", " << sp.t_cur << std::endl;
     if (0 == (n_t + 1) % sp.checkpoint_freq) {
-      if (cbns_download_Q(h, Q.data()) != CBNS_OK ||
-          cbns_host_output_bin(ckpt.c_str(), sp.t_cur, IM, JM, KM, Q.data()) != CBNS_OK) {
+      if (cbns_save_checkpoint(h, ckpt.c_str()) != CBNS_OK) {
         std::cerr << "Unable to save the checkpoint file by process 0\n";
         return 1;
       }

@@ -6,6 +6,7 @@ Mirrors the reference's Block3d public interface (include/Block3d.h:126-163):
 native libraries; nothing here computes the solution.
 """
 import ctypes
+import os
 
 import numpy as np
 
@@ -94,6 +95,17 @@ class Solver:
         out = np.empty(self.shape) if out is None else out
         _check(_lib.gpu().cbns_download_Q_p(self._h, _ptr(out)), "cbns_download_Q_p")
         return out
+
+    def load_checkpoint(self, path):
+        """Restart from a checkpoint file in the reference's output_bin format,
+        streamed to the device (cbns_load_checkpoint); returns the file's t_cur."""
+        t = ctypes.c_double()
+        _check(_lib.gpu().cbns_load_checkpoint(self._h, os.fsencode(path), ctypes.byref(t)), "cbns_load_checkpoint")
+        return t.value
+
+    def save_checkpoint(self, path):
+        """Write Q and t_cur in the reference's output_bin format (cbns_save_checkpoint)."""
+        _check(_lib.gpu().cbns_save_checkpoint(self._h, os.fsencode(path)), "cbns_save_checkpoint")
 
     def download_prims(self):
         arrs = [np.empty(self.prim_shape) for _ in range(6)]
@@ -252,6 +264,14 @@ class Server:
         _check(_lib.gpu().cbns_server_submit_tgv(self._s, ctypes.byref(params), params.IM, params.JM, params.KM,
                                                  int(seed), float(amp), int(nmodes), int(kmax), int(keep_state),
                                                  ctypes.byref(rid)), "cbns_server_submit_tgv")
+        return rid.value
+
+    def submit_checkpoint(self, params, path, keep_state=False):
+        """A request that starts from a checkpoint file, read by the worker at admission."""
+        rid = ctypes.c_uint64()
+        _check(_lib.gpu().cbns_server_submit_checkpoint(self._s, ctypes.byref(params), params.IM, params.JM,
+                                                        params.KM, os.fsencode(path), int(keep_state),
+                                                        ctypes.byref(rid)), "cbns_server_submit_checkpoint")
         return rid.value
 
     def cancel(self, rid):

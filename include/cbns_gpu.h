@@ -113,6 +113,20 @@ cbns_status cbns_download_Q_p(cbns_handle* h, double* Q_p);
 cbns_status cbns_download_prims(cbns_handle* h, double* rho, double* u, double* v,
                                 double* w, double* p, double* T);
 
+/* Checkpoints streamed between a file and the device, in the format of
+ * Block3d::output_bin / read_bin (src/Block3d.cpp:964-987, :318-357): t_cur
+ * (binary64), IM_G, JM_G, KM_G (uint32), then Q in the get_idx_Q layout.
+ * cbns_load_checkpoint replaces Block3d::read_bin + cbns_upload_Q on restart
+ * (src/cbns3d.cpp:145-153): it checks the padded extents (CBNS_ERR_FORMAT on a
+ * mismatch or a short file, CBNS_ERR_IO if the file cannot be opened), streams
+ * the state to the device through two pinned chunk buffers, then does what
+ * cbns_upload_Q does, with t_cur from the file (*t_out, may be NULL).  A failed
+ * load leaves the solve's state unchanged.  cbns_save_checkpoint writes the
+ * current Q and t_cur the same way (Block3d::output_bin); the file is byte for
+ * byte what cbns_host_output_bin writes for cbns_download_Q's array. */
+cbns_status cbns_load_checkpoint(cbns_handle* h, const char* path, double* t_out);
+cbns_status cbns_save_checkpoint(cbns_handle* h, const char* path);
+
 /* Block3d::calc_dt (src/Block3d.cpp:515-553): CFL / max over interior cells. */
 cbns_status cbns_calc_dt(cbns_handle* h, double* dt);
 
@@ -238,6 +252,13 @@ cbns_status cbns_server_submit(cbns_server* s, const cbns_params* p, uint32_t IM
 cbns_status cbns_server_submit_tgv(cbns_server* s, const cbns_params* p, uint32_t IM, uint32_t JM, uint32_t KM,
                                    uint64_t seed, double amp, int nmodes, int kmax, int keep_state,
                                    uint64_t* id);
+/* A request whose initial state is a checkpoint file in the format of
+ * cbns_save_checkpoint, read by the worker at admission (cbns_load_checkpoint),
+ * so the caller holds no state.  It starts at the file's t_cur (p->t_cur is
+ * not used); a file that cannot be read retires the request with CBNS_ERR_IO
+ * or CBNS_ERR_FORMAT. */
+cbns_status cbns_server_submit_checkpoint(cbns_server* s, const cbns_params* p, uint32_t IM, uint32_t JM,
+                                          uint32_t KM, const char* path, int keep_state, uint64_t* id);
 cbns_status cbns_server_cancel(cbns_server* s, uint64_t id);
 /* Waits for a request (timeout_s < 0: no limit; CBNS_ERR_TIMEOUT if it runs out)
  * and returns its final status. */

@@ -47,6 +47,38 @@ def test_driver_run(tmp_path):
     assert (tmp_path / last / "output000.vtr").read_text() == (ref_dir / "output000.vtr").read_text()
 
 
+def test_driver_restarts_from_its_checkpoint(tmp_path):
+    """is_restart = 0 resumes from checkpoint000.dat (src/cbns3d.cpp:136-144),
+    which the driver streams to the device; the resumed run ends bitwise where
+    the library ends after loading the same file and taking the same steps."""
+    from cbns3d_cart_mpi_gb300 import build
+    from cbns3d_cart_mpi_gb300.params import write_input_txt
+    from cbns3d_cart_mpi_gb300.solver import Solver, read_bin
+
+    p = tgv_params(12, JM=8, KM=10, t_end=0.03, nstep_max=100)
+    p.checkpoint_freq = 3
+    p.num_output = 1
+    write_input_txt(p, str(tmp_path / "input.txt"))
+    r = subprocess.run([build.DRIVER, "1", "1", "1"], cwd=tmp_path, capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr
+    first = (tmp_path / "checkpoint000.dat").read_bytes()
+    (tmp_path / "first.dat").write_bytes(first)
+    p.is_restart = 0
+    p.t_end = 0.06
+    write_input_txt(p, str(tmp_path / "input.txt"))
+    r = subprocess.run([build.DRIVER, "1", "1", "1"], cwd=tmp_path, capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr
+    steps = [ln for ln in r.stdout.splitlines() if ln.count(",") == 2 and ln.split(",")[0].strip().isdigit()]
+    assert len(steps) == 3 and "Finished!" in r.stdout
+
+    s = Solver(p)
+    s.load_checkpoint(str(tmp_path / "first.dat"))
+    for _ in range(3):
+        s.step()
+    t_ck, Qck = read_bin(str(tmp_path / "checkpoint000.dat"), 12, 8, 10)
+    assert np.array_equal(Qck, s.download_Q()) and t_ck == s.time()[0]
+
+
 def test_driver_rejects_more_than_one_process(tmp_path):
     from cbns3d_cart_mpi_gb300 import build
     from cbns3d_cart_mpi_gb300.params import write_input_txt
