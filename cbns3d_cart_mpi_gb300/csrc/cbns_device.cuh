@@ -44,6 +44,8 @@ struct SolveCtl {
 // but p and T as perturbations p - p_ref, T - T_ref (binary32 keeps 24 bits of
 // the O(0.1) fluctuations instead of the O(70) mean pressure).
 template <typename R>
+// The arrays are consecutive blocks of V values of one allocation, in member
+// order (the update kernel's stores address them from the first).
 struct PrimSet {
   R* rho;
   R* u;

@@ -130,17 +130,22 @@ __device__ __forceinline__ MixedCell mixed_cell(const SolveDev& s, const double 
   return m;
 }
 
+// The primitive arrays are consecutive blocks of V values in PrimSet order, so
+// one base pointer addresses all of them (fewer live registers in the update).
 __device__ __forceinline__ void store_mixed(const SolveDev& s, long long o, const MixedCell& m) {
+  const long long V = s.V;
+  float* u = s.Uf + o;
 #pragma unroll
-  for (int n = 0; n < NEQ; ++n) s.Uf[n * s.V + o] = m.U[n];
-  s.pf.rho[o] = m.rho;
-  s.pf.u[o] = m.u;
-  s.pf.v[o] = m.v;
-  s.pf.w[o] = m.w;
-  s.pf.p[o] = m.p;
-  s.pf.T[o] = m.T;
-  s.pf.srho[o] = m.srho;
-  s.pf.H[o] = m.H;
+  for (int n = 0; n < NEQ; ++n) u[n * V] = m.U[n];
+  float* b = s.pf.rho + o;
+  b[0] = m.rho;
+  b[V] = m.u;
+  b[2 * V] = m.v;
+  b[3 * V] = m.w;
+  b[4 * V] = m.p;
+  b[5 * V] = m.T;
+  b[6 * V] = m.srho;
+  b[7 * V] = m.H;
 }
 
 __global__ void k_aos_to_soa(const SolveDev* __restrict__ solves, int sidx, const double* __restrict__ aos,
@@ -655,8 +660,10 @@ __global__ void __launch_bounds__(kMaxThreads) k_viscous(const SolveDev* __restr
     const R Tx = d4<R>(P.T, o, 1, ax, bx), Ty = d4<R>(P.T, o, sy, ay, by), Tz = d4<R>(P.T, o, sz, az, bz);
     const R Tl = MIXED ? CS.T_ref + P.T[o] : P.T[o];
     const R C = CS.C_T_inf;
-    // Sutherland's law, (1 + C) / (T + C) * T^1.5 (src/Block3d.cpp:777).
-    const R mu = div_(((R)1 + C) * Tl * sqrt_(Tl), Tl + C);
+    // Sutherland's law, (1 + C) / (T + C) * T^1.5 (src/Block3d.cpp:777), as
+    // (1 + C) T^2 / sqrt(T (T + C)^2): one reciprocal square root, no division.
+    const R TC = Tl + C;
+    const R mu = (((R)1 + C) * (Tl * Tl)) * rsqrt(Tl * (TC * TC));
     if (tc.i >= 0 && tc.i < s.IM && tc.j >= 0 && tc.j < s.JM && tc.k >= 0 && tc.k < s.KM) P.mu[o] = mu;
     const R mr = mu * CS.Re_inv;
     const R m23 = (R)(2.0 / 3.0) * mr;
@@ -742,18 +749,27 @@ __device__ __forceinline__ void update_tiles(const SolveDev* __restrict__ solves
     // The face fluxes are stored doubled: hf = 0.5 / h.
     const R idx = consts_of<R>(s).hfx, idy = consts_of<R>(s).hfy, idz = consts_of<R>(s).hfz;
 
+    const Consts<R>& CS = consts_of<R>(s);
     double qn[NEQ];
 #pragma unroll
     for (int n = 0; n < NEQ; ++n) {
-      R df = (F0[n * IV + fx] - F0[n * IV + fo]) * idx + (F1[n * IV + fy] - F1[n * IV + fo]) * idy +
-             (F2[n * IV + fz] - F2[n * IV + fo]) * idz;
+      // Inviscid flux differences, then minus the 4th-order central divergence
+      // of the viscous fluxes (src/Block3d.cpp:887-910, calc_viscous_flux_contribution:
+      // ((f[-2]-f[+2])/12 + (f[+1]-f[-1])*2/3) / h per direction), as one chain
+      // of fused multiply-adds with the 1/h-folded weights negated.
+      R df = (F0[n * IV + fx] - F0[n * IV + fo]) * idx;
+      df = fma_(F1[n * IV + fy] - F1[n * IV + fo], idy, df);
+      df = fma_(F2[n * IV + fz] - F2[n * IV + fo], idz, df);
       if (n > 0) {
-        // -(d/dx) of the viscous fluxes, as 4th-order central differences
-        // (src/Block3d.cpp:887-910): ((f[-2]-f[+2])/12 + (f[+1]-f[-1])*2/3) / h.
-        const Consts<R>& CS = consts_of<R>(s);
-        R dv = d4<R>(V0 + (n - 1) * RV, r, 1, CS.c12x, CS.c23x) + d4<R>(V1 + (n - 1) * RV, r, ry, CS.c12y, CS.c23y) +
-               d4<R>(V2 + (n - 1) * RV, r, rz, CS.c12z, CS.c23z);
-        df -= dv;
+        const R* vx = V0 + (n - 1) * RV;
+        const R* vy = V1 + (n - 1) * RV;
+        const R* vz = V2 + (n - 1) * RV;
+        df = fma_(vx[r - 2] - vx[r + 2], -CS.c12x, df);
+        df = fma_(vx[r + 1] - vx[r - 1], -CS.c23x, df);
+        df = fma_(vy[r - 2 * ry] - vy[r + 2 * ry], -CS.c12y, df);
+        df = fma_(vy[r + ry] - vy[r - ry], -CS.c23y, df);
+        df = fma_(vz[r - 2 * rz] - vz[r + 2 * rz], -CS.c12z, df);
+        df = fma_(vz[r + rz] - vz[r - rz], -CS.c23z, df);
       }
       const double dfd = (double)df;
       const double q0 = s.Q[n * V + o];
@@ -793,33 +809,36 @@ __device__ __forceinline__ void update_tiles(const SolveDev* __restrict__ solves
       if constexpr (MIXED) {
         store_mixed(s, d, mc);
       } else {
-        s.pd.rho[d] = qn[0];
-        s.pd.u[d] = uu;
-        s.pd.v[d] = vv;
-        s.pd.w[d] = ww;
-        s.pd.p[d] = pp;
-        s.pd.T[d] = TT;
-        s.pd.srho[d] = sr;
-        s.pd.H[d] = HH;
+        double* b = s.pd.rho + d;  // consecutive PrimSet blocks, as in store_mixed
+        b[0] = qn[0];
+        b[V] = uu;
+        b[2 * V] = vv;
+        b[3 * V] = ww;
+        b[4 * V] = pp;
+        b[5 * V] = TT;
+        b[6 * V] = sr;
+        b[7 * V] = HH;
       }
     };
     store(o);
     const bool xl = i < NG, xh = i >= s.IM - NG, yl = j < NG, yh = j >= s.JM - NG, zl = k < NG,
                zh = k >= s.KM - NG;
     if (xl || xh || yl || yh || zl || zh) {
-      // Image offsets per axis: slot 0 = the cell, 1 = +extent, 2 = -extent.
+      // Image m = a + 3 b + 9 c (m = 0 is the cell itself); per axis, slot 0 =
+      // the cell's own coordinate, 1 = + extent (used when near the low end),
+      // 2 = - extent (near the high end).  A rolled loop keeps few registers live.
       const long long sy = s.nx, sz = (long long)s.nx * s.ny;
-      const long long dx3[3] = {0, (long long)s.IM, -(long long)s.IM};
-      const long long dy3[3] = {0, (long long)s.JM * sy, -(long long)s.JM * sy};
-      const long long dz3[3] = {0, (long long)s.KM * sz, -(long long)s.KM * sz};
-      const bool ux[3] = {true, xl, xh}, uy[3] = {true, yl, yh}, uz[3] = {true, zl, zh};
-#pragma unroll
-      for (int c3 = 0; c3 < 3; ++c3)
-#pragma unroll
-        for (int b2 = 0; b2 < 3; ++b2)
-#pragma unroll
-          for (int a1 = 0; a1 < 3; ++a1)
-            if ((a1 | b2 | c3) && ux[a1] && uy[b2] && uz[c3]) store(o + dx3[a1] + dy3[b2] + dz3[c3]);
+#pragma unroll 1
+      for (int m = 1; m < 27; ++m) {
+        const int a = m % 3, b = (m / 3) % 3, c = m / 9;
+        const bool use = (a == 0 || (a == 1 ? xl : xh)) && (b == 0 || (b == 1 ? yl : yh)) &&
+                         (c == 0 || (c == 1 ? zl : zh));
+        if (!use) continue;
+        const long long ox = a == 0 ? 0 : (a == 1 ? (long long)s.IM : -(long long)s.IM);
+        const long long oy = b == 0 ? 0 : (b == 1 ? (long long)s.JM : -(long long)s.JM);
+        const long long oz = c == 0 ? 0 : (c == 1 ? (long long)s.KM : -(long long)s.KM);
+        store(o + ox + oy * sy + oz * sz);
+      }
     }
   }
 }
