@@ -74,7 +74,7 @@ size_t tile_count(long long ex, long long ey, long long ez, int rows = TILE_Y) {
 
 // Byte offsets of everything a solve's arena holds (see cbns_create).
 struct ArenaLayout {
-  size_t oQ, oQp, oStage, oPrim, oF[3], oFv[3], oFf[3], oFvf[3], oUf, oPf, oCtl, oDesc, oTi, oTr, oTp, oPart, oOut,
+  size_t oQ, oQp, oStage, oPrim, oF[3], oTv, oFf[3], oTvf, oUf, oPf, oCtl, oDesc, oTi, oTr, oTp, oPart, oOut,
       total;
 };
 
@@ -93,12 +93,12 @@ ArenaLayout arena_layout(const SolveDev& s, bool mixed, size_t n_int, size_t n_r
   L.oPrim = take(9 * dV);
   if (!mixed) {
     for (int d = 0; d < 3; ++d) L.oF[d] = take(sizeof(double) * NEQ * (size_t)s.IV);
-    for (int d = 0; d < 3; ++d) L.oFv[d] = take(sizeof(double) * (NEQ - 1) * (size_t)s.RV);
+    L.oTv = take(sizeof(double) * kViscTerms * (size_t)s.RV);
   } else {
     L.oUf = take(NEQ * fV);
     L.oPf = take(9 * fV);
     for (int d = 0; d < 3; ++d) L.oFf[d] = take(sizeof(float) * NEQ * (size_t)s.IV);
-    for (int d = 0; d < 3; ++d) L.oFvf[d] = take(sizeof(float) * (NEQ - 1) * (size_t)s.RV);
+    L.oTvf = take(sizeof(float) * kViscTerms * (size_t)s.RV);
   }
   L.oCtl = take(sizeof(SolveCtl));
   L.oDesc = take(sizeof(SolveDev));
@@ -244,7 +244,7 @@ cbns_status cbns_create(const cbns_params* p, uint32_t IM, uint32_t JM, uint32_t
   const size_t oQ = L.oQ, oQp = L.oQp, oStage = L.oStage, oPrim = L.oPrim, oUf = L.oUf, oPf = L.oPf;
   const size_t oCtl = L.oCtl, oDesc = L.oDesc, oTi = L.oTi, oTr = L.oTr, oTp = L.oTp, oPart = L.oPart,
                oOut = L.oOut;
-  const size_t *oF = L.oF, *oFv = L.oFv, *oFf = L.oFf, *oFvf = L.oFvf;
+  const size_t *oF = L.oF, *oFf = L.oFf;
   h->arena_bytes = off;
   cudaError_t e = cudaMalloc(&h->arena, off);
   if (e != cudaSuccess) return bail(cuda_fail(e, "cudaMalloc(arena)"));
@@ -261,10 +261,10 @@ cbns_status cbns_create(const cbns_params* p, uint32_t IM, uint32_t JM, uint32_t
   if (!mixed) {
     for (int d = 0; d < 3; ++d) {
       s.F[d] = (double*)(A + oF[d]);
-      s.Fv[d] = (double*)(A + oFv[d]);
       s.Ff[d] = nullptr;
-      s.Fvf[d] = nullptr;
     }
+    s.Tv = (double*)(A + L.oTv);
+    s.Tvf = nullptr;
     s.Uf = nullptr;
     s.pf = PrimSet<float>{};
   } else {
@@ -274,10 +274,10 @@ cbns_status cbns_create(const cbns_params* p, uint32_t IM, uint32_t JM, uint32_t
                           pfb + 5 * s.V, pfb + 6 * s.V, pfb + 7 * s.V, pfb + 8 * s.V};
     for (int d = 0; d < 3; ++d) {
       s.Ff[d] = (float*)(A + oFf[d]);
-      s.Fvf[d] = (float*)(A + oFvf[d]);
       s.F[d] = nullptr;
-      s.Fv[d] = nullptr;
     }
+    s.Tvf = (float*)(A + L.oTvf);
+    s.Tv = nullptr;
   }
   const cbns_params& P = h->params;
   // Reference state of the FP32-mixed perturbation form: the reference's

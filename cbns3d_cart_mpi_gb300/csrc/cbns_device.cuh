@@ -22,6 +22,18 @@ namespace cbns {
 constexpr int NEQ = 5;
 constexpr int NG = 4;
 constexpr int NGV = 2;
+// Viscous terms kept on the NGV ring: six stresses and three energy fluxes.
+constexpr int kViscTerms = 9;
+enum ViscTerm { TXX = 0, TYY, TZZ, TXY, TXZ, TYZ, EX, EY, EZ };
+// The term differenced along direction d in the equation of momentum component
+// n - 1 (n = 1..3) or energy (n = 4): the components of Ev, Fv, Gv
+// (src/Block3d.cpp:812-868).
+__host__ __device__ constexpr int visc_term(int n, int d) {
+  return n == 1 ? (d == 0 ? TXX : d == 1 ? TXY : TXZ)
+       : n == 2 ? (d == 0 ? TXY : d == 1 ? TYY : TYZ)
+       : n == 3 ? (d == 0 ? TXZ : d == 1 ? TYZ : TZZ)
+                : (d == 0 ? EX : d == 1 ? EY : EZ);
+}
 constexpr int TILE_X = 32;
 constexpr int TILE_Y = 4;
 constexpr int TILE_THREADS = TILE_X * TILE_Y;
@@ -89,17 +101,19 @@ struct SolveDev {
   double* Qp;
   // binary64 primitives (binary64 mode; in FP32-mixed mode filled on demand for output)
   PrimSet<double> pd;
-  // binary64 mode: face fluxes (interior, 5 components) and viscous fluxes Ev, Fv,
-  // Gv on the NGV ring (4 components)
+  // binary64 mode: face fluxes (interior, 5 components) and the viscous terms on
+  // the NGV ring: 9 blocks of RV values, the stresses txx, tyy, tzz, txy, txz,
+  // tyz and the energy fluxes of Ev, Fv, Gv (their other 9 components are
+  // stresses: Ev = (txx, txy, txz, ex), Fv = (txy, tyy, tyz, ey), Gv = (txz, tyz, tzz, ez))
   double* F[3];
-  double* Fv[3];
+  double* Tv;
   // FP32-mixed mode: the stage input as a binary32 perturbation of the reference
   // state (rho - rho_ref, rho*u, rho*v, rho*w, E - E_ref), its primitives, and
-  // binary32 face and viscous fluxes
+  // binary32 face fluxes and viscous terms
   float* Uf;
   PrimSet<float> pf;
   float* Ff[3];
-  float* Fvf[3];
+  float* Tvf;
   // reference state of the perturbation form (u_ref = 0, E_ref = p_ref/(gamma-1))
   double rho_ref, p_ref, E_ref, T_ref;
   // parameters (src/read_input.cpp:78-90)

@@ -677,30 +677,22 @@ __global__ void __launch_bounds__(kMaxThreads) k_viscous(const SolveDev* __restr
     const R uu = P.u[o], vv = P.v[o], ww = P.w[o];
     const long long r = ring_off(s, tc.i, tc.j, tc.k);
     const long long RV = s.RV;
-    R* Ev;
-    R* Fv;
-    R* Gv;
+    R* tv;
     if constexpr (MIXED) {
-      Ev = s.Fvf[0];
-      Fv = s.Fvf[1];
-      Gv = s.Fvf[2];
+      tv = s.Tvf + r;
     } else {
-      Ev = s.Fv[0];
-      Fv = s.Fv[1];
-      Gv = s.Fv[2];
+      tv = s.Tv + r;
     }
-    Ev[r] = txx;
-    Ev[RV + r] = txy;
-    Ev[2 * RV + r] = txz;
-    Ev[3 * RV + r] = uu * txx + vv * txy + ww * txz - mk * Tx;
-    Fv[r] = txy;
-    Fv[RV + r] = tyy;
-    Fv[2 * RV + r] = tyz;
-    Fv[3 * RV + r] = uu * txy + vv * tyy + ww * tyz - mk * Ty;
-    Gv[r] = txz;
-    Gv[RV + r] = tyz;
-    Gv[2 * RV + r] = tzz;
-    Gv[3 * RV + r] = uu * txz + vv * tyz + ww * tzz - mk * Tz;
+    // Ev, Fv, Gv (src/Block3d.cpp:812-868) share their stresses: nine terms.
+    tv[TXX * RV] = txx;
+    tv[TYY * RV] = tyy;
+    tv[TZZ * RV] = tzz;
+    tv[TXY * RV] = txy;
+    tv[TXZ * RV] = txz;
+    tv[TYZ * RV] = tyz;
+    tv[EX * RV] = uu * txx + vv * txy + ww * txz - mk * Tx;
+    tv[EY * RV] = uu * txy + vv * tyy + ww * tyz - mk * Ty;
+    tv[EZ * RV] = uu * txz + vv * tyz + ww * tzz - mk * Tz;
   }
 }
 
@@ -736,15 +728,13 @@ __device__ __forceinline__ void update_tiles(const SolveDev* __restrict__ solves
     const R* F0;
     const R* F1;
     const R* F2;
-    const R* V0;
-    const R* V1;
-    const R* V2;
+    const R* TV;
     if constexpr (MIXED) {
       F0 = s.Ff[0], F1 = s.Ff[1], F2 = s.Ff[2];
-      V0 = s.Fvf[0], V1 = s.Fvf[1], V2 = s.Fvf[2];
+      TV = s.Tvf;
     } else {
       F0 = s.F[0], F1 = s.F[1], F2 = s.F[2];
-      V0 = s.Fv[0], V1 = s.Fv[1], V2 = s.Fv[2];
+      TV = s.Tv;
     }
     // The face fluxes are stored doubled: hf = 0.5 / h.
     const R idx = consts_of<R>(s).hfx, idy = consts_of<R>(s).hfy, idz = consts_of<R>(s).hfz;
@@ -761,9 +751,9 @@ __device__ __forceinline__ void update_tiles(const SolveDev* __restrict__ solves
       df = fma_(F1[n * IV + fy] - F1[n * IV + fo], idy, df);
       df = fma_(F2[n * IV + fz] - F2[n * IV + fo], idz, df);
       if (n > 0) {
-        const R* vx = V0 + (n - 1) * RV;
-        const R* vy = V1 + (n - 1) * RV;
-        const R* vz = V2 + (n - 1) * RV;
+        const R* vx = TV + visc_term(n, 0) * RV;
+        const R* vy = TV + visc_term(n, 1) * RV;
+        const R* vz = TV + visc_term(n, 2) * RV;
         df = fma_(vx[r - 2] - vx[r + 2], -CS.c12x, df);
         df = fma_(vx[r + 1] - vx[r - 1], -CS.c23x, df);
         df = fma_(vy[r - 2 * ry] - vy[r + 2 * ry], -CS.c12y, df);
@@ -843,18 +833,17 @@ __device__ __forceinline__ void update_tiles(const SolveDev* __restrict__ solves
   }
 }
 
-// The binary64 update is FP64-pipe bound and keeps its registers; the binary32
-// one is memory-latency bound and wants the warps: at least three CTAs of 256
-// threads per SM caps it at 80 registers without spills.  (Measured: an explicit
-// minimum of one CTA for the binary64 kernel makes it 6% slower than none.)
+// Register caps, measured at 256^3: the binary64 update (FP64-pipe bound) runs
+// 11% faster at 80 registers (24 warps per SM, a few spills) than unconstrained
+// (126 registers); the binary32 one (memory-latency bound) 12% faster at 64
+// (32 warps per SM) than at 80.
 template <typename R>
-__global__ void __launch_bounds__(kMaxThreads) k_update(const SolveDev* __restrict__ solves,
-                                                        const TileRef* __restrict__ tiles, int ntiles, int stage) {
+__global__ void __maxnreg__(80) k_update(const SolveDev* __restrict__ solves,
+                                         const TileRef* __restrict__ tiles, int ntiles, int stage) {
   update_tiles<R>(solves, tiles, ntiles, stage);
 }
-__global__ void __launch_bounds__(kMaxThreads, 3) k_update_f32(const SolveDev* __restrict__ solves,
-                                                               const TileRef* __restrict__ tiles, int ntiles,
-                                                               int stage) {
+__global__ void __maxnreg__(64) k_update_f32(const SolveDev* __restrict__ solves,
+                                              const TileRef* __restrict__ tiles, int ntiles, int stage) {
   update_tiles<float>(solves, tiles, ntiles, stage);
 }
 
