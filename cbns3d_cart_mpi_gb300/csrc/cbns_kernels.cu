@@ -640,9 +640,11 @@ template <typename R>
 __device__ __forceinline__ R d4(const R* __restrict__ f, long long o, long long st, R c12h, R c23h) {
   return (f[o - 2 * st] - f[o + 2 * st]) * c12h + (f[o + st] - f[o - st]) * c23h;
 }
+// Register caps: 64 for binary64 (FP64-pipe bound; lower caps measured no
+// faster) and 40 for binary32 (memory bound; 4% faster than at 48, spills at 32).
 template <typename R>
-__global__ void __launch_bounds__(kMaxThreads) k_viscous(const SolveDev* __restrict__ solves,
-                                                         const TileRef* __restrict__ tiles, int ntiles) {
+__global__ void __maxnreg__(sizeof(R) == 4 ? 40 : 64) k_viscous(const SolveDev* __restrict__ solves,
+                                                                const TileRef* __restrict__ tiles, int ntiles) {
   constexpr bool MIXED = sizeof(R) == 4;
   for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
     TileCell tc = tile_cell(tiles[t], -NGV);
