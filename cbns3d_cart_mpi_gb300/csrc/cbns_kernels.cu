@@ -109,7 +109,7 @@ __device__ __forceinline__ MixedCell mixed_cell(const SolveDev& s, const double 
   const Consts<float>& C = s.cf;
   const float rp = (float)(q[0] - s.cd.rho_ref);
   const float Ep = (float)(q[4] - s.cd.E_ref);
-  const float r = (float)q[0];
+  const float r = C.rho_ref + rp;  // binary32 density without another conversion
   m.U[0] = rp;
   m.U[1] = (float)q[1];
   m.U[2] = (float)q[2];
@@ -416,26 +416,38 @@ __device__ __forceinline__ void weno5_pair(const R (&v)[6], Weno<R>& L, Weno<R>&
 
 // r[n] = base[n] + num[n] / den[n] for ten parts (both states of a face).
 // Binary64: one division (Montgomery's simultaneous inversion).  Every den is
-// positive and at least 2.56e-22, so no prefix product underflows, and one that
-// overflows makes the last one infinite; the batch is used while that product
-// lies in about [1e-300, 1e300] (biased exponent 27 .. 2019, tested on the
-// integer pipe), otherwise each quotient is divided on its own.
+// positive and at least 2.56e-22; the batch is used while the product of each
+// half lies in about [1e-150, 1e150] (biased exponent 525 .. 1520, tested on the
+// integer pipe), which keeps every partial product and partial reciprocal in
+// the normal range; otherwise each quotient is divided on its own.
 // Binary32: each quotient is divided (the binary32 pipe divides cheaply).
 __device__ __forceinline__ void weno_divide10(const Weno<double> (&w)[10], const double (&base)[10],
                                               double (&r)[10]) {
-  double pre[10];
-  pre[0] = w[0].den;
+  // Two halves of five: prefix products within each half, one reciprocal of the
+  // whole product, then 1/(half product) = reciprocal x (other half's product).
+  // The same 28 multiplications as one chain of ten, at half its depth.
+  double pa[5], pb[5];
+  pa[0] = w[0].den;
+  pb[0] = w[5].den;
 #pragma unroll
-  for (int n = 1; n < 10; ++n) pre[n] = pre[n - 1] * w[n].den;
-  const unsigned bexp = (unsigned)((unsigned long long)__double_as_longlong(pre[9]) >> 52);
-  if (bexp - 27u < 1993u) {
-    double inv = 1.0 / pre[9];
+  for (int n = 1; n < 5; ++n) {
+    pa[n] = pa[n - 1] * w[n].den;
+    pb[n] = pb[n - 1] * w[5 + n].den;
+  }
+  const unsigned ea = (unsigned)((unsigned long long)__double_as_longlong(pa[4]) >> 52);
+  const unsigned eb = (unsigned)((unsigned long long)__double_as_longlong(pb[4]) >> 52);
+  if (ea - 525u < 996u && eb - 525u < 996u) {
+    const double inv = 1.0 / (pa[4] * pb[4]);
+    double ia = inv * pb[4], ib = inv * pa[4];  // 1/pa[4], 1/pb[4]
 #pragma unroll
-    for (int n = 9; n > 0; --n) {
-      r[n] = fma(w[n].num, inv * pre[n - 1], base[n]);
-      inv *= w[n].den;
+    for (int n = 4; n > 0; --n) {
+      r[n] = fma(w[n].num, ia * pa[n - 1], base[n]);
+      r[5 + n] = fma(w[5 + n].num, ib * pb[n - 1], base[5 + n]);
+      ia *= w[n].den;
+      ib *= w[5 + n].den;
     }
-    r[0] = fma(w[0].num, inv, base[0]);
+    r[0] = fma(w[0].num, ia, base[0]);
+    r[5] = fma(w[5].num, ib, base[5]);
   } else {
 #pragma unroll
     for (int n = 0; n < 10; ++n) r[n] = base[n] + w[n].num / w[n].den;
@@ -742,6 +754,8 @@ __device__ __forceinline__ void update_tiles(const SolveDev* __restrict__ solves
     const R idx = consts_of<R>(s).hfx, idy = consts_of<R>(s).hfy, idz = consts_of<R>(s).hfz;
 
     const Consts<R>& CS = consts_of<R>(s);
+    // FP32-mixed stages 2 and 3: the binary32 weight of dt df (1/4 or 2/3 of dt).
+    const float cdt = MIXED && stage != 1 ? (float)((stage == 2 ? 0.25 : 2.0 / 3.0) * dt) : 0.0f;
     double qn[NEQ];
 #pragma unroll
     for (int n = 0; n < NEQ; ++n) {
@@ -763,14 +777,23 @@ __device__ __forceinline__ void update_tiles(const SolveDev* __restrict__ solves
         df = fma_(vz[r - 2 * rz] - vz[r + 2 * rz], -CS.c12z, df);
         df = fma_(vz[r + rz] - vz[r - rz], -CS.c23z, df);
       }
-      const double dfd = (double)df;
       const double q0 = s.Q[n * V + o];
-      if (stage == 1) {
-        qn[n] = q0 - dt * dfd;
-      } else if (stage == 2) {
-        qn[n] = 0.75 * q0 + 0.25 * (s.Qp[n * V + o] - dt * dfd);
+      if (MIXED && stage != 1) {
+        // FP32-mixed stages 2 and 3: the increment c dt df in binary32 (df has
+        // binary32 accuracy), the combination of the binary64 states in binary64:
+        // 3/4 q0 + 1/4 qp - 1/4 dt df and 1/3 q0 + 2/3 qp - 2/3 dt df.
+        const double qp = s.Qp[n * V + o];
+        const double inc = (double)(cdt * (float)df);
+        qn[n] = stage == 2 ? fma(0.75, q0, fma(0.25, qp, -inc)) : fma(1.0 / 3.0, q0, fma(2.0 / 3.0, qp, -inc));
       } else {
-        qn[n] = (q0 + 2.0 * (s.Qp[n * V + o] - dt * dfd)) * (1.0 / 3.0);
+        const double dfd = (double)df;
+        if (stage == 1) {
+          qn[n] = q0 - dt * dfd;
+        } else if (stage == 2) {
+          qn[n] = 0.75 * q0 + 0.25 * (s.Qp[n * V + o] - dt * dfd);
+        } else {
+          qn[n] = (q0 + 2.0 * (s.Qp[n * V + o] - dt * dfd)) * (1.0 / 3.0);
+        }
       }
     }
     double* out = stage == 3 ? s.Q : s.Qp;
@@ -780,7 +803,7 @@ __device__ __forceinline__ void update_tiles(const SolveDev* __restrict__ solves
     MixedCell mc;
     if constexpr (MIXED) {
       mc = mixed_cell(s, qn);
-      if (!(qn[0] > 0.0) || !(s.cf.p_ref + mc.p > 0.0f)) atomicOr(&ctl->status, 1);
+      if (!(mc.rho > 0.0f) || !(s.cf.p_ref + mc.p > 0.0f)) atomicOr(&ctl->status, 1);
     } else {
       const double ir = 1.0 / qn[0];
       uu = qn[1] * ir, vv = qn[2] * ir, ww = qn[3] * ir;
