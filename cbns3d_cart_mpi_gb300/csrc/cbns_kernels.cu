@@ -78,20 +78,40 @@ __device__ __forceinline__ float sqrt_(float a) { return a * rsqrtf(a); }
 
 __device__ __forceinline__ int wrap(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
 
+struct Prims64 {
+  double u, v, w, p, T, sr, H;
+};
+
+// Binary64 primitives of one state (Block3d::calc_primitive, src/Block3d.cpp:359-385),
+// with 1/rho and sqrt(rho) from one reciprocal square root (a few ulp from the
+// reference's division and square root).  The start-up fill and the update
+// both use it, so a solve restarted from its own state continues bitwise.
+__device__ __forceinline__ Prims64 prims64(const SolveDev& s, double r, double ru, double rv, double rw, double E) {
+  const double rs = rsqrt(r);
+  const double ir = rs * rs;
+  Prims64 q;
+  q.u = ru * ir;
+  q.v = rv * ir;
+  q.w = rw * ir;
+  const double q2 = q.u * q.u + q.v * q.v + q.w * q.w;
+  q.p = s.gam1 * (E - 0.5 * r * q2);
+  q.T = s.gM2 * q.p * ir;
+  q.sr = r * rs;
+  q.H = s.cd.gamma_gam1_inv * q.p * ir + 0.5 * q2;
+  return q;
+}
+
 __device__ __forceinline__ void store_prims(const SolveDev& s, long long o, double r, double ru,
                                             double rv, double rw, double E) {
-  double ir = 1.0 / r;
-  double uu = ru * ir, vv = rv * ir, ww = rw * ir;
-  double q2 = uu * uu + vv * vv + ww * ww;
-  double pp = s.gam1 * (E - 0.5 * r * q2);
+  const Prims64 q = prims64(s, r, ru, rv, rw, E);
   s.pd.rho[o] = r;
-  s.pd.u[o] = uu;
-  s.pd.v[o] = vv;
-  s.pd.w[o] = ww;
-  s.pd.p[o] = pp;
-  s.pd.T[o] = s.gM2 * pp * ir;
-  s.pd.srho[o] = sqrt(r);
-  s.pd.H[o] = s.cd.gamma_gam1_inv * pp * ir + 0.5 * q2;
+  s.pd.u[o] = q.u;
+  s.pd.v[o] = q.v;
+  s.pd.w[o] = q.w;
+  s.pd.p[o] = q.p;
+  s.pd.T[o] = q.T;
+  s.pd.srho[o] = q.sr;
+  s.pd.H[o] = q.H;
 }
 
 // FP32-mixed: the binary32 perturbation state and primitives of a binary64 state.
@@ -264,22 +284,22 @@ __device__ __forceinline__ double warp_max(double v) {
 }
 
 // The reference's per-cell sum over x, y, z of |u_d| + c/h_d + fv/h_d^2 with
-// fv = 2 mu C_dt_v |u| / (rho c), regrouped as
-//   (|u| + |v| + |w|) + c (1/hx + 1/hy + 1/hz) + fv (1/hx^2 + 1/hy^2 + 1/hz^2)
-// with one reciprocal of rho and one reciprocal square root (c = c^2 / c).
+// c = sqrt(gamma p / rho) and fv = 2 mu C_dt_v |u| / (rho c), regrouped as
+//   (|u| + |v| + |w|) + c (1/hx + 1/hy + 1/hz) + fv (1/hx^2 + 1/hy^2 + 1/hz^2),
+// with one reciprocal square root: z = 1/sqrt(gamma p rho) = 1/(rho c) and
+// c = gamma p z.
 template <typename R>
 __device__ __forceinline__ double dt_speed(const SolveDev& s, long long o) {
   const PrimSet<R>& P = prims_of<R>(s);
   const R rr = P.rho[o], uu = P.u[o], vv = P.v[o], ww = P.w[o];
   const Consts<R>& C = consts_of<R>(s);
   const R pp = (sizeof(R) == 4) ? C.p_ref + P.p[o] : P.p[o];
-  const R ir = div_((R)1, rr);
-  const R c2 = (C.gamma * pp) * ir;
-  const R ic = rsqrt(c2);
-  const R c = c2 * ic;
+  const R gp = C.gamma * pp;
+  const R z = rsqrt(gp * rr);
+  const R c = gp * z;
   const R q2 = fma_(ww, ww, fma_(vv, vv, uu * uu));
   const R q = (sizeof(R) == 4 && !(q2 > (R)0)) ? (R)0 : sqrt_(q2);  // binary32 sqrt_ is q2 * rsqrt(q2)
-  const R fv = (C.C_dt_v2 * P.mu[o]) * q * (ir * ic);
+  const R fv = (C.C_dt_v2 * P.mu[o]) * q * z;
   return (double)((fabs(uu) + fabs(vv) + fabs(ww)) + fma_(c, C.sum_ih, fv * C.sum_ih2));
 }
 
@@ -805,13 +825,8 @@ __device__ __forceinline__ void update_tiles(const SolveDev* __restrict__ solves
       mc = mixed_cell(s, qn);
       if (!(mc.rho > 0.0f) || !(s.cf.p_ref + mc.p > 0.0f)) atomicOr(&ctl->status, 1);
     } else {
-      const double ir = 1.0 / qn[0];
-      uu = qn[1] * ir, vv = qn[2] * ir, ww = qn[3] * ir;
-      const double q2 = uu * uu + vv * vv + ww * ww;
-      pp = s.gam1 * (qn[4] - 0.5 * qn[0] * q2);
-      TT = s.gM2 * pp * ir;
-      sr = sqrt(qn[0]);
-      HH = s.cd.gamma_gam1_inv * pp * ir + 0.5 * q2;
+      const Prims64 q = prims64(s, qn[0], qn[1], qn[2], qn[3], qn[4]);
+      uu = q.u, vv = q.v, ww = q.w, pp = q.p, TT = q.T, sr = q.sr, HH = q.H;
       if (!(qn[0] > 0.0) || !(pp > 0.0)) atomicOr(&ctl->status, 1);
     }
 
