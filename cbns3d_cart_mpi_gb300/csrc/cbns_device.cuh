@@ -103,8 +103,8 @@ struct SolveDev {
   PrimSet<double> pd;
   // binary64 mode: face fluxes (interior, 5 components) and the viscous terms on
   // the NGV ring: 9 blocks of RV values, the stresses txx, tyy, tzz, txy, txz,
-  // tyz and the energy fluxes of Ev, Fv, Gv (their other 9 components are
-  // stresses: Ev = (txx, txy, txz, ex), Fv = (txy, tyy, tyz, ey), Gv = (txz, tyz, tzz, ez))
+  // tyz and the energy fluxes ex, ey, ez -- the 9 distinct components of
+  // Ev = (txx, txy, txz, ex), Fv = (txy, tyy, tyz, ey), Gv = (txz, tyz, tzz, ez)
   double* F[3];
   double* Tv;
   // FP32-mixed mode: the stage input as a binary32 perturbation of the reference

@@ -1,29 +1,33 @@
 // cbns_kernels.cu — sm_103a kernels of one RK3 stage of the cbns3d right-hand side.
 //
-// One stage (src/cbns3d.cpp:203-240) is four launches over a flattened tile
+// One stage (src/cbns3d.cpp:203-240) is five launches over a flattened tile
 // table that may span many solves:
 //   k_inviscid<0,1,2>  characteristic WENO5 + Roe eigenvectors + local Lax-Friedrichs
 //                      flux at every face normal to x, y, z (Block3d::rec_riemann_x/y/z)
-//   k_viscous          4th-order velocity/temperature gradients, Sutherland mu, stress,
-//                      heat flux and the viscous fluxes Ev, Fv, Gv on the NGV ring
+//   k_viscous          4th-order velocity/temperature gradients, Sutherland mu, and the
+//                      nine distinct terms of the viscous fluxes Ev, Fv, Gv (six
+//                      stresses, three energy fluxes) on the NGV ring
 //                      (calc_viscous_terms + calc_viscous_flux)
 //   k_update           flux differences + 4th-order viscous divergence, SSP-RK3 update,
-//                      then the periodic ghost fill and the primitive recovery of the
+//   (k_update_f32)     then the periodic ghost fill and the primitive recovery of the
 //                      new state, written to the cell and all its ghost images
 //                      (calc_viscous_flux_contribution tail, update_rk3,
 //                      boundary_condition, calc_primitive)
 // plus, once per step, k_dt_reduce + k_dt_finalize (calc_dt, the MIN all-reduce,
 // the clip to t_end and is_finished).
 //
-// The arithmetic is binary64 throughout.  GB300 issues binary64 at about 1/64 of
-// the binary32 rate (about 2 DFMA per clock per SM), so the kernels are bound by
-// the FP64 pipe and are written to issue few binary64 instructions: the
-// eigenvector products use the structure of L and R for axis-aligned normals,
-// the stencil projections are shared by the two biased reconstructions of a
-// face, the five WENO normalisations of a state share one division, and
-// divisions by constants become multiplications.  These rewrites change
-// rounding only (a few ulp per operation); the results stay within the 1e-11
-// relative tolerance of the reference after 100 steps.
+// Binary64 solves run the kernels in binary64.  GB300 issues binary64 at about
+// 1/64 of the binary32 rate (about 2 DFMA per clock per SM), so these kernels
+// are bound by the FP64 pipe and are written to issue few binary64
+// instructions: the eigenvector products use the structure of L and R for
+// axis-aligned normals, the stencil projections are shared by the two biased
+// reconstructions of a face, WENO5 works on first differences, the ten WENO
+// normalisations of a face share one division, and divisions by constants
+// become multiplications.  These rewrites change rounding only (a few ulp per
+// operation); the results stay within the 1e-11 relative tolerance of the
+// reference after 100 steps.  FP32-mixed solves run the same kernels
+// instantiated for binary32 on a perturbation of the state about the free
+// stream, with the binary64 state and its RK3 combination kept in binary64.
 #include <cuda_runtime.h>
 
 #include <cmath>
