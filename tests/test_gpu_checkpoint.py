@@ -35,12 +35,13 @@ def test_load_reference_checkpoint(golden_dir):
     assert np.array_equal(a.download_Q(), b.download_Q()) and a.time() == b.time()
 
 
-@pytest.mark.parametrize("shape", [(4, 5, 6), (60, 52, 44), (96, 96, 96)])  # 1, 2 and 6 chunks
-def test_save_matches_host_writer_and_continues(tmp_path, shape):
+@pytest.mark.parametrize("shape,precision", [((4, 5, 6), "fp64"), ((60, 52, 44), "fp64"), ((96, 96, 96), "fp64"),
+                                             ((16, 12, 20), "fp32_mixed")])  # 1, 2 and 6 chunks
+def test_save_matches_host_writer_and_continues(tmp_path, shape, precision):
     from cbns3d_cart_mpi_gb300.solver import Solver, output_bin
     IM, JM, KM = shape
     p = tgv_params(IM, JM=JM, KM=KM)
-    s = Solver(p)
+    s = Solver(p, precision=precision)
     s.init_tgv(seed=3, amp=1e-3, nmodes=8, kmax=3)
     s.step()
     s.step()
@@ -48,7 +49,7 @@ def test_save_matches_host_writer_and_continues(tmp_path, shape):
     t, _ = s.time()
     output_bin(str(tmp_path / "b.dat"), t, s.download_Q(), IM, JM, KM)
     assert (tmp_path / "a.dat").read_bytes() == (tmp_path / "b.dat").read_bytes()
-    r = Solver(p)
+    r = Solver(p, precision=precision)
     assert r.load_checkpoint(str(tmp_path / "a.dat")) == t
     assert np.array_equal(r.download_Q(), s.download_Q())
     # A restart sets the lagged mu to 1 before its first calc_dt, so the solves
