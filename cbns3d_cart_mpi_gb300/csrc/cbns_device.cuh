@@ -49,6 +49,8 @@ struct SolveCtl {
   int status;                    // CBNS_ERR_NONPHYSICAL bit pattern once a stage met a bad state
   unsigned int steps;            // steps taken since upload
   int pad;
+  float cdt[2];                  // binary32 dt/4 and 2 dt/3: FP32-mixed stages 2 and 3
+  float pad2[2];
 };
 
 // Cell-centred primitive fields of a stage input.  Binary64 solves store them

@@ -362,6 +362,8 @@ __global__ void k_dt_finalize(const SolveDev* __restrict__ solves, int nsolves, 
   if (ctl->t_end - ctl->t_cur < dt) dt = ctl->t_end - ctl->t_cur;
   ctl->t_cur += dt;
   ctl->dt = dt;
+  ctl->cdt[0] = (float)(0.25 * dt);
+  ctl->cdt[1] = (float)((2.0 / 3.0) * dt);
   ctl->active = 1;
   ctl->steps += 1;
 }
@@ -377,6 +379,8 @@ __global__ void k_dt_raw(const SolveDev* __restrict__ solves, int sidx, double* 
 __global__ void k_set_dt(const SolveDev* __restrict__ solves, int sidx, double dt) {
   SolveCtl* ctl = solves[sidx].ctl;
   ctl->dt = dt;
+  ctl->cdt[0] = (float)(0.25 * dt);
+  ctl->cdt[1] = (float)((2.0 / 3.0) * dt);
   ctl->active = 1;
 }
 
@@ -778,8 +782,9 @@ __device__ __forceinline__ void update_tiles(const SolveDev* __restrict__ solves
     const R idx = consts_of<R>(s).hfx, idy = consts_of<R>(s).hfy, idz = consts_of<R>(s).hfz;
 
     const Consts<R>& CS = consts_of<R>(s);
-    // FP32-mixed stages 2 and 3: the binary32 weight of dt df (1/4 or 2/3 of dt).
-    const float cdt = MIXED && stage != 1 ? (float)((stage == 2 ? 0.25 : 2.0 / 3.0) * dt) : 0.0f;
+    // FP32-mixed stages 2 and 3: the binary32 weight of dt df (1/4 or 2/3 of dt,
+    // formed once per step with dt).
+    const float cdt = MIXED && stage != 1 ? ctl->cdt[stage - 2] : 0.0f;
     double qn[NEQ];
 #pragma unroll
     for (int n = 0; n < NEQ; ++n) {
