@@ -108,7 +108,7 @@ def main():
     np.savez(os.path.join(HERE, "tgv_pert.npz"), Q0=interior(state(wd, 0)[1]), Q3=interior(state(wd, 3)[1]),
              dt=steps[:, 1], t=steps[:, 2], N=np.array([12, 12, 12]), Re=800.0, Mach=0.2)
 
-    # 64^3 history: the spec parity case.
+    # 64^3 history: the 100-step parity case.
     p = tgv_params(64)
     wd, steps = run(harness, "tgv64", p, 100, 10)
     dx = 2.0 * np.pi / 64

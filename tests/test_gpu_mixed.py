@@ -3,7 +3,7 @@
 FP32-mixed runs the WENO5 reconstruction, the Roe eigenvector projections and
 the inviscid and viscous fluxes in binary32, on the perturbation of the state
 about the free stream (rho = 1, p = 1/(gamma M^2)); the RK3 accumulation of the
-conserved state stays binary64.  The benchmark spec's bound is 1e-5 relative L-inf
+conserved state stays binary64.  The bound is 1e-5 relative L-inf
 per conserved field against the binary64 oracle; the tests check it on the
 64^3 100-step case and state the measured error.
 """

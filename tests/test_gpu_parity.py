@@ -2,13 +2,13 @@
 
 Tolerances:
   * per conserved field (rho, rho*u, rho*v, rho*w, E), max|a-b| / max|b| <= 1e-11
-    (the spec parity bar, checked after 100 RK3 steps at 64^3 and on every
+    (the parity bar, checked after 100 RK3 steps at 64^3 and on every
     short case); the kinetic-energy and enstrophy histories to 1e-10;
   * on short runs also an absolute bound: max|a-b| <= 1e-13 times the field's
     scale, where the three momentum components share the momentum scale.  The
     per-field bound alone is loose for rho*w early on, because w starts at 0
     (max|rho*w| is 1.4e-3 after one step at 16^3).  The GPU kernels reorder
-    binary64 operations (shared projections, one division per five WENO weights,
+    binary64 operations (shared projections, one division per ten WENO weights,
     fused multiply-adds), so they differ from the reference by rounding only.
 """
 import os
@@ -128,7 +128,7 @@ def test_ghosts_after_step_are_periodic_images(golden_dir):
 
 
 def test_history_64_100_steps(golden_dir):
-    """North-star parity: 64^3 TGV, 100 RK3 steps, against the reference's own
+    """Parity bar: 64^3 TGV, 100 RK3 steps, against the reference's own
     history and the oracle's full state; KE and enstrophy every 10 steps."""
     from oracle.oracle import OracleBlock
     from cbns3d_cart_mpi_gb300.solver import initial_condition
