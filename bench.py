@@ -308,7 +308,12 @@ def run_ours(args, rank, world, local):
         if rank == 0:
             a = Qm[NG:-NG, NG:-NG, NG:-NG].reshape(-1, 5)
             b = Q64[NG:-NG, NG:-NG, NG:-NG].reshape(-1, 5)
-            err = (np.abs(a - b).max(axis=0) / np.abs(b).max(axis=0)).tolist()
+            # L-inf error over each field's scale; the three momentum fields share
+            # the largest momentum magnitude (rho w starts at exactly zero, so its own
+            # maximum is no scale in the first steps).
+            scale = np.abs(b).max(axis=0)
+            scale[1:4] = scale[1:4].max()
+            err = (np.abs(a - b).max(axis=0) / scale).tolist()
             mtot = sum(v[1] for v in mprof.values())
             mdom = max(mprof, key=lambda k: mprof[k][1])
             if mdom.startswith("inviscid_"):
@@ -319,7 +324,7 @@ def run_ours(args, rank, world, local):
             line["fp32_mixed"] = {
                 "value": world * cells * args.steps / (mms * 1e-3), "unit": UNIT, "ms_per_step": mms / args.steps,
                 "speedup_vs_fp64": ms / mms,
-                "rel_linf_vs_fp64": dict(zip(["rho", "rho*u", "rho*v", "rho*w", "E"], err)),
+                "linf_vs_fp64_over_field_scale": dict(zip(["rho", "rho*u", "rho*v", "rho*w", "E"], err)),
                 "error_after_steps": args.warmup + 2 * args.steps,
                 "kernels": {k: {"launches": v[0], "ms_per_launch": v[1] / v[0], "share": v[1] / mtot}
                             for k, v in mprof.items()},
