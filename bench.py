@@ -356,7 +356,7 @@ def run_ours(args, rank, world, local):
                            "path": "cbns_upload_Q (pinned) + cbns_step + cbns_download_Q (pinned), per step"}
     s.close()
 
-    if rank == 0 and not args.no_cpu_baseline:
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:  # the host baseline is an N=1 figure
         v, th, sec = cpu_sample(N, args.cpu_steps)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": th, "kind": "port",
                                 "sample": "%d full RK3 step(s) of the %d^3 workload, %.1f s" % (args.cpu_steps, N, sec)}
