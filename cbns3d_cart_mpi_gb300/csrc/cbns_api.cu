@@ -198,8 +198,14 @@ cbns_status cbns_create(const cbns_params* p, uint32_t IM, uint32_t JM, uint32_t
     cudaGetLastError();
     return fail(CBNS_ERR_NO_DEVICE, "cbns_create: no CUDA device");
   }
+  // The calling thread's current device, unless CBNS_DEVICE names one.
   int dev = 0;
-  if (const char* e = std::getenv("CBNS_DEVICE")) dev = std::atoi(e);
+  if (const char* e = std::getenv("CBNS_DEVICE")) {
+    dev = std::atoi(e);
+  } else if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    dev = 0;
+  }
   if (dev < 0 || dev >= ndev) return fail(CBNS_ERR_NO_DEVICE, "cbns_create: CBNS_DEVICE out of range");
   cudaDeviceProp prop;
   CBNS_CUDA(cudaGetDeviceProperties(&prop, dev));

@@ -272,8 +272,15 @@ cbns_status cbns_server_create(const cbns_server_opts* opts, cbns_server** out) 
     cudaGetLastError();
     return serve_fail(CBNS_ERR_NO_DEVICE, "cbns_server_create: no CUDA device");
   }
+  // The calling thread's current device, unless CBNS_DEVICE names one; the
+  // worker thread makes it current before it creates any solve.
   int dev = 0;
-  if (const char* e = std::getenv("CBNS_DEVICE")) dev = std::atoi(e);
+  if (const char* e = std::getenv("CBNS_DEVICE")) {
+    dev = std::atoi(e);
+  } else if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    dev = 0;
+  }
   if (dev < 0 || dev >= ndev) return serve_fail(CBNS_ERR_NO_DEVICE, "cbns_server_create: CBNS_DEVICE out of range");
   cudaSetDevice(dev);
   size_t free_b = 0, total_b = 0;

@@ -84,7 +84,8 @@ cbns_status cbns_params_derive(cbns_params* p);
 
 /* Block3d::Block3d + allocate_mem (src/Block3d.cpp:11-135) and gen_mesh's spacing
  * (src/Block3d.cpp:208-219): dx = 2*pi/p->IM etc.  IM, JM, KM are this block's
- * extents (the whole grid on one GPU).  Selects device 0 unless CBNS_DEVICE is set. */
+ * extents (the whole grid on one GPU).  Uses the calling thread's current CUDA device unless the environment variable
+ * CBNS_DEVICE names one. */
 cbns_status cbns_create(const cbns_params* p, uint32_t IM, uint32_t JM, uint32_t KM,
                         int precision, cbns_handle** out);
 cbns_status cbns_destroy(cbns_handle* h);
@@ -240,6 +241,8 @@ typedef struct cbns_server_stats {
   double clock_s;
 } cbns_server_stats;
 
+/* Starts a server on the calling thread's current CUDA device (or the one
+ * CBNS_DEVICE names); its worker thread owns every solve it admits. */
 cbns_status cbns_server_create(const cbns_server_opts* opts, cbns_server** out);
 /* Cancels queued and running requests and joins the worker. */
 cbns_status cbns_server_destroy(cbns_server* s);
