@@ -86,13 +86,22 @@ class Solver:
         _check(_lib.gpu().cbns_init_tgv(self._h, int(seed), float(amp), int(nmodes), int(kmax),
                                         self.params.t_cur if t is None else t), "cbns_init_tgv")
 
+    def _out_state(self, out):
+        """A buffer the library may write a padded state into: float64, C-contiguous,
+        exactly one state long."""
+        if out is None:
+            return np.empty(self.shape)
+        if out.dtype != np.float64 or not out.flags.c_contiguous or out.size != int(np.prod(self.shape)):
+            raise ValueError("out must be a C-contiguous float64 array of %d values" % int(np.prod(self.shape)))
+        return out
+
     def download_Q(self, out=None):
-        out = np.empty(self.shape) if out is None else out
+        out = self._out_state(out)
         _check(_lib.gpu().cbns_download_Q(self._h, _ptr(out)), "cbns_download_Q")
         return out
 
     def download_Q_p(self, out=None):
-        out = np.empty(self.shape) if out is None else out
+        out = self._out_state(out)
         _check(_lib.gpu().cbns_download_Q_p(self._h, _ptr(out)), "cbns_download_Q_p")
         return out
 
@@ -239,6 +248,7 @@ class Server:
         sv = ctypes.c_void_p()
         _check(_lib.gpu().cbns_server_create(ctypes.byref(opts), ctypes.byref(sv)), "cbns_server_create")
         self._s = sv
+        self._shapes = {}  # request id -> padded state shape
         self.precision = precision
 
     def close(self):
@@ -252,19 +262,26 @@ class Server:
         except Exception:
             pass
 
+    def _track(self, rid, params):
+        self._shapes[rid] = (params.KM + 2 * NG, params.JM + 2 * NG, params.IM + 2 * NG, NEQ)
+        return rid
+
     def submit(self, params, Q0, keep_state=False):
         rid = ctypes.c_uint64()
         Q0 = np.ascontiguousarray(Q0, dtype=np.float64)
+        n = NEQ * (params.IM + 2 * NG) * (params.JM + 2 * NG) * (params.KM + 2 * NG)
+        if Q0.size != n:
+            raise ValueError("Q0 has %d values, %d expected" % (Q0.size, n))
         _check(_lib.gpu().cbns_server_submit(self._s, ctypes.byref(params), params.IM, params.JM, params.KM,
                                              _ptr(Q0), int(keep_state), ctypes.byref(rid)), "cbns_server_submit")
-        return rid.value
+        return self._track(rid.value, params)
 
     def submit_tgv(self, params, seed=0, amp=0.0, nmodes=0, kmax=4, keep_state=False):
         rid = ctypes.c_uint64()
         _check(_lib.gpu().cbns_server_submit_tgv(self._s, ctypes.byref(params), params.IM, params.JM, params.KM,
                                                  int(seed), float(amp), int(nmodes), int(kmax), int(keep_state),
                                                  ctypes.byref(rid)), "cbns_server_submit_tgv")
-        return rid.value
+        return self._track(rid.value, params)
 
     def submit_checkpoint(self, params, path, keep_state=False):
         """A request that starts from a checkpoint file, read by the worker at admission."""
@@ -272,7 +289,7 @@ class Server:
         _check(_lib.gpu().cbns_server_submit_checkpoint(self._s, ctypes.byref(params), params.IM, params.JM,
                                                         params.KM, os.fsencode(path), int(keep_state),
                                                         ctypes.byref(rid)), "cbns_server_submit_checkpoint")
-        return rid.value
+        return self._track(rid.value, params)
 
     def cancel(self, rid):
         _check(_lib.gpu().cbns_server_cancel(self._s, int(rid)), "cbns_server_cancel")
@@ -285,8 +302,15 @@ class Server:
         out["status"] = st
         return out
 
-    def result(self, rid, shape):
-        Q = np.empty(shape)
+    def result(self, rid, shape=None):
+        """The kept final state of a request (padded, get_idx_Q layout).  The buffer
+        is sized from the request's own extents; a given shape must match them."""
+        own = self._shapes.get(int(rid))
+        if own is None:
+            raise ValueError("unknown request %d" % int(rid))
+        if shape is not None and tuple(shape) != own:
+            raise ValueError("request %d has shape %s, not %s" % (int(rid), own, tuple(shape)))
+        Q = np.empty(own)
         _check(_lib.gpu().cbns_server_result(self._s, int(rid), _ptr(Q)), "cbns_server_result")
         return Q
 
@@ -344,6 +368,8 @@ def initial_condition_perturbed(params, seed, amp=1e-3, nmodes=16, kmax=4):
 
 def output_bin(fname, t_cur, Q, IM, JM, KM):
     Q = np.ascontiguousarray(Q, dtype=np.float64)
+    if Q.size != NEQ * (IM + 2 * NG) * (JM + 2 * NG) * (KM + 2 * NG):
+        raise ValueError("Q has %d values, not one padded %dx%dx%d state" % (Q.size, IM, JM, KM))
     _check(_lib.host().cbns_host_output_bin(str(fname).encode(), float(t_cur), IM, JM, KM, _ptr(Q)),
            "cbns_host_output_bin")
 
