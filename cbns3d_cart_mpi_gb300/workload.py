@@ -52,3 +52,19 @@ def state_bytes_per_step(IM, JM, KM):
     """Minimum HBM traffic of one step: read Q, write Q_p (stage 1); read Q, Q_p,
     write one (stages 2, 3) -> 320 B per cell (binary64, 5 fields)."""
     return 320 * IM * JM * KM
+
+
+# Compulsory HBM bytes per interior cell of the FP32-mixed update kernel, by stage:
+# reads Q (5 binary64: 40 B), Q_p (40 B, stages 2-3 only), the 15 binary32 face fluxes
+# (60 B; the neighbours' are their own cells'), the 9 binary32 viscous terms on the
+# NGV ring (36 B x 1.047 ring/interior at 256^3); writes the binary64 state (40 B), the
+# binary32 perturbation state (20 B) and 8 binary32 primitives (32 B), plus the periodic
+# ghost images of those writes (9.7% of the cells at 256^3, 9 B).  ncu measured 245 B per
+# cell on average over a stage-2 launch at 160^3.
+MIXED_UPDATE_BYTES_PER_CELL = {1: 239, 2: 279, 3: 279}
+
+
+def mixed_update_bytes(IM, JM, KM):
+    """Average compulsory bytes of one FP32-mixed update launch over the three stages."""
+    return sum(MIXED_UPDATE_BYTES_PER_CELL.values()) / 3.0 * IM * JM * KM
+
