@@ -85,3 +85,29 @@ def test_mixed_prims_download_is_binary64_of_Q():
     gp, op = s.download_prims(), o.get_prims()
     for k in ("rho", "u", "v", "w", "p", "T"):
         np.testing.assert_allclose(gp[k], op[k], rtol=1e-15, atol=1e-15, err_msg=k)
+
+
+@pytest.mark.parametrize("Re,Mach,seed", [(400.0, 0.3, 21), (3200.0, 0.05, 22)])
+def test_mixed_parameter_corners_within_1e5_of_oracle(Re, Mach, seed):
+    """Corners of the ensemble/serving parameter range (Ma 0.05 has the largest
+    mean pressure relative to the fluctuations, the hardest case for the
+    perturbation form): 40 steps of perturbed data against the binary64 oracle,
+    per field over its scale (the momentum fields share one)."""
+    from oracle.oracle import OracleBlock
+    from cbns3d_cart_mpi_gb300.solver import Solver, initial_condition_perturbed
+    p = tgv_params(24, JM=20, KM=16, Re=Re, Mach=Mach)
+    Q0 = initial_condition_perturbed(p, seed=seed, amp=1e-3, nmodes=16, kmax=4)
+    s = Solver(p, precision="fp32_mixed")
+    s.upload_Q(Q0, 0.0)
+    o = OracleBlock(p)
+    o.set_Q(Q0, 0.0)
+    for _ in range(40):
+        s.step()
+        o.step()
+    a = s.download_Q()[NG:-NG, NG:-NG, NG:-NG].reshape(-1, 5)
+    b = o.get_Q()[NG:-NG, NG:-NG, NG:-NG].reshape(-1, 5)
+    scale = np.abs(b).max(axis=0)
+    scale[1:4] = scale[1:4].max()
+    err = np.abs(a - b).max(axis=0) / scale
+    print("FP32-mixed Re %g Ma %g, 40 steps: error over field scale" % (Re, Mach), err)
+    assert (err <= 1e-5).all(), err

@@ -235,3 +235,25 @@ def test_diagnostics_match_oracle():
     ke, en = s.diagnostics()
     ko, eo = o.diagnostics()
     assert abs(ke - ko) <= 1e-13 * ko and abs(en - eo) <= 1e-13 * eo
+
+
+@pytest.mark.parametrize("Re,Mach,shape,seed", [(400.0, 0.3, (24, 20, 16), 11), (3200.0, 0.05, (20, 28, 12), 12),
+                                                (900.0, 0.15, (33, 17, 9), 13)])
+def test_parameter_corners_vs_oracle(Re, Mach, shape, seed):
+    """The ensemble and serving workloads draw Re in [400, 3200] and Ma in
+    [0.05, 0.3] with perturbed initial data: corners of that range on odd block
+    shapes, 20 steps against the oracle at the parity bar."""
+    from oracle.oracle import OracleBlock
+    from cbns3d_cart_mpi_gb300.solver import Solver, initial_condition_perturbed
+    IM, JM, KM = shape
+    p = tgv_params(IM, JM=JM, KM=KM, Re=Re, Mach=Mach)
+    Q0 = initial_condition_perturbed(p, seed=seed, amp=1e-3, nmodes=16, kmax=4)
+    s = Solver(p)
+    s.upload_Q(Q0, 0.0)
+    o = OracleBlock(p)
+    o.set_Q(Q0, 0.0)
+    for n in range(20):
+        dt, t = s.step()
+        dto, to = o.step()
+        assert abs(dt - dto) <= 1e-13 * dto, n
+    assert_close(interior(s.download_Q()), interior(o.get_Q()), 1e-11, "Re %g Ma %g" % (Re, Mach), tight=1e-13)
