@@ -25,9 +25,10 @@
 #include "../../../include/cbns_host.h"
 
 // Output staging: the primitives of the current state are downloaded once
-// (cbns_download_prims), then the ASCII VTK writer — the slow part at large
-// grids — runs on a host thread while the GPU keeps stepping.  One writer at a
-// time; the next output waits for the previous one before reusing the buffers.
+// (cbns_download_prims), then the ASCII VTK writer (1.3 GB of text at 256^3,
+// formatted on every host core) runs on a host thread while the GPU keeps
+// stepping.  One writer at a time; the next output waits for the previous one
+// before reusing the buffers.
 class OutputStager {
  public:
   explicit OutputStager(const cbns_params& sp) : sp_(sp) {

@@ -2,13 +2,20 @@
 #include "../../../include/cbns_host.h"
 #include "../cbns_modes.h"
 
+#include <algorithm>
 #include <cmath>
+#include <condition_variable>
 #include <cstdint>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <fstream>
+#include <mutex>
+#include <new>
 #include <sstream>
 #include <string>
+#include <system_error>
+#include <thread>
 #include <vector>
 
 namespace {
@@ -19,6 +26,192 @@ constexpr double PI = 3.14159265358979323846;  // include/constants.h:19
 
 inline size_t pidx(uint32_t IM_G, uint32_t JM_G, long i, long j, long k) {
   return (size_t)(NG + i) + (size_t)IM_G * ((size_t)(NG + j) + (size_t)JM_G * (size_t)(NG + k));
+}
+
+// ---------------------------------------------------------------------------
+// VTK text.  The reference prints every value with printf("%e ", x)
+// (src/Block3d.cpp:420): 7 significant digits, correctly rounded.  At 256^3 a
+// .vtr file holds 84 million of them, ~20 s of snprintf on one core, so the
+// writer formats the numbers itself and spreads them over the host cores.
+
+// 10^k for k in [-300, 300], each correctly rounded (strtod of "1eK").
+struct DecimalPowers {
+  double v[601];
+  DecimalPowers() {
+    char b[16];
+    for (int k = -300; k <= 300; k++) {
+      std::snprintf(b, sizeof b, "1e%d", k);
+      v[k + 300] = std::strtod(b, nullptr);
+    }
+  }
+  double operator()(int k) const { return v[k + 300]; }
+};
+const DecimalPowers& decimal_powers() {
+  static const DecimalPowers t;
+  return t;
+}
+
+// The text of printf("%e ", x) into out (at most 24 bytes); returns its length.
+// y = |x| * 10^(6-e) (e the decimal exponent) carries the 7 digits in its integer
+// part; one correctly rounded power and one product leave y within 2.3e-16
+// relative, 2.3e-9 absolute below 1e7, of the exact value.  So y's rounding to
+// an integer is the exact one whenever its fraction lies farther than 1e-6 from
+// one half; otherwise (a tie or near-tie), and for zero, subnormal, very large
+// or non-finite x, the text comes from snprintf itself.
+inline int put_e(char* out, double x) {
+  const double a = std::fabs(x);
+  if (!(a > 1e-290 && a < 1e290)) return std::snprintf(out, 24, "%e ", x);
+  const DecimalPowers& P = decimal_powers();
+  int e2;
+  std::frexp(a, &e2);  // 2^(e2-1) <= a < 2^e2
+  // floor((e2-1) log10 2) is the decimal exponent of a or one below it
+  int e10 = (int)std::floor((e2 - 1) * 0.30102999566398120);
+  double y = a * P(6 - e10);
+  if (y >= 1e7) {
+    e10++;
+    y = a * P(6 - e10);
+  }
+  const double r = std::floor(y), f = y - r;
+  if (std::fabs(f - 0.5) < 1e-6) return std::snprintf(out, 24, "%e ", x);
+  uint32_t d = (uint32_t)r + (f > 0.5 ? 1u : 0u);
+  if (d == 10000000u) {  // 9.9999995... rounds up to the next decade
+    d = 1000000u;
+    e10++;
+  }
+  if (d < 1000000u || d > 9999999u) return std::snprintf(out, 24, "%e ", x);
+  char* o = out;
+  if (std::signbit(x)) *o++ = '-';
+  o[0] = (char)('0' + d / 1000000u);
+  o[1] = '.';
+  uint32_t m = d % 1000000u;
+  for (int i = 7; i >= 2; i--) {
+    o[i] = (char)('0' + m % 10u);
+    m /= 10u;
+  }
+  o[8] = 'e';
+  o += 9;
+  int ex = e10 < 0 ? -e10 : e10;
+  *o++ = e10 < 0 ? '-' : '+';
+  if (ex >= 100) {
+    *o++ = (char)('0' + ex / 100);
+    ex %= 100;
+  }
+  *o++ = (char)('0' + ex / 10);
+  *o++ = (char)('0' + ex % 10);
+  *o++ = ' ';
+  return (int)(o - out);
+}
+
+constexpr char kLineBreak[] = "\n        ";  // after every fifth value (src/Block3d.cpp:421)
+// A value is at most 15 characters ("-1.234567e+308 "), a line break 9 per five
+// values; put_e's snprintf may be told of 24 bytes, hence the slack.
+constexpr size_t kCharsPerValue = 17;
+constexpr size_t kPutSlack = 32;
+
+// Values c0..c1-1 (i fastest) of one cell-data array in the reference's line
+// layout; c0 is a multiple of 5, so the text starts a line.  Returns the length.
+size_t format_cells(char* out, const double* arr, uint32_t IM, uint32_t JM, uint32_t IM_G, uint32_t JM_G,
+                    uint64_t c0, uint64_t c1) {
+  char* o = out;
+  uint64_t i = c0 % IM, j = (c0 / IM) % JM, k = c0 / ((uint64_t)IM * JM);
+  for (uint64_t c = c0; c < c1; c++) {
+    o += put_e(o, arr[pidx(IM_G, JM_G, (long)i, (long)j, (long)k)]);
+    if (c % 5 == 4) {
+      std::memcpy(o, kLineBreak, sizeof kLineBreak - 1);
+      o += sizeof kLineBreak - 1;
+    }
+    if (++i == IM) {
+      i = 0;
+      if (++j == JM) {
+        j = 0;
+        k++;
+      }
+    }
+  }
+  return (size_t)(o - out);
+}
+
+// Host threads for the text: CBNS_HOST_THREADS if set, else every core.
+unsigned text_threads() {
+  if (const char* e = std::getenv("CBNS_HOST_THREADS")) {
+    long n = std::strtol(e, nullptr, 10);
+    if (n >= 1) return (unsigned)std::min(n, 1024L);
+  }
+  unsigned n = std::thread::hardware_concurrency();
+  return n ? n : 1;
+}
+
+// The <CellData> arrays of a .vtr file.  Worker threads format chunks of
+// kChunkValues values (a multiple of 5) into a ring of kRing buffers; the calling
+// thread writes the chunks in order, so the file is the serial writer's byte for
+// byte.  A worker takes chunk c only once chunk c - kRing has been written.
+bool write_cell_data(FILE* fh, const char* const names[5], const double* const arrs[5], uint32_t IM,
+                     uint32_t JM, uint32_t KM) {
+  constexpr uint64_t kChunkValues = 5 * 3276;
+  const uint32_t IM_G = IM + 2 * NG, JM_G = JM + 2 * NG;
+  const uint64_t n = (uint64_t)IM * JM * KM;
+  const uint64_t per_field = (n + kChunkValues - 1) / kChunkValues, total = 5 * per_field;
+  const unsigned want = (unsigned)std::min<uint64_t>(text_threads(), std::max<uint64_t>(total, 1));
+  const size_t kRing = 2 * (size_t)want + 2;
+  std::vector<std::vector<char>> ring(kRing, std::vector<char>(kChunkValues * kCharsPerValue + kPutSlack));
+  std::vector<size_t> len(kRing, 0);
+  std::vector<char> ready(kRing, 0);
+  std::mutex mu;
+  std::condition_variable cv_take, cv_ready;
+  uint64_t next = 0, written = 0;
+  auto format = [&](uint64_t c) {
+    const uint64_t f = c / per_field, c0 = (c % per_field) * kChunkValues, c1 = std::min(c0 + kChunkValues, n);
+    return format_cells(ring[c % kRing].data(), arrs[f], IM, JM, IM_G, JM_G, c0, c1);
+  };
+  auto worker = [&] {
+    for (;;) {
+      uint64_t c;
+      {
+        std::unique_lock<std::mutex> lk(mu);
+        cv_take.wait(lk, [&] { return next >= total || next < written + kRing; });
+        if (next >= total) return;
+        c = next++;
+      }
+      const size_t l = format(c);
+      {
+        std::lock_guard<std::mutex> lk(mu);
+        len[c % kRing] = l;
+        ready[c % kRing] = 1;
+      }
+      cv_ready.notify_all();
+    }
+  };
+  std::vector<std::thread> pool;
+  try {
+    for (unsigned t = 0; t < want && total > 0; t++) pool.emplace_back(worker);
+  } catch (const std::system_error&) {
+    // fewer threads than asked: the ones started (or, with none, this thread) do the work
+  }
+  bool ok = true;
+  for (int f = 0; f < 5; f++) {
+    ok = std::fprintf(fh, "      <DataArray type=\"Float64\" Name=\"%s\" format=\"ascii\">\n        ", names[f]) > 0 && ok;
+    for (uint64_t q = 0; q < per_field; q++) {
+      const uint64_t c = (uint64_t)f * per_field + q;
+      const size_t s = c % kRing;
+      if (pool.empty()) {
+        len[s] = format(c);
+      } else {
+        std::unique_lock<std::mutex> lk(mu);
+        cv_ready.wait(lk, [&] { return ready[s] != 0; });
+      }
+      ok = std::fwrite(ring[s].data(), 1, len[s], fh) == len[s] && ok;
+      {
+        std::lock_guard<std::mutex> lk(mu);
+        ready[s] = 0;
+        written = c + 1;
+      }
+      cv_take.notify_all();
+    }
+    if (n % 5 != 0) ok = std::fputc('\n', fh) != EOF && ok;
+    ok = std::fprintf(fh, "      </DataArray>\n") > 0 && ok;
+  }
+  for (std::thread& t : pool) t.join();
+  return ok;
 }
 
 // Cell-centred primitive fields of the Taylor-Green vortex
@@ -205,7 +398,6 @@ cbns_status cbns_host_output_vtk_xml(const char* dir, const char* fname, int ran
                                      const double* z, const double* rho, const double* u, const double* v,
                                      const double* w, const double* p) {
   if (!dir || !fname || !x || !y || !z || !rho || !u || !v || !w || !p) return CBNS_ERR_INVALID_ARG;
-  const uint32_t IM_G = IM + 2 * NG, JM_G = JM + 2 * NG;
   char rk[16];
   std::snprintf(rk, sizeof rk, "%03d", rank);
   std::string base = std::string(dir) + "/" + fname;
@@ -217,31 +409,22 @@ cbns_status cbns_host_output_vtk_xml(const char* dir, const char* fname, int ran
   std::fprintf(fh, "  <RectilinearGrid WholeExtent=\"0 %d 0 %d 0 %d\">\n", (int)IM, (int)JM, (int)KM);
   std::fprintf(fh, "    <Piece Extent=\"0 %d 0 %d 0 %d\">\n", (int)IM, (int)JM, (int)KM);
   std::fprintf(fh, "    <CellData>\n");
-  auto cell_data = [&](const char* name, const double* arr) {
-    std::fprintf(fh, "      <DataArray type=\"Float64\" Name=\"%s\" format=\"ascii\">\n", name);
-    std::fprintf(fh, "        ");
-    uint32_t cnt = 0;
-    for (uint32_t k = 0; k < KM; k++)
-      for (uint32_t j = 0; j < JM; j++)
-        for (uint32_t i = 0; i < IM; i++) {
-          std::fprintf(fh, "%e ", arr[pidx(IM_G, JM_G, i, j, k)]);
-          if (4 == cnt++ % 5) std::fprintf(fh, "\n        ");
-        }
-    if (0 != cnt % 5) std::fprintf(fh, "\n");
-    std::fprintf(fh, "      </DataArray>\n");
-  };
-  cell_data("rho", rho);
-  cell_data("u", u);
-  cell_data("v", v);
-  cell_data("w", w);
-  cell_data("p", p);
+  const char* const names[5] = {"rho", "u", "v", "w", "p"};
+  const double* const arrs[5] = {rho, u, v, w, p};
+  bool ok;
+  try {
+    ok = write_cell_data(fh, names, arrs, IM, JM, KM);
+  } catch (const std::bad_alloc&) {
+    ok = false;
+  }
   std::fprintf(fh, "    </CellData>\n");
   std::fprintf(fh, "    <Coordinates>\n");
   auto coord = [&](const char* name, uint32_t n, const double* arr) {
     std::fprintf(fh, "      <DataArray type=\"Float64\" Name=\"%s\" format=\"ascii\">\n", name);
     std::fprintf(fh, "        ");
+    char b[kPutSlack];
     for (uint32_t i = 0; i < n; i++) {
-      std::fprintf(fh, "%e ", arr[i]);
+      std::fwrite(b, 1, (size_t)put_e(b, arr[i]), fh);
       if (4 == i % 5) std::fprintf(fh, "\n        ");
     }
     if (0 != n % 5) std::fprintf(fh, "\n");
@@ -254,7 +437,7 @@ cbns_status cbns_host_output_vtk_xml(const char* dir, const char* fname, int ran
   std::fprintf(fh, "    </Piece>\n");
   std::fprintf(fh, "  </RectilinearGrid>\n");
   std::fprintf(fh, "</VTKFile>\n");
-  bool ok = std::fclose(fh) == 0;
+  ok = (std::fclose(fh) == 0) && ok;
   if (!ok) return CBNS_ERR_IO;
   if (rank == 0) {
     // Block3d::output_vtm (src/Block3d.cpp:471-500).

@@ -159,6 +159,68 @@ def test_vtk_text_matches_reference(golden_dir, tmp_path, which, key):
         assert (tmp_path / f).read_text() == ref, f
 
 
+def _cell_text(values):
+    """The lines of one cell-data array as the reference prints them
+    (src/Block3d.cpp:416-424), built with Python's %e: both are correctly rounded."""
+    out = ["        "]
+    for c, v in enumerate(values):
+        out.append("%e " % v)
+        if c % 5 == 4:
+            out.append("\n        ")
+    if len(values) % 5:
+        out.append("\n")
+    return "".join(out)
+
+
+def _wide_ranging_fields(shape, seed):
+    """Five padded fields whose values test a %e formatter: typical densities,
+    magnitudes from 1e-300 to 1e300, random bit patterns, decimal near-ties and
+    exact binary ties, powers of ten and their neighbours, signed zeros,
+    subnormals and infinities."""
+    rng = np.random.default_rng(seed)
+    n = int(np.prod(shape))
+    rho = 1.0 + 1e-3 * rng.standard_normal(n)
+    u = rng.standard_normal(n) * 10.0 ** rng.integers(-300, 300, n).astype(float)
+    v = rng.integers(0, 2**64, n, dtype=np.uint64).view(np.float64).copy()
+    v[~np.isfinite(v)] = 0.0
+    digits = rng.integers(1_000_000, 10_000_000, n).astype(float)
+    w = (digits + 0.5) * 10.0 ** rng.integers(-290, 290, n).astype(float)
+    for _ in range(3):
+        step = rng.integers(-1, 2, n)
+        w = np.where(step > 0, np.nextafter(w, np.inf), np.where(step < 0, np.nextafter(w, 0.0), w))
+    w[::7] = digits[::7] + 0.5                      # exact binary ties: half to even
+    w[3::7] = (digits[3::7] + 0.5) * 2.0 ** -20
+    pw = 10.0 ** rng.integers(-300, 300, n).astype(float)
+    p = np.where(rng.random(n) < 0.5, np.nextafter(pw, np.inf), np.nextafter(pw, 0.0))
+    p[::11] = 9.9999995 * 10.0 ** rng.integers(-20, 20, p[::11].size).astype(float)
+    special = [0.0, -0.0, 5e-324, -1e-310, 2.2250738585072014e-308, 1e-290, 1.0000001e-290, 9.999999e289,
+               1e290, 1.7976931348623157e308, np.inf, -np.inf, 0.5, 1.0, 9.9999995, 1234567.5, 1234568.5]
+    p[:len(special)] = special
+    return [a.reshape(shape) for a in (rho, u, v, w, p)]
+
+
+@pytest.mark.parametrize("threads", ["1", "3", None])
+def test_vtk_text_of_wide_ranging_values(tmp_path, monkeypatch, threads):
+    """The writer formats the numbers itself, in chunks spread over host threads;
+    over a grid of several chunks per array and values of every kind, the text is
+    printf's "%e " in the reference's line layout, whatever the thread count."""
+    from cbns3d_cart_mpi_gb300.solver import output_vtk_xml
+    if threads is None:
+        monkeypatch.delenv("CBNS_HOST_THREADS", raising=False)
+    else:
+        monkeypatch.setenv("CBNS_HOST_THREADS", threads)
+    IM, JM, KM = 37, 41, 23
+    p = tgv_params(IM, JM=JM, KM=KM)
+    fields = _wide_ranging_fields((KM + 2 * NG, JM + 2 * NG, IM + 2 * NG), seed=3)
+    names = ("rho", "u", "v", "w", "p")
+    output_vtk_xml(str(tmp_path), "output", p, dict(zip(names, fields)))
+    text = (tmp_path / "output000.vtr").read_text()
+    for name, a in zip(names, fields):
+        got = text.split('<DataArray type="Float64" Name="%s" format="ascii">\n' % name)[1]
+        got = got.split("      </DataArray>")[0]
+        assert got == _cell_text(a[NG:-NG, NG:-NG, NG:-NG].ravel()), name
+
+
 def test_initial_condition_matches_reference(golden_dir):
     from cbns3d_cart_mpi_gb300.solver import initial_condition
     for name, dims in (("tgv16.npz", (16, 16, 16)), ("tgv_odd.npz", (12, 16, 20))):
