@@ -23,7 +23,14 @@ GPU_SOURCES = ["cbns_kernels.cu", "cbns_api.cu", "cbns_probe.cu", "cbns_noalloc.
 HOST_SOURCES = ["host/cbns_host.cpp"]
 DRIVER_SOURCE = "host/cbns3d_gb300.cpp"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
+# Host code is compiled without contracting a*b+c into fused multiply-adds
+# (-ffp-contract=off): g++ contracts by default on aarch64 but cannot on x86-64's
+# base ISA, so without it the initial condition and the per-solve constants
+# would differ in the last bit between the two hosts and from the reference.
+# Device code keeps nvcc's contraction.
+HOST_FP = ["-ffp-contract=off"]
+NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", HOST_FP[0],
+              "--expt-relaxed-constexpr"]
 
 GPU_LIB = os.path.join(LIB, "libcbns_gpu.so")
 HOST_LIB = os.path.join(LIB, "libcbns_host.so")
@@ -88,8 +95,8 @@ def build(verbose=False, extra_nvcc=()):
         path = os.path.join(CSRC, src)
         obj = os.path.join(objdir, os.path.basename(src) + ".o")
         if _stale(obj, [path] + hdrs + [__file__]):
-            _atomic(lambda out: ["g++", "-O2", "-std=c++17", "-fPIC", "-Wall", "-pthread", "-c", path, "-o", out],
-                    obj)
+            _atomic(lambda out: ["g++", "-O2", "-std=c++17", "-fPIC", "-Wall", "-pthread"] + HOST_FP +
+                    ["-c", path, "-o", out], obj)
         return obj
 
     with ThreadPoolExecutor(max_workers=max(2, os.cpu_count() or 2)) as ex:

@@ -293,7 +293,7 @@ __device__ __forceinline__ double warp_max(double v) {
 // with one reciprocal square root: z = 1/sqrt(gamma p rho) = 1/(rho c) and
 // c = gamma p z.
 template <typename R>
-__device__ __forceinline__ double dt_speed(const SolveDev& s, long long o) {
+__device__ __forceinline__ R dt_speed(const SolveDev& s, long long o) {
   const PrimSet<R>& P = prims_of<R>(s);
   const R rr = P.rho[o], uu = P.u[o], vv = P.v[o], ww = P.w[o];
   const Consts<R>& C = consts_of<R>(s);
@@ -304,35 +304,42 @@ __device__ __forceinline__ double dt_speed(const SolveDev& s, long long o) {
   const R q2 = fma_(ww, ww, fma_(vv, vv, uu * uu));
   const R q = (sizeof(R) == 4 && !(q2 > (R)0)) ? (R)0 : sqrt_(q2);  // binary32 sqrt_ is q2 * rsqrt(q2)
   const R fv = (C.C_dt_v2 * P.mu[o]) * q * z;
-  return (double)((fabs(uu) + fabs(vv) + fabs(ww)) + fma_(c, C.sum_ih, fv * C.sum_ih2));
+  return (fabs(uu) + fabs(vv) + fabs(ww)) + fma_(c, C.sum_ih, fv * C.sum_ih2);
 }
 
 // Each CTA walks its tiles (grid stride) keeping a running per-thread maximum,
 // and folds it into the solve's control block (one block reduction and one
 // atomicMax) only when the next tile belongs to another solve or the walk ends.
 // Tiles of one solve are contiguous in the table, so a bounded grid issues
-// about one atomic per CTA instead of one per tile.
+// about one atomic per CTA instead of one per tile.  The running maximum stays
+// in the compute type and is widened once per fold (exact and monotonic, so
+// the same maximum); whether the solve has finished is tested once per solve.
 template <typename R>
 __global__ void __launch_bounds__(kMaxThreads) k_dt_reduce(const SolveDev* __restrict__ solves,
                                                            const TileRef* __restrict__ tiles, int ntiles,
                                                            double t_end, int use_t_end, int skip_finished) {
   __shared__ double red[kMaxThreads / 32];
   const int nwarps = (int)(blockDim.x / 32);
-  double run = 0.0;
+  R run = (R)0;
+  int live_solve = -1;
+  bool live = false;
   for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
     TileCell tc = tile_cell(tiles[t], 0);
     const SolveDev& s = solves[tc.s];
-    const SolveCtl* ctl = s.ctl;
-    const double te = use_t_end ? t_end : ctl->t_end;
-    const bool live = !(skip_finished && ctl->t_cur + 1.0e-5 > te);  // uniform over the tile
+    if (tc.s != live_solve) {  // uniform over the CTA
+      const SolveCtl* ctl = s.ctl;
+      const double te = use_t_end ? t_end : ctl->t_end;
+      live = !(skip_finished && ctl->t_cur + 1.0e-5 > te);
+      live_solve = tc.s;
+    }
     if (live && tc.i < s.IM && tc.j < s.JM) {
-      double sum = dt_speed<R>(s, pad_off(s, tc.i, tc.j, tc.k));
+      const R sum = dt_speed<R>(s, pad_off(s, tc.i, tc.j, tc.k));
       if (sum > run) run = sum;  // a NaN is skipped, as the reference's ternary does
     }
     const int tn = t + (int)gridDim.x;
     const bool flush = tn >= ntiles || tiles[tn].solve != tiles[t].solve;  // uniform over the CTA
     if (flush) {
-      double m = warp_max(run);
+      double m = warp_max((double)run);
       if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
       __syncthreads();
       if (threadIdx.x == 0) {
@@ -341,7 +348,7 @@ __global__ void __launch_bounds__(kMaxThreads) k_dt_reduce(const SolveDev* __res
         if (m > 0.0) atomicMax(&s.ctl->smax_bits, (unsigned long long)__double_as_longlong(m));
       }
       __syncthreads();
-      run = 0.0;
+      run = (R)0;
     }
   }
 }
