@@ -98,7 +98,7 @@ ArenaLayout arena_layout(const SolveDev& s, bool mixed, size_t n_int, size_t n_r
     L.oUf = take(NEQ * fV);
     L.oPf = take(9 * fV);
     for (int d = 0; d < 3; ++d) L.oFf[d] = take(sizeof(float) * NEQ * (size_t)s.IV);
-    L.oTvf = take(sizeof(float) * kViscTerms * (size_t)s.RV);
+    L.oTvf = take(sizeof(float4) * 3 * (size_t)s.RV);
   }
   L.oCtl = take(sizeof(SolveCtl));
   L.oDesc = take(sizeof(SolveDev));
@@ -270,7 +270,7 @@ cbns_status cbns_create(const cbns_params* p, uint32_t IM, uint32_t JM, uint32_t
       s.Ff[d] = nullptr;
     }
     s.Tv = (double*)(A + L.oTv);
-    s.Tvf = nullptr;
+    s.Tvg = nullptr;
     s.Uf = nullptr;
     s.pf = PrimSet<float>{};
   } else {
@@ -282,7 +282,7 @@ cbns_status cbns_create(const cbns_params* p, uint32_t IM, uint32_t JM, uint32_t
       s.Ff[d] = (float*)(A + oFf[d]);
       s.F[d] = nullptr;
     }
-    s.Tvf = (float*)(A + L.oTvf);
+    s.Tvg = (float4*)(A + L.oTvf);
     s.Tv = nullptr;
   }
   const cbns_params& P = h->params;

@@ -17,6 +17,8 @@
 
 #include <cstdint>
 
+#include <vector_types.h>
+
 namespace cbns {
 
 constexpr int NEQ = 5;
@@ -111,11 +113,15 @@ struct SolveDev {
   double* Tv;
   // FP32-mixed mode: the stage input as a binary32 perturbation of the reference
   // state (rho - rho_ref, rho*u, rho*v, rho*w, E - E_ref), its primitives, and
-  // binary32 face fluxes and viscous terms
+  // binary32 face fluxes and viscous terms.  The viscous terms are grouped by the
+  // direction d they are differenced along: block d (RV float4 values) holds at
+  // each ring point the terms of the x-, y-, z-momentum and energy equations,
+  // (visc_term(1,d), visc_term(2,d), visc_term(3,d), visc_term(4,d)), so the
+  // update reads a direction's four terms with one 16-byte load per offset.
   float* Uf;
   PrimSet<float> pf;
   float* Ff[3];
-  float* Tvf;
+  float4* Tvg;
   // reference state of the perturbation form (u_ref = 0, E_ref = p_ref/(gamma-1))
   double rho_ref, p_ref, E_ref, T_ref;
   // parameters (src/read_input.cpp:78-90)

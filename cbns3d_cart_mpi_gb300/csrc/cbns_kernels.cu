@@ -726,22 +726,28 @@ __global__ void __maxnreg__(sizeof(R) == 4 ? 40 : 64) k_viscous(const SolveDev* 
     const R uu = P.u[o], vv = P.v[o], ww = P.w[o];
     const long long r = ring_off(s, tc.i, tc.j, tc.k);
     const long long RV = s.RV;
-    R* tv;
-    if constexpr (MIXED) {
-      tv = s.Tvf + r;
-    } else {
-      tv = s.Tv + r;
-    }
     // Ev, Fv, Gv (src/Block3d.cpp:812-868) share their stresses: nine terms.
-    tv[TXX * RV] = txx;
-    tv[TYY * RV] = tyy;
-    tv[TZZ * RV] = tzz;
-    tv[TXY * RV] = txy;
-    tv[TXZ * RV] = txz;
-    tv[TYZ * RV] = tyz;
-    tv[EX * RV] = uu * txx + vv * txy + ww * txz - mk * Tx;
-    tv[EY * RV] = uu * txy + vv * tyy + ww * tyz - mk * Ty;
-    tv[EZ * RV] = uu * txz + vv * tyz + ww * tzz - mk * Tz;
+    const R ex = uu * txx + vv * txy + ww * txz - mk * Tx;
+    const R ey = uu * txy + vv * tyy + ww * tyz - mk * Ty;
+    const R ez = uu * txz + vv * tyz + ww * tzz - mk * Tz;
+    if constexpr (MIXED) {
+      // grouped by differencing direction: Ev, Fv, Gv as one float4 each
+      float4* g = s.Tvg + r;
+      g[0] = make_float4(txx, txy, txz, ex);
+      g[RV] = make_float4(txy, tyy, tyz, ey);
+      g[2 * RV] = make_float4(txz, tyz, tzz, ez);
+    } else {
+      double* tv = s.Tv + r;
+      tv[TXX * RV] = txx;
+      tv[TYY * RV] = tyy;
+      tv[TZZ * RV] = tzz;
+      tv[TXY * RV] = txy;
+      tv[TXZ * RV] = txz;
+      tv[TYZ * RV] = tyz;
+      tv[EX * RV] = ex;
+      tv[EY * RV] = ey;
+      tv[EZ * RV] = ez;
+    }
   }
 }
 
@@ -777,13 +783,10 @@ __device__ __forceinline__ void update_tiles(const SolveDev* __restrict__ solves
     const R* F0;
     const R* F1;
     const R* F2;
-    const R* TV;
     if constexpr (MIXED) {
       F0 = s.Ff[0], F1 = s.Ff[1], F2 = s.Ff[2];
-      TV = s.Tvf;
     } else {
       F0 = s.F[0], F1 = s.F[1], F2 = s.F[2];
-      TV = s.Tv;
     }
     // The face fluxes are stored doubled: hf = 0.5 / h.
     const R idx = consts_of<R>(s).hfx, idy = consts_of<R>(s).hfy, idz = consts_of<R>(s).hfz;
@@ -792,26 +795,51 @@ __device__ __forceinline__ void update_tiles(const SolveDev* __restrict__ solves
     // FP32-mixed stages 2 and 3: the binary32 weight of dt df (1/4 or 2/3 of dt,
     // formed once per step with dt).
     const float cdt = MIXED && stage != 1 ? ctl->cdt[stage - 2] : 0.0f;
+    // FP32-mixed: minus the 4th-order central divergence of the viscous fluxes
+    // (src/Block3d.cpp:887-910, calc_viscous_flux_contribution:
+    // ((f[-2]-f[+2])/12 + (f[+1]-f[-1])*2/3) / h per direction) of equations
+    // 1..4, one direction at a time from its grouped terms: four 16-byte loads
+    // per direction.
+    float dv[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    if constexpr (MIXED) {
+      auto direction = [&](const float4* __restrict__ g, long long st, float c12, float c23) {
+        const float4 m2 = g[-2 * st], p2 = g[2 * st], m1 = g[-st], p1 = g[st];
+        dv[0] = fmaf(p1.x - m1.x, -c23, fmaf(m2.x - p2.x, -c12, dv[0]));
+        dv[1] = fmaf(p1.y - m1.y, -c23, fmaf(m2.y - p2.y, -c12, dv[1]));
+        dv[2] = fmaf(p1.z - m1.z, -c23, fmaf(m2.z - p2.z, -c12, dv[2]));
+        dv[3] = fmaf(p1.w - m1.w, -c23, fmaf(m2.w - p2.w, -c12, dv[3]));
+      };
+      const float4* G = s.Tvg + r;
+      direction(G, 1, CS.c12x, CS.c23x);
+      direction(G + RV, ry, CS.c12y, CS.c23y);
+      direction(G + 2 * RV, rz, CS.c12z, CS.c23z);
+    }
     double qn[NEQ];
 #pragma unroll
     for (int n = 0; n < NEQ; ++n) {
-      // Inviscid flux differences, then minus the 4th-order central divergence
-      // of the viscous fluxes (src/Block3d.cpp:887-910, calc_viscous_flux_contribution:
-      // ((f[-2]-f[+2])/12 + (f[+1]-f[-1])*2/3) / h per direction), as one chain
-      // of fused multiply-adds with the 1/h-folded weights negated.
-      R df = (F0[n * IV + fx] - F0[n * IV + fo]) * idx;
-      df = fma_(F1[n * IV + fy] - F1[n * IV + fo], idy, df);
-      df = fma_(F2[n * IV + fz] - F2[n * IV + fo], idz, df);
-      if (n > 0) {
-        const R* vx = TV + visc_term(n, 0) * RV;
-        const R* vy = TV + visc_term(n, 1) * RV;
-        const R* vz = TV + visc_term(n, 2) * RV;
-        df = fma_(vx[r - 2] - vx[r + 2], -CS.c12x, df);
-        df = fma_(vx[r + 1] - vx[r - 1], -CS.c23x, df);
-        df = fma_(vy[r - 2 * ry] - vy[r + 2 * ry], -CS.c12y, df);
-        df = fma_(vy[r + ry] - vy[r - ry], -CS.c23y, df);
-        df = fma_(vz[r - 2 * rz] - vz[r + 2 * rz], -CS.c12z, df);
-        df = fma_(vz[r + rz] - vz[r - rz], -CS.c23z, df);
+      R df;
+      if constexpr (MIXED) {
+        // the viscous part above, then the inviscid flux differences
+        df = fma_(F0[n * IV + fx] - F0[n * IV + fo], idx, n > 0 ? dv[n - 1] : 0.0f);
+        df = fma_(F1[n * IV + fy] - F1[n * IV + fo], idy, df);
+        df = fma_(F2[n * IV + fz] - F2[n * IV + fo], idz, df);
+      } else {
+        // Inviscid flux differences, then minus the viscous divergence, as one
+        // chain of fused multiply-adds with the 1/h-folded weights negated.
+        df = (F0[n * IV + fx] - F0[n * IV + fo]) * idx;
+        df = fma_(F1[n * IV + fy] - F1[n * IV + fo], idy, df);
+        df = fma_(F2[n * IV + fz] - F2[n * IV + fo], idz, df);
+        if (n > 0) {
+          const double* vx = s.Tv + visc_term(n, 0) * RV;
+          const double* vy = s.Tv + visc_term(n, 1) * RV;
+          const double* vz = s.Tv + visc_term(n, 2) * RV;
+          df = fma_(vx[r - 2] - vx[r + 2], -CS.c12x, df);
+          df = fma_(vx[r + 1] - vx[r - 1], -CS.c23x, df);
+          df = fma_(vy[r - 2 * ry] - vy[r + 2 * ry], -CS.c12y, df);
+          df = fma_(vy[r + ry] - vy[r - ry], -CS.c23y, df);
+          df = fma_(vz[r - 2 * rz] - vz[r + 2 * rz], -CS.c12z, df);
+          df = fma_(vz[r + rz] - vz[r - rz], -CS.c23z, df);
+        }
       }
       const double q0 = s.Q[n * V + o];
       if (MIXED && stage != 1) {

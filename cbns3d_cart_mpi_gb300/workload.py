@@ -56,12 +56,12 @@ def state_bytes_per_step(IM, JM, KM):
 
 # Compulsory HBM bytes per interior cell of the FP32-mixed update kernel, by stage:
 # reads Q (5 binary64: 40 B), Q_p (40 B, stages 2-3 only), the 15 binary32 face fluxes
-# (60 B; the neighbours' are their own cells'), the 9 binary32 viscous terms on the
-# NGV ring (36 B x 1.047 ring/interior at 256^3); writes the binary64 state (40 B), the
-# binary32 perturbation state (20 B) and 8 binary32 primitives (32 B), plus the periodic
-# ghost images of those writes (9.7% of the cells at 256^3, 9 B).  ncu measured 245 B per
-# cell on average over a stage-2 launch at 160^3.
-MIXED_UPDATE_BYTES_PER_CELL = {1: 239, 2: 279, 3: 279}
+# (60 B; the neighbours' are their own cells'), the viscous terms on the NGV ring,
+# grouped by differencing direction as 3 x 4 binary32 (48 B x 1.047 ring/interior at
+# 256^3); writes the binary64 state (40 B), the binary32 perturbation state (20 B) and
+# 8 binary32 primitives (32 B), plus the periodic ghost images of those writes (9.7% of
+# the cells at 256^3, 9 B).
+MIXED_UPDATE_BYTES_PER_CELL = {1: 251, 2: 291, 3: 291}
 
 
 def mixed_update_bytes(IM, JM, KM):
