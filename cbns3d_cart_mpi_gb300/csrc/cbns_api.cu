@@ -95,8 +95,8 @@ ArenaLayout arena_layout(const SolveDev& s, bool mixed, size_t n_int, size_t n_r
     for (int d = 0; d < 3; ++d) L.oF[d] = take(sizeof(double) * NEQ * (size_t)s.IV);
     L.oTv = take(sizeof(double) * kViscTerms * (size_t)s.RV);
   } else {
-    L.oUf = take(NEQ * fV);
-    L.oPf = take(9 * fV);
+    L.oUf = take(NEQ * fV);  // U4 (4 values per cell), then UE
+    L.oPf = take(9 * fV);    // PA and PB (4 values per cell each), then mu
     for (int d = 0; d < 3; ++d) L.oFf[d] = take(sizeof(float) * NEQ * (size_t)s.IV);
     L.oTvf = take(sizeof(float4) * 3 * (size_t)s.RV);
   }
@@ -271,13 +271,16 @@ cbns_status cbns_create(const cbns_params* p, uint32_t IM, uint32_t JM, uint32_t
     }
     s.Tv = (double*)(A + L.oTv);
     s.Tvg = nullptr;
-    s.Uf = nullptr;
-    s.pf = PrimSet<float>{};
+    s.U4 = nullptr;
+    s.UE = nullptr;
+    s.PA = s.PB = nullptr;
+    s.muf = nullptr;
   } else {
-    s.Uf = (float*)(A + oUf);
-    float* pfb = (float*)(A + oPf);
-    s.pf = PrimSet<float>{pfb + 0 * s.V, pfb + 1 * s.V, pfb + 2 * s.V, pfb + 3 * s.V, pfb + 4 * s.V,
-                          pfb + 5 * s.V, pfb + 6 * s.V, pfb + 7 * s.V, pfb + 8 * s.V};
+    s.U4 = (float4*)(A + oUf);
+    s.UE = (float*)(s.U4 + s.V);
+    s.PA = (float4*)(A + oPf);
+    s.PB = s.PA + s.V;
+    s.muf = (float*)(s.PB + s.V);
     for (int d = 0; d < 3; ++d) {
       s.Ff[d] = (float*)(A + oFf[d]);
       s.F[d] = nullptr;

@@ -55,13 +55,10 @@ struct SolveCtl {
   float pad2[2];
 };
 
-// Cell-centred primitive fields of a stage input.  Binary64 solves store them
-// absolute; FP32-mixed solves store rho, u, v, w, sqrt(rho), H and mu absolute
-// but p and T as perturbations p - p_ref, T - T_ref (binary32 keeps 24 bits of
-// the O(0.1) fluctuations instead of the O(70) mean pressure).
+// Cell-centred binary64 primitive fields of a stage input, one array each.  The
+// arrays are consecutive blocks of V values of one allocation, in member order
+// (the update kernel's stores address them from the first).
 template <typename R>
-// The arrays are consecutive blocks of V values of one allocation, in member
-// order (the update kernel's stores address them from the first).
 struct PrimSet {
   R* rho;
   R* u;
@@ -118,8 +115,17 @@ struct SolveDev {
   // each ring point the terms of the x-, y-, z-momentum and energy equations,
   // (visc_term(1,d), visc_term(2,d), visc_term(3,d), visc_term(4,d)), so the
   // update reads a direction's four terms with one 16-byte load per offset.
-  float* Uf;
-  PrimSet<float> pf;
+  //
+  // The binary32 state and primitives are packed per cell, so a stencil point
+  // costs one or two 16-byte loads instead of a load per field.  rho, u, v, w,
+  // sqrt(rho), H and mu are absolute; p and T are perturbations p - p_ref and
+  // T - T_ref (binary32 keeps 24 bits of the O(0.1) fluctuations instead of the
+  // O(70) mean pressure).
+  float4* U4;   // (rho - rho_ref, rho*u, rho*v, rho*w), padded
+  float* UE;    // E - E_ref, padded
+  float4* PA;   // (u, v, w, T - T_ref), padded
+  float4* PB;   // (rho, p - p_ref, sqrt(rho), H), padded
+  float* muf;   // Sutherland mu, interior; lagged into calc_dt like the reference
   float* Ff[3];
   float4* Tvg;
   // reference state of the perturbation form (u_ref = 0, E_ref = p_ref/(gamma-1))
@@ -207,17 +213,6 @@ inline void fill_consts(SolveDev& s) {
   f.gamma_gam1_inv = (float)c.gamma_gam1_inv;
   f.pref_over_rref = (float)c.pref_over_rref;
   f.low_rho = (float)c.low_rho;
-}
-
-template <typename R>
-__host__ __device__ inline const PrimSet<R>& prims_of(const SolveDev& s);
-template <>
-__host__ __device__ inline const PrimSet<double>& prims_of<double>(const SolveDev& s) {
-  return s.pd;
-}
-template <>
-__host__ __device__ inline const PrimSet<float>& prims_of<float>(const SolveDev& s) {
-  return s.pf;
 }
 
 struct TileRef {

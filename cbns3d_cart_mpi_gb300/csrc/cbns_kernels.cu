@@ -154,22 +154,13 @@ __device__ __forceinline__ MixedCell mixed_cell(const SolveDev& s, const double 
   return m;
 }
 
-// The primitive arrays are consecutive blocks of V values in PrimSet order, so
-// one base pointer addresses all of them (fewer live registers in the update).
+// The packed binary32 state and primitives of one cell: four 16-byte stores and
+// one 4-byte store.
 __device__ __forceinline__ void store_mixed(const SolveDev& s, long long o, const MixedCell& m) {
-  const long long V = s.V;
-  float* u = s.Uf + o;
-#pragma unroll
-  for (int n = 0; n < NEQ; ++n) u[n * V] = m.U[n];
-  float* b = s.pf.rho + o;
-  b[0] = m.rho;
-  b[V] = m.u;
-  b[2 * V] = m.v;
-  b[3 * V] = m.w;
-  b[4 * V] = m.p;
-  b[5 * V] = m.T;
-  b[6 * V] = m.srho;
-  b[7 * V] = m.H;
+  s.U4[o] = make_float4(m.U[0], m.U[1], m.U[2], m.U[3]);
+  s.UE[o] = m.U[4];
+  s.PA[o] = make_float4(m.u, m.v, m.w, m.T);
+  s.PB[o] = make_float4(m.rho, m.p, m.srho, m.H);
 }
 
 __global__ void k_aos_to_soa(const SolveDev* __restrict__ solves, int sidx, const double* __restrict__ aos,
@@ -216,7 +207,7 @@ __global__ void k_prepare(const SolveDev* __restrict__ solves, const TileRef* __
     const bool interior = tc.i >= 0 && tc.i < s.IM && tc.j >= 0 && tc.j < s.JM && tc.k >= 0 && tc.k < s.KM;
     if (interior) {
       s.pd.mu[o] = 1.0;
-      if (s.mixed) s.pf.mu[o] = 1.0f;
+      if (s.mixed) s.muf[o] = 1.0f;
     }
   }
 }
@@ -294,16 +285,25 @@ __device__ __forceinline__ double warp_max(double v) {
 // c = gamma p z.
 template <typename R>
 __device__ __forceinline__ R dt_speed(const SolveDev& s, long long o) {
-  const PrimSet<R>& P = prims_of<R>(s);
-  const R rr = P.rho[o], uu = P.u[o], vv = P.v[o], ww = P.w[o];
   const Consts<R>& C = consts_of<R>(s);
-  const R pp = (sizeof(R) == 4) ? C.p_ref + P.p[o] : P.p[o];
+  R rr, uu, vv, ww, pp, mu;
+  if constexpr (sizeof(R) == 4) {
+    const float4 a = s.PA[o], b = s.PB[o];
+    rr = b.x, uu = a.x, vv = a.y, ww = a.z;
+    pp = C.p_ref + b.y;
+    mu = s.muf[o];
+  } else {
+    const PrimSet<double>& P = s.pd;
+    rr = P.rho[o], uu = P.u[o], vv = P.v[o], ww = P.w[o];
+    pp = P.p[o];
+    mu = P.mu[o];
+  }
   const R gp = C.gamma * pp;
   const R z = rsqrt(gp * rr);
   const R c = gp * z;
   const R q2 = fma_(ww, ww, fma_(vv, vv, uu * uu));
   const R q = (sizeof(R) == 4 && !(q2 > (R)0)) ? (R)0 : sqrt_(q2);  // binary32 sqrt_ is q2 * rsqrt(q2)
-  const R fv = (C.C_dt_v2 * P.mu[o]) * q * z;
+  const R fv = (C.C_dt_v2 * mu) * q * z;
   return (fabs(uu) + fabs(vv) + fabs(ww)) + fma_(c, C.sum_ih, fv * C.sum_ih2);
 }
 
@@ -522,7 +522,6 @@ __device__ __forceinline__ void face_flux(const SolveDev& s, const R* __restrict
                                           R (&out)[NEQ]) {
   constexpr int T1 = (D + 1) % 3;
   constexpr int T2 = (D + 2) % 3;
-  const PrimSet<R>& P = prims_of<R>(s);
   const long long st = D == 0 ? 1ll : (D == 1 ? (long long)s.nx : (long long)s.nx * s.ny);
   const long long V = s.V;
   const long long cl = c - st;
@@ -531,13 +530,25 @@ __device__ __forceinline__ void face_flux(const SolveDev& s, const R* __restrict
 
   // Roe-averaged state of the two cells either side (src/eigenvectors_roe.cpp:87-106).
   // (sqrt(rho_L) f_L + sqrt(rho_R) f_R) / (sqrt(rho_L) + sqrt(rho_R)) = f_R + wL (f_L - f_R).
-  const R sL = P.srho[cl], sR = P.srho[c];
-  const R wL = div_(sL, sL + sR);
-  R Uv[3];
-  Uv[0] = fma_(wL, P.u[cl] - P.u[c], P.u[c]);
-  Uv[1] = fma_(wL, P.v[cl] - P.v[c], P.v[c]);
-  Uv[2] = fma_(wL, P.w[cl] - P.w[c], P.w[c]);
-  const R HH = fma_(wL, P.H[cl] - P.H[c], P.H[c]);
+  R Uv[3], HH;
+  {
+    // sqrt(rho), u, v, w, H of the cells either side (l: c - st, r: c)
+    R sl, sr, ul, ur, vl, vr, wl, wr, hl, hr;
+    if constexpr (sizeof(R) == 4) {
+      const float4 al = s.PA[cl], ar = s.PA[c], bl = s.PB[cl], br = s.PB[c];
+      sl = bl.z, sr = br.z, hl = bl.w, hr = br.w;
+      ul = al.x, ur = ar.x, vl = al.y, vr = ar.y, wl = al.z, wr = ar.z;
+    } else {
+      const PrimSet<double>& P = s.pd;
+      sl = P.srho[cl], sr = P.srho[c], hl = P.H[cl], hr = P.H[c];
+      ul = P.u[cl], ur = P.u[c], vl = P.v[cl], vr = P.v[c], wl = P.w[cl], wr = P.w[c];
+    }
+    const R wL = div_(sl, sl + sr);
+    Uv[0] = fma_(wL, ul - ur, ur);
+    Uv[1] = fma_(wL, vl - vr, vr);
+    Uv[2] = fma_(wL, wl - wr, wr);
+    HH = fma_(wL, hl - hr, hr);
+  }
   const R q2 = Uv[0] * Uv[0] + Uv[1] * Uv[1] + Uv[2] * Uv[2];
   const R hq2 = (R)0.5 * q2;
   const R c2 = gam1 * (HH - hq2);
@@ -553,7 +564,13 @@ __device__ __forceinline__ void face_flux(const SolveDev& s, const R* __restrict
 #pragma unroll
   for (int m = 0; m < 6; ++m) {
     const long long o = c + (m - 3) * st;
-    const R f0 = U[o], f1 = U[V + o], f2 = U[2 * V + o], f3 = U[3 * V + o], f4 = U[4 * V + o];
+    R f0, f1, f2, f3, f4;
+    if constexpr (sizeof(R) == 4) {
+      const float4 a = s.U4[o];
+      f0 = a.x, f1 = a.y, f2 = a.z, f3 = a.w, f4 = s.UE[o];
+    } else {
+      f0 = U[o], f1 = U[V + o], f2 = U[2 * V + o], f3 = U[3 * V + o], f4 = U[4 * V + o];
+    }
     const R fm[3] = {f1, f2, f3};
     const R t = fma_(-Uv[2], f3, fma_(-Uv[1], f2, fma_(-Uv[0], f1, fma_(hq2, f0, f4))));
     const R A = K * t;
@@ -663,7 +680,7 @@ __global__ void __maxnreg__(sizeof(R) == 4 ? 64 : 128) k_inviscid(const SolveDev
     const R* U;
     R* F;
     if constexpr (MIXED) {
-      U = s.Uf;
+      U = nullptr;  // face_flux reads the packed s.U4, s.UE
       F = s.Ff[D];
     } else {
       U = stage == 1 ? s.Q : s.Qp;
@@ -684,8 +701,12 @@ __global__ void __maxnreg__(sizeof(R) == 4 ? 64 : 128) k_inviscid(const SolveDev
 // FP32-mixed: T is stored as T - T_ref; its derivatives are the same.
 
 template <typename R>
+__device__ __forceinline__ R d4v(R m2, R p2, R m1, R p1, R c12h, R c23h) {
+  return (m2 - p2) * c12h + (p1 - m1) * c23h;
+}
+template <typename R>
 __device__ __forceinline__ R d4(const R* __restrict__ f, long long o, long long st, R c12h, R c23h) {
-  return (f[o - 2 * st] - f[o + 2 * st]) * c12h + (f[o + st] - f[o - st]) * c23h;
+  return d4v<R>(f[o - 2 * st], f[o + 2 * st], f[o - st], f[o + st], c12h, c23h);
 }
 // Register caps: 64 for binary64 (FP64-pipe bound; lower caps measured no
 // faster) and 40 for binary32 (memory bound; 4% faster than at 48, spills at 32).
@@ -698,22 +719,47 @@ __global__ void __maxnreg__(sizeof(R) == 4 ? 40 : 64) k_viscous(const SolveDev* 
     const SolveDev& s = solves[tc.s];
     if (!s.ctl->active) continue;
     if (tc.i >= s.IM + NGV || tc.j >= s.JM + NGV) continue;
-    const PrimSet<R>& P = prims_of<R>(s);
     const long long o = pad_off(s, tc.i, tc.j, tc.k);
     const long long sy = s.nx, sz = (long long)s.nx * s.ny;
     const Consts<R>& CS = consts_of<R>(s);
     const R ax = CS.c12x, bx = CS.c23x, ay = CS.c12y, by = CS.c23y, az = CS.c12z, bz = CS.c23z;
-    const R ux = d4<R>(P.u, o, 1, ax, bx), uy = d4<R>(P.u, o, sy, ay, by), uz = d4<R>(P.u, o, sz, az, bz);
-    const R vx = d4<R>(P.v, o, 1, ax, bx), vy = d4<R>(P.v, o, sy, ay, by), vz = d4<R>(P.v, o, sz, az, bz);
-    const R wx = d4<R>(P.w, o, 1, ax, bx), wy = d4<R>(P.w, o, sy, ay, by), wz = d4<R>(P.w, o, sz, az, bz);
-    const R Tx = d4<R>(P.T, o, 1, ax, bx), Ty = d4<R>(P.T, o, sy, ay, by), Tz = d4<R>(P.T, o, sz, az, bz);
-    const R Tl = MIXED ? CS.T_ref + P.T[o] : P.T[o];
+    R ux, uy, uz, vx, vy, vz, wx, wy, wz, Tx, Ty, Tz, Tl, uu, vv, ww;
+    if constexpr (MIXED) {
+      // (u, v, w, T - T_ref) packed: four 16-byte loads per direction
+      auto grad = [&](long long st, float c12h, float c23h, float& gu, float& gv, float& gw, float& gT) {
+        const float4 m2 = s.PA[o - 2 * st], p2 = s.PA[o + 2 * st], m1 = s.PA[o - st], p1 = s.PA[o + st];
+        gu = d4v(m2.x, p2.x, m1.x, p1.x, c12h, c23h);
+        gv = d4v(m2.y, p2.y, m1.y, p1.y, c12h, c23h);
+        gw = d4v(m2.z, p2.z, m1.z, p1.z, c12h, c23h);
+        gT = d4v(m2.w, p2.w, m1.w, p1.w, c12h, c23h);
+      };
+      grad(1, ax, bx, ux, vx, wx, Tx);
+      grad(sy, ay, by, uy, vy, wy, Ty);
+      grad(sz, az, bz, uz, vz, wz, Tz);
+      const float4 a = s.PA[o];
+      uu = a.x, vv = a.y, ww = a.z;
+      Tl = CS.T_ref + a.w;
+    } else {
+      const PrimSet<double>& P = s.pd;
+      ux = d4<R>(P.u, o, 1, ax, bx), uy = d4<R>(P.u, o, sy, ay, by), uz = d4<R>(P.u, o, sz, az, bz);
+      vx = d4<R>(P.v, o, 1, ax, bx), vy = d4<R>(P.v, o, sy, ay, by), vz = d4<R>(P.v, o, sz, az, bz);
+      wx = d4<R>(P.w, o, 1, ax, bx), wy = d4<R>(P.w, o, sy, ay, by), wz = d4<R>(P.w, o, sz, az, bz);
+      Tx = d4<R>(P.T, o, 1, ax, bx), Ty = d4<R>(P.T, o, sy, ay, by), Tz = d4<R>(P.T, o, sz, az, bz);
+      uu = P.u[o], vv = P.v[o], ww = P.w[o];
+      Tl = P.T[o];
+    }
     const R C = CS.C_T_inf;
     // Sutherland's law, (1 + C) / (T + C) * T^1.5 (src/Block3d.cpp:777), as
     // (1 + C) T^2 / sqrt(T (T + C)^2): one reciprocal square root, no division.
     const R TC = Tl + C;
     const R mu = (((R)1 + C) * (Tl * Tl)) * rsqrt(Tl * (TC * TC));
-    if (tc.i >= 0 && tc.i < s.IM && tc.j >= 0 && tc.j < s.JM && tc.k >= 0 && tc.k < s.KM) P.mu[o] = mu;
+    if (tc.i >= 0 && tc.i < s.IM && tc.j >= 0 && tc.j < s.JM && tc.k >= 0 && tc.k < s.KM) {
+      if constexpr (MIXED) {
+        s.muf[o] = mu;
+      } else {
+        s.pd.mu[o] = mu;
+      }
+    }
     const R mr = mu * CS.Re_inv;
     const R m23 = (R)(2.0 / 3.0) * mr;
     const R txx = m23 * ((R)2 * ux - vy - wz);
@@ -723,7 +769,6 @@ __global__ void __maxnreg__(sizeof(R) == 4 ? 40 : 64) k_viscous(const SolveDev* 
     const R txz = mr * (uz + wx);
     const R tyz = mr * (vz + wy);
     const R mk = mr * CS.kappa;
-    const R uu = P.u[o], vv = P.v[o], ww = P.w[o];
     const long long r = ring_off(s, tc.i, tc.j, tc.k);
     const long long RV = s.RV;
     // Ev, Fv, Gv (src/Block3d.cpp:812-868) share their stresses: nine terms.
