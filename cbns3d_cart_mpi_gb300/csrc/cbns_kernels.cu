@@ -665,6 +665,209 @@ __device__ __forceinline__ void face_flux(const SolveDev& s, const R* __restrict
   }
 }
 
+// ---------------------------------------------------------------------------
+// FP32-mixed faces two at a time.  The binary32 face kernel is bound by
+// instruction issue, and every operation of a face is the same for all faces, so
+// a thread computes the faces of two rows (j, j+1) in the two lanes of
+// Blackwell's packed binary32 instructions (fma/add/mul .f32x2), which do two
+// faces' arithmetic per issued instruction.  Loads, the reciprocal and
+// reciprocal square roots (MUFU), abs/max and the stores stay per face.  Each
+// lane performs face_flux<D, float, true>'s operations; subtractions are
+// fma(b, -1, a) (the same rounding as a - b), and the terms whose sign the
+// scalar code took for free are formed with the opposite sign where that leaves
+// the result unchanged (a squared e_k; the right-biased numerator negated
+// together with its denominator; alpha times (L - R) instead of -alpha times
+// (R - L)).
+
+struct f2 {
+  float2 v;
+};
+__device__ __forceinline__ f2 bc(float a) { return {make_float2(a, a)}; }
+__device__ __forceinline__ f2 lanes(float a, float b) { return {make_float2(a, b)}; }
+__device__ __forceinline__ f2 add2(f2 a, f2 b) { return {__fadd2_rn(a.v, b.v)}; }
+__device__ __forceinline__ f2 sub2(f2 a, f2 b) { return {__ffma2_rn(b.v, make_float2(-1.0f, -1.0f), a.v)}; }
+__device__ __forceinline__ f2 mul2(f2 a, f2 b) { return {__fmul2_rn(a.v, b.v)}; }
+__device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) { return {__ffma2_rn(a.v, b.v, c.v)}; }
+__device__ __forceinline__ f2 rcp2(f2 a) { return {make_float2(__fdividef(1.0f, a.v.x), __fdividef(1.0f, a.v.y))}; }
+__device__ __forceinline__ f2 rsqrt2(f2 a) { return {make_float2(rsqrtf(a.v.x), rsqrtf(a.v.y))}; }
+
+// One biased stencil (weno5_side); num is returned with the sign sg of its g's.
+__device__ __forceinline__ void weno5_side_x2(f2 D1, f2 C1, f2 D2, f2 C2, f2 D3, f2 C3, f2 e1, f2 e2, f2 e3,
+                                              f2 g1, f2 g2s, f2 g3s, f2& num, f2& den) {
+  const f2 eps4 = bc(4.0e-6f);
+  const f2 is1 = fma2(C1, D1, fma2(e1, e1, eps4));
+  const f2 is2 = fma2(C2, D2, fma2(e2, e2, eps4));
+  const f2 is3 = fma2(C3, D3, fma2(e3, e3, eps4));
+  const f2 a1 = mul2(is1, is1), a2 = mul2(is2, is2), a3 = mul2(is3, is3);
+  const f2 p1 = mul2(a2, a3), q2 = mul2(a1, a3), q3 = mul2(a1, a2);
+  den = fma2(bc(6.0f), q2, fma2(bc(3.0f), q3, p1));
+  num = fma2(q2, g2s, fma2(q3, g3s, mul2(p1, g1)));
+}
+
+// weno5_pair on two faces: the left-biased result v2 + numL/denL and the
+// right-biased v3 - numRn/denR (numRn the negated numerator).
+__device__ __forceinline__ void weno5_pair_x2(const f2 (&v)[6], f2& numL, f2& denL, f2& numRn, f2& denR) {
+  const f2 d0 = sub2(v[1], v[0]), d1 = sub2(v[2], v[1]), d2 = sub2(v[3], v[2]), d3 = sub2(v[4], v[3]),
+           d4 = sub2(v[5], v[4]);
+  const f2 D1 = sub2(d1, d0), D2 = sub2(d2, d1), D3 = sub2(d3, d2), D4 = sub2(d4, d3);
+  const f2 c13 = bc((float)(13.0 / 3.0));
+  const f2 C1 = mul2(c13, D1), C2 = mul2(c13, D2), C3 = mul2(c13, D3), C4 = mul2(c13, D4);
+  const f2 k56 = bc((float)(5.0 / 6.0)), mk13 = bc((float)(-1.0 / 3.0));
+  const f2 m3 = bc(-3.0f), two = bc(2.0f), mhalf = bc(-0.5f);
+  // left: e = d0 - 3 d1 (sign immaterial), d1 + d2, d3 - 3 d2;
+  //       g1 = 5/6 d1 - 1/3 d0, g2s = 2 d2 + d1, g3s = 2 d2 - 0.5 d3
+  weno5_side_x2(D1, C1, D2, C2, D3, C3, fma2(m3, d1, d0), add2(d1, d2), fma2(m3, d2, d3),
+                fma2(k56, d1, mul2(mk13, d0)), fma2(two, d2, d1), fma2(two, d2, mul2(mhalf, d3)), numL, denL);
+  // right, numerator negated: e = d4 - 3 d3, d2 + d3, d1 - 3 d2 (sign immaterial);
+  //       -g1 = 5/6 d3 - 1/3 d4, -g2s = 2 d2 + d3, -g3s = 2 d2 - 0.5 d1
+  weno5_side_x2(D4, C4, D3, C3, D2, C2, fma2(m3, d3, d4), add2(d2, d3), fma2(m3, d2, d1),
+                fma2(k56, d3, mul2(mk13, d4)), fma2(two, d2, d3), fma2(two, d2, mul2(mhalf, d1)), numRn, denR);
+}
+
+template <int D>
+__device__ __forceinline__ void face_flux_x2(const SolveDev& s, long long c0, long long c1, f2 (&out)[NEQ]) {
+  constexpr int T1 = (D + 1) % 3;
+  constexpr int T2 = (D + 2) % 3;
+  const long long st = D == 0 ? 1ll : (D == 1 ? (long long)s.nx : (long long)s.nx * s.ny);
+  const Consts<float>& C = s.cf;
+  const f2 gam1 = bc(C.gam1), half = bc(0.5f), mone = bc(-1.0f);
+
+  // Roe average of the cells either side of each face
+  f2 Uv[3], HH;
+  {
+    const float4 al0 = s.PA[c0 - st], ar0 = s.PA[c0], bl0 = s.PB[c0 - st], br0 = s.PB[c0];
+    const float4 al1 = s.PA[c1 - st], ar1 = s.PA[c1], bl1 = s.PB[c1 - st], br1 = s.PB[c1];
+    const f2 sl = lanes(bl0.z, bl1.z), sr = lanes(br0.z, br1.z);
+    const f2 ssum = add2(sl, sr);
+    const f2 wL = lanes(__fdividef(sl.v.x, ssum.v.x), __fdividef(sl.v.y, ssum.v.y));
+    const f2 ur = lanes(ar0.x, ar1.x), vr = lanes(ar0.y, ar1.y), wr = lanes(ar0.z, ar1.z), hr = lanes(br0.w, br1.w);
+    Uv[0] = fma2(wL, sub2(lanes(al0.x, al1.x), ur), ur);
+    Uv[1] = fma2(wL, sub2(lanes(al0.y, al1.y), vr), vr);
+    Uv[2] = fma2(wL, sub2(lanes(al0.z, al1.z), wr), wr);
+    HH = fma2(wL, sub2(lanes(bl0.w, bl1.w), hr), hr);
+  }
+  const f2 q2 = fma2(Uv[2], Uv[2], fma2(Uv[1], Uv[1], mul2(Uv[0], Uv[0])));
+  const f2 hq2 = mul2(half, q2);
+  const f2 c2 = mul2(gam1, sub2(HH, hq2));
+  const f2 ic = rsqrt2(c2);
+  const f2 cc = mul2(c2, ic);
+  const f2 K = mul2(mul2(bc(0.5f * C.gam1), ic), ic);
+  const f2 hic = mul2(half, ic), nhic = mul2(bc(-0.5f), ic);
+  const f2 un = Uv[D], u1 = Uv[T1], u2 = Uv[T2];
+  const f2 nU0 = mul2(mone, Uv[0]), nU1 = mul2(mone, Uv[1]), nU2 = mul2(mone, Uv[2]);
+  const f2 nun = mul2(mone, un), nu1 = mul2(mone, u1), nu2 = mul2(mone, u2);
+
+  // characteristic projections of the six cells c-3 .. c+2 of each face
+  f2 w[NEQ][6];
+#pragma unroll
+  for (int m = 0; m < 6; ++m) {
+    const long long o0 = c0 + (m - 3) * st, o1 = c1 + (m - 3) * st;
+    const float4 a0 = s.U4[o0], a1 = s.U4[o1];
+    const f2 f0 = lanes(a0.x, a1.x), f1 = lanes(a0.y, a1.y), f2v = lanes(a0.z, a1.z), f3 = lanes(a0.w, a1.w);
+    const f2 f4 = lanes(s.UE[o0], s.UE[o1]);
+    const f2 fm[3] = {f1, f2v, f3};
+    const f2 t = fma2(nU2, f3, fma2(nU1, f2v, fma2(nU0, f1, fma2(hq2, f0, f4))));
+    const f2 A = mul2(K, t);
+    const f2 gn = fma2(nun, f0, fm[D]);  // -g = f_D - U_D f0
+    w[0][m] = fma2(nhic, gn, A);
+    w[1][m] = fma2(bc(-2.0f), A, f0);
+    w[2][m] = fma2(hic, gn, A);
+    w[3][m] = fma2(nu1, f0, fm[T1]);
+    w[4][m] = fma2(nu2, f0, fm[T2]);
+  }
+
+  // both biased reconstructions of every field (src/weno.cpp:77-152)
+  f2 rl[NEQ], rr[NEQ];
+#pragma unroll
+  for (int n = 0; n < NEQ; ++n) {
+    f2 numL, denL, numRn, denR;
+    weno5_pair_x2(w[n], numL, denL, numRn, denR);
+    rl[n] = fma2(numL, rcp2(denL), w[n][2]);
+    rr[n] = fma2(numRn, mul2(mone, rcp2(denR)), w[n][3]);
+  }
+
+  // back to conserved perturbations
+  f2 rhoL, mL[3], EL, rhoR, mR[3], ER;
+  const f2 uncc = mul2(un, cc);
+  {
+    const f2 sp = add2(rl[0], rl[2]), dm = sub2(rl[2], rl[0]);
+    rhoL = add2(sp, rl[1]);
+    mL[D] = fma2(un, rhoL, mul2(cc, dm));
+    mL[T1] = fma2(u1, rhoL, rl[3]);
+    mL[T2] = fma2(u2, rhoL, rl[4]);
+    EL = fma2(u2, rl[4], fma2(u1, rl[3], fma2(hq2, rl[1], fma2(uncc, dm, mul2(HH, sp)))));
+  }
+  {
+    const f2 sp = add2(rr[0], rr[2]), dm = sub2(rr[2], rr[0]);
+    rhoR = add2(sp, rr[1]);
+    mR[D] = fma2(un, rhoR, mul2(cc, dm));
+    mR[T1] = fma2(u1, rhoR, rr[3]);
+    mR[T2] = fma2(u2, rhoR, rr[4]);
+    ER = fma2(u2, rr[4], fma2(u1, rr[3], fma2(hq2, rr[1], fma2(uncc, dm, mul2(HH, sp)))));
+  }
+
+  // local Lax-Friedrichs flux, doubled (src/lf_flux.cpp:32-99)
+  const f2 rref = bc(C.rho_ref), pref = bc(C.p_ref), gamma = bc(C.gamma);
+  const f2 dL = add2(rref, rhoL), dR = add2(rref, rhoR);
+  const f2 ip = rcp2(mul2(dL, dR));
+  const f2 iL = mul2(ip, dR), iR = mul2(ip, dL);
+  f2 vL[3], vR[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    vL[a] = mul2(mL[a], iL);
+    vR[a] = mul2(mR[a], iR);
+  }
+  const f2 kL = fma2(mL[2], vL[2], fma2(mL[1], vL[1], mul2(mL[0], vL[0])));
+  const f2 kR = fma2(mR[2], vR[2], fma2(mR[1], vR[1], mul2(mR[0], vR[0])));
+  const f2 pL = mul2(gam1, fma2(bc(-0.5f), kL, EL));
+  const f2 pR = mul2(gam1, fma2(bc(-0.5f), kR, ER));
+  const f2 c2L = mul2(mul2(gamma, iL), add2(pref, pL)), c2R = mul2(mul2(gamma, iR), add2(pref, pR));
+  const f2 cL = mul2(c2L, rsqrt2(c2L)), cR = mul2(c2R, rsqrt2(c2R));
+  const f2 alpha = lanes(fmaxf(fabsf(vR[D].v.x) + cR.v.x, fabsf(vL[D].v.x) + cL.v.x),
+                         fmaxf(fabsf(vR[D].v.y) + cR.v.y, fabsf(vL[D].v.y) + cL.v.y));
+  const f2 fL = mL[D], fR = mR[D];
+  out[0] = fma2(alpha, sub2(rhoL, rhoR), add2(fL, fR));
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const f2 fLa = (a == D) ? fma2(fL, vL[a], add2(pL, pR)) : mul2(fL, vL[a]);
+    out[1 + a] = fma2(alpha, sub2(mL[a], mR[a]), fma2(fR, vR[a], fLa));
+  }
+  const f2 gi = bc(C.gam1_inv);
+  const f2 HLf = fma2(c2L, gi, mul2(half, mul2(kL, iL)));
+  const f2 HRf = fma2(c2R, gi, mul2(half, mul2(kR, iR)));
+  out[4] = fma2(alpha, sub2(EL, ER), fma2(fR, HRf, mul2(fL, HLf)));
+}
+
+// Threads of 32 x (tile_rows / 2): a thread takes rows j and j+1 of its tile
+// (the tile table is the one of the other stage kernels).  When JM is odd the
+// last row's partner lane repeats the row and is not stored.
+template <int D>
+__global__ void __maxnreg__(128) k_inviscid_x2(const SolveDev* __restrict__ solves,
+                                               const TileRef* __restrict__ tiles, int ntiles) {
+  const int rows = 2 * (int)(blockDim.x / TILE_X);
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const TileRef tr = tiles[t];
+    const SolveDev& s = solves[tr.solve];
+    if (!s.ctl->active) continue;
+    const int i = tr.ti * TILE_X + (int)(threadIdx.x % TILE_X);
+    const int j = tr.tj * rows + 2 * (int)(threadIdx.x / TILE_X);
+    const int k = tr.tk;
+    if (i >= s.IM || j >= s.JM) continue;
+    const bool pair = j + 1 < s.JM;
+    const long long c0 = pad_off(s, i, j, k);
+    const long long c1 = pair ? c0 + s.nx : c0;
+    f2 f[NEQ];
+    face_flux_x2<D>(s, c0, c1, f);
+    float* F = s.Ff[D];
+    const long long fo = int_off(s, i, j, k);
+#pragma unroll
+    for (int n = 0; n < NEQ; ++n) {
+      F[n * s.IV + fo] = f[n].v.x;
+      if (pair) F[n * s.IV + fo + s.IM] = f[n].v.y;
+    }
+  }
+}
+
 // Register caps: 128 for binary64 (16 warps per SM at 128 threads per CTA;
 // measured 3.4% faster than the same kernel under __launch_bounds__(256)) and 64
 // for binary32 (issue bound; 32 warps per SM).
@@ -1175,9 +1378,16 @@ static void stage_ty(const SolveDev* d, const TileRef* tiles, int ntiles, const 
                      int stage, const LaunchCfg& cfg, cudaStream_t st, Profiler* pf) {
   const int g = grid_for(ntiles, cfg.max_ctas);
   const int nt = 32 * cfg.tile_rows;
-  CBNS_LAUNCH(pf, KID_INVISCID_X, st, (k_inviscid<0, R><<<g, nt, 0, st>>>(d, tiles, ntiles, stage)));
-  CBNS_LAUNCH(pf, KID_INVISCID_Y, st, (k_inviscid<1, R><<<g, nt, 0, st>>>(d, tiles, ntiles, stage)));
-  CBNS_LAUNCH(pf, KID_INVISCID_Z, st, (k_inviscid<2, R><<<g, nt, 0, st>>>(d, tiles, ntiles, stage)));
+  if constexpr (sizeof(R) == 4) {
+    const int nt2 = 16 * cfg.tile_rows;  // two rows per thread
+    CBNS_LAUNCH(pf, KID_INVISCID_X, st, (k_inviscid_x2<0><<<g, nt2, 0, st>>>(d, tiles, ntiles)));
+    CBNS_LAUNCH(pf, KID_INVISCID_Y, st, (k_inviscid_x2<1><<<g, nt2, 0, st>>>(d, tiles, ntiles)));
+    CBNS_LAUNCH(pf, KID_INVISCID_Z, st, (k_inviscid_x2<2><<<g, nt2, 0, st>>>(d, tiles, ntiles)));
+  } else {
+    CBNS_LAUNCH(pf, KID_INVISCID_X, st, (k_inviscid<0, R><<<g, nt, 0, st>>>(d, tiles, ntiles, stage)));
+    CBNS_LAUNCH(pf, KID_INVISCID_Y, st, (k_inviscid<1, R><<<g, nt, 0, st>>>(d, tiles, ntiles, stage)));
+    CBNS_LAUNCH(pf, KID_INVISCID_Z, st, (k_inviscid<2, R><<<g, nt, 0, st>>>(d, tiles, ntiles, stage)));
+  }
   CBNS_LAUNCH(pf, KID_VISCOUS, st,
               (k_viscous<R><<<grid_for(nring, cfg.max_ctas), nt, 0, st>>>(d, ring_tiles, nring)));
   if constexpr (sizeof(R) == 4) {

@@ -108,3 +108,25 @@ def test_tiles_cover_each_domain_exactly():
                     covered.add((i, j, tk))
         assert len(covered) == ex * ey * ez
         assert tx < 2 ** 16 and ty < 2 ** 16 and ez < 2 ** 16  # TileRef fields are 16-bit
+
+
+def test_paired_face_kernel_covers_each_face_once():
+    """k_inviscid_x2: threads of 32 x rows/2 over the same tiles, each taking
+    rows j and j+1; the partner lane of an odd last row repeats row j and is not
+    stored.  Every interior face is stored exactly once, and every cell a lane
+    reads (its row's, or the repeated one's) lies in the interior."""
+    for (ex, ey, ez), rows in itertools.product([(4, 5, 6), (33, 17, 9), (64, 7, 3), (260, 260, 2)], (2, 4, 8)):
+        tx, ty = -(-ex // 32), -(-ey // rows)
+        stored = {}
+        for tk, tj, ti in itertools.product(range(ez), range(ty), range(tx)):
+            for t in range(32 * rows // 2):
+                i, j = ti * 32 + t % 32, tj * rows + 2 * (t // 32)
+                if i >= ex or j >= ey:
+                    continue
+                pair = j + 1 < ey
+                lanes = [(i, j, tk), (i, j + 1 if pair else j, tk)]
+                for c in lanes:
+                    assert 0 <= c[0] < ex and 0 <= c[1] < ey and 0 <= c[2] < ez
+                for c in lanes[:1 + pair]:
+                    stored[c] = stored.get(c, 0) + 1
+        assert len(stored) == ex * ey * ez and set(stored.values()) == {1}
