@@ -27,7 +27,10 @@
 // operation); the results stay within the 1e-11 relative tolerance of the
 // reference after 100 steps.  FP32-mixed solves run the same kernels
 // instantiated for binary32 on a perturbation of the state about the free
-// stream, with the binary64 state and its RK3 combination kept in binary64.
+// stream, with the binary64 state and its RK3 combination kept in binary64;
+// their face kernels (k_inviscid_x2<D>) compute two faces per thread in the
+// lanes of packed binary32x2 instructions, and their binary32 arrays are packed
+// per cell so that a stencil point is one or two 16-byte loads.
 #include <cuda_runtime.h>
 
 #include <cmath>
