@@ -457,8 +457,8 @@ __device__ __forceinline__ void weno5_pair(const R (&v)[6], Weno<R>& L, Weno<R>&
 // positive and at least 2.56e-22; the batch is used while the product of each
 // half lies in about [1e-150, 1e150] (biased exponent 525 .. 1520, tested on the
 // integer pipe), which keeps every partial product and partial reciprocal in
-// the normal range; otherwise each quotient is divided on its own.
-// Binary32: each quotient is divided (the binary32 pipe divides cheaply).
+// the normal range; otherwise each quotient is divided on its own.  (The
+// binary32 faces multiply by per-face reciprocals: face_flux_x2.)
 __device__ __forceinline__ void weno_divide10(const Weno<double> (&w)[10], const double (&base)[10],
                                               double (&r)[10]) {
   // Two halves of five: prefix products within each half, one reciprocal of the
@@ -492,12 +492,6 @@ __device__ __forceinline__ void weno_divide10(const Weno<double> (&w)[10], const
   }
 }
 
-__device__ __forceinline__ void weno_divide10(const Weno<float> (&w)[10], const float (&base)[10],
-                                              float (&r)[10]) {
-#pragma unroll
-  for (int n = 0; n < 10; ++n) r[n] = base[n] + div_(w[n].num, w[n].den);
-}
-
 // ---------------------------------------------------------------------------
 // Numerical flux at one face (src/Block3d.cpp:566-616 and its y/z twins).
 //
@@ -513,39 +507,28 @@ __device__ __forceinline__ void weno_divide10(const Weno<float> (&w)[10], const 
 //   E = H s + U_D c d + q^2/2 r1 + U_t1 r3 + U_t2 r4.
 // The Roe average (ratio = sqrt(rho_R/rho_L)) is formed from per-cell sqrt(rho).
 // lf_flux (src/lf_flux.cpp:32-99) takes the reconstructed conserved states.
-//
-// PERT (FP32-mixed): f is the perturbation (rho', m, E') of the reference state.
-// L and R are linear and WENO5 reproduces constants, so reconstructing the
-// perturbation and adding rho_ref, E_ref back is the same scheme; the momentum
-// flux drops the constant p_ref (it cancels in every flux difference), so every
-// binary32 flux component is O(1) instead of O(p_ref).
+// Binary64; the FP32-mixed faces are face_flux_x2 below.
 
-template <int D, typename R, bool PERT>
+template <int D, typename R>
 __device__ __forceinline__ void face_flux(const SolveDev& s, const R* __restrict__ U, long long c,
                                           R (&out)[NEQ]) {
+  static_assert(sizeof(R) == 8, "binary64 faces; FP32-mixed faces are face_flux_x2");
   constexpr int T1 = (D + 1) % 3;
   constexpr int T2 = (D + 2) % 3;
   const long long st = D == 0 ? 1ll : (D == 1 ? (long long)s.nx : (long long)s.nx * s.ny);
   const long long V = s.V;
   const long long cl = c - st;
   const Consts<R>& C = consts_of<R>(s);
-  const R gam1 = C.gam1, gamma = C.gamma, gam1_inv = C.gam1_inv;
+  const R gam1 = C.gam1, gamma = C.gamma;
 
   // Roe-averaged state of the two cells either side (src/eigenvectors_roe.cpp:87-106).
   // (sqrt(rho_L) f_L + sqrt(rho_R) f_R) / (sqrt(rho_L) + sqrt(rho_R)) = f_R + wL (f_L - f_R).
   R Uv[3], HH;
   {
     // sqrt(rho), u, v, w, H of the cells either side (l: c - st, r: c)
-    R sl, sr, ul, ur, vl, vr, wl, wr, hl, hr;
-    if constexpr (sizeof(R) == 4) {
-      const float4 al = s.PA[cl], ar = s.PA[c], bl = s.PB[cl], br = s.PB[c];
-      sl = bl.z, sr = br.z, hl = bl.w, hr = br.w;
-      ul = al.x, ur = ar.x, vl = al.y, vr = ar.y, wl = al.z, wr = ar.z;
-    } else {
-      const PrimSet<double>& P = s.pd;
-      sl = P.srho[cl], sr = P.srho[c], hl = P.H[cl], hr = P.H[c];
-      ul = P.u[cl], ur = P.u[c], vl = P.v[cl], vr = P.v[c], wl = P.w[cl], wr = P.w[c];
-    }
+    const PrimSet<double>& P = s.pd;
+    const R sl = P.srho[cl], sr = P.srho[c], hl = P.H[cl], hr = P.H[c];
+    const R ul = P.u[cl], ur = P.u[c], vl = P.v[cl], vr = P.v[c], wl = P.w[cl], wr = P.w[c];
     const R wL = div_(sl, sl + sr);
     Uv[0] = fma_(wL, ul - ur, ur);
     Uv[1] = fma_(wL, vl - vr, vr);
@@ -567,13 +550,7 @@ __device__ __forceinline__ void face_flux(const SolveDev& s, const R* __restrict
 #pragma unroll
   for (int m = 0; m < 6; ++m) {
     const long long o = c + (m - 3) * st;
-    R f0, f1, f2, f3, f4;
-    if constexpr (sizeof(R) == 4) {
-      const float4 a = s.U4[o];
-      f0 = a.x, f1 = a.y, f2 = a.z, f3 = a.w, f4 = s.UE[o];
-    } else {
-      f0 = U[o], f1 = U[V + o], f2 = U[2 * V + o], f3 = U[3 * V + o], f4 = U[4 * V + o];
-    }
+    const R f0 = U[o], f1 = U[V + o], f2 = U[2 * V + o], f3 = U[3 * V + o], f4 = U[4 * V + o];
     const R fm[3] = {f1, f2, f3};
     const R t = fma_(-Uv[2], f3, fma_(-Uv[1], f2, fma_(-Uv[0], f1, fma_(hq2, f0, f4))));
     const R A = K * t;
@@ -606,7 +583,7 @@ __device__ __forceinline__ void face_flux(const SolveDev& s, const R* __restrict
     }
   }
 
-  // Back to conserved variables (perturbations when PERT).
+  // Back to conserved variables.
   R rhoL, mL[3], EL, rhoR, mR[3], ER;
   {
     R sp = rl[0] + rl[2], dm = rl[2] - rl[0];
@@ -626,14 +603,10 @@ __device__ __forceinline__ void face_flux(const SolveDev& s, const R* __restrict
   }
 
   // Local Lax-Friedrichs flux (src/lf_flux.cpp:32-99); both 1/rho from one division.
-  // PERT: rhoX, EX are perturbations; dL, dR the full densities, pL, pR the
-  // pressure perturbations, pfL, pfR the full pressures.
   // The stored flux is twice the reference's: the halves are folded into the
   // flux difference's 0.5/h (an exact power-of-two scaling).
-  const R dL = PERT ? C.rho_ref + rhoL : rhoL;
-  const R dR = PERT ? C.rho_ref + rhoR : rhoR;
-  const R ip = div_((R)1, dL * dR);
-  const R iL = ip * dR, iR = ip * dL;
+  const R ip = div_((R)1, rhoL * rhoR);
+  const R iL = ip * rhoR, iR = ip * rhoL;
   R vL[3], vR[3];
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
@@ -645,9 +618,7 @@ __device__ __forceinline__ void face_flux(const SolveDev& s, const R* __restrict
   const R kR = fma_(mR[2], vR[2], fma_(mR[1], vR[1], mR[0] * vR[0]));
   const R pL = gam1 * fma_((R)-0.5, kL, EL);
   const R pR = gam1 * fma_((R)-0.5, kR, ER);
-  const R pfL = PERT ? C.p_ref + pL : pL;
-  const R pfR = PERT ? C.p_ref + pR : pR;
-  const R c2L = (gamma * iL) * pfL, c2R = (gamma * iR) * pfR;
+  const R c2L = (gamma * iL) * pL, c2R = (gamma * iR) * pR;
   const R cL = c2L * rsqrt(c2L), cR = c2R * rsqrt(c2R);
   const R alpha = fmax(fabs(vR[D]) + cR, fabs(vL[D]) + cL);
   const R fL = mL[D], fR = mR[D];  // mass fluxes rho*q_n
@@ -657,15 +628,8 @@ __device__ __forceinline__ void face_flux(const SolveDev& s, const R* __restrict
     const R fLa = (a == D) ? fma_(fL, vL[a], pL + pR) : fL * vL[a];
     out[1 + a] = fma_(-alpha, mR[a] - mL[a], fma_(fR, vR[a], fLa));
   }
-  if constexpr (PERT) {
-    // rho q_n H with H = c^2/(gamma-1) + q^2/2 from the full sound speed.
-    const R HL = fma_(c2L, gam1_inv, (R)0.5 * (kL * iL));
-    const R HR = fma_(c2R, gam1_inv, (R)0.5 * (kR * iR));
-    out[4] = fma_(-alpha, ER - EL, fma_(fR, HR, fL * HL));
-  } else {
-    // rho q_n H = q_n (E + p).
-    out[4] = fma_(-alpha, ER - EL, fma_(vR[D], ER + pR, vL[D] * (EL + pL)));
-  }
+  // rho q_n H = q_n (E + p).
+  out[4] = fma_(-alpha, ER - EL, fma_(vR[D], ER + pR, vL[D] * (EL + pL)));
 }
 
 // ---------------------------------------------------------------------------
@@ -675,12 +639,17 @@ __device__ __forceinline__ void face_flux(const SolveDev& s, const R* __restrict
 // Blackwell's packed binary32 instructions (fma/add/mul .f32x2), which do two
 // faces' arithmetic per issued instruction.  Loads, the reciprocal and
 // reciprocal square roots (MUFU), abs/max and the stores stay per face.  Each
-// lane performs face_flux<D, float, true>'s operations; subtractions are
-// fma(b, -1, a) (the same rounding as a - b), and the terms whose sign the
-// scalar code took for free are formed with the opposite sign where that leaves
-// the result unchanged (a squared e_k; the right-biased numerator negated
-// together with its denominator; alpha times (L - R) instead of -alpha times
-// (R - L)).
+// lane performs face_flux's operations in binary32 on the perturbation form:
+// f is the perturbation (rho', m, E') of the reference state; L and R are
+// linear and WENO5 reproduces constants, so reconstructing the perturbation and
+// adding rho_ref, E_ref back is the same scheme; the momentum flux drops the
+// constant p_ref (it cancels in every flux difference), so every binary32 flux
+// component is O(1) instead of O(p_ref); the energy flux is rho q_n H with H
+// from the full sound speed.  Subtractions are fma(b, -1, a) (the same rounding
+// as a - b), and terms whose sign a scalar fma takes for free are formed with
+// the opposite sign where that leaves the result unchanged (a squared e_k; the
+// right-biased numerator negated together with its reciprocal; alpha times
+// (L - R) instead of -alpha times (R - L)).
 
 struct f2 {
   float2 v;
@@ -871,29 +840,21 @@ __global__ void __maxnreg__(128) k_inviscid_x2(const SolveDev* __restrict__ solv
   }
 }
 
-// Register caps: 128 for binary64 (16 warps per SM at 128 threads per CTA;
-// measured 3.4% faster than the same kernel under __launch_bounds__(256)) and 64
-// for binary32 (issue bound; 32 warps per SM).
+// Binary64 faces, one per thread.  Register cap 128 (16 warps per SM at 128
+// threads per CTA; measured 3.4% faster than the same kernel under
+// __launch_bounds__(256)).
 template <int D, typename R>
-__global__ void __maxnreg__(sizeof(R) == 4 ? 64 : 128) k_inviscid(const SolveDev* __restrict__ solves,
-                                                          const TileRef* __restrict__ tiles, int ntiles, int stage) {
-  constexpr bool MIXED = sizeof(R) == 4;
+__global__ void __maxnreg__(128) k_inviscid(const SolveDev* __restrict__ solves, const TileRef* __restrict__ tiles,
+                                            int ntiles, int stage) {
   for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
     TileCell tc = tile_cell(tiles[t], 0);
     const SolveDev& s = solves[tc.s];
     if (!s.ctl->active) continue;
     if (tc.i >= s.IM || tc.j >= s.JM) continue;
-    const R* U;
-    R* F;
-    if constexpr (MIXED) {
-      U = nullptr;  // face_flux reads the packed s.U4, s.UE
-      F = s.Ff[D];
-    } else {
-      U = stage == 1 ? s.Q : s.Qp;
-      F = s.F[D];
-    }
+    const R* U = stage == 1 ? s.Q : s.Qp;
+    R* F = s.F[D];
     R f[NEQ];
-    face_flux<D, R, MIXED>(s, U, pad_off(s, tc.i, tc.j, tc.k), f);
+    face_flux<D, R>(s, U, pad_off(s, tc.i, tc.j, tc.k), f);
     const long long fo = int_off(s, tc.i, tc.j, tc.k);
 #pragma unroll
     for (int n = 0; n < NEQ; ++n) F[n * s.IV + fo] = f[n];
