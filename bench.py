@@ -14,8 +14,9 @@ ours:       W untimed steps, then K steps timed with CUDA events on the solve's
                 measured live by cbns_probe_peak;
               * e2e: K steps through the C ABI with host buffers: upload Q from
                 pinned memory, one step, download Q, every step, on two handles
-                driven by two host threads (one handle's copies overlap the
-                other's kernels); the one-handle sequential loop beside it;
+                driven by two host threads, K steps each (one handle's copies
+                overlap the other's kernels); the one-handle sequential loop of
+                K steps beside it;
               * cpu_baseline: the oracle's CPU restatement of the reference (all
                 host threads) on a bounded sample of the same workload.
 reference:  the reference algorithm on the host cores (the oracle's restatement,
@@ -359,9 +360,9 @@ def run_ours(args, rank, world, local):
     # e2e: host buffers through the C ABI, copies inside the timed region.  Every
     # step uploads its input state from pinned host memory, steps, and downloads
     # its result.  Each C-ABI call synchronises its handle's stream, so two
-    # handles on two host threads keep one handle's copies in flight under the
-    # other's kernels (the K steps split between them); the one-handle sequential
-    # loop is reported beside it.
+    # handles on two host threads, K steps each, keep one handle's copies in
+    # flight under the other's kernels; the one-handle sequential loop of K steps
+    # is reported beside it.
     if not args.no_e2e:
         n = int(np.prod(s.shape))
         s2 = Solver(p)
@@ -384,8 +385,7 @@ def run_ours(args, rank, world, local):
         e2e_steps(s, pinned[0], pinned[1], args.steps)
         seq = reduce_max(time.perf_counter() - t0, world)
         barrier(world)
-        share = [args.steps - args.steps // 2, args.steps // 2]
-        threads = [threading.Thread(target=e2e_steps, args=(h, hin, hout, k)) for (h, hin, hout), k in zip(jobs, share)]
+        threads = [threading.Thread(target=e2e_steps, args=(h, hin, hout, args.steps)) for h, hin, hout in jobs]
         t0 = time.perf_counter()
         for t in threads:
             t.start()
@@ -394,10 +394,10 @@ def run_ours(args, rank, world, local):
         sec = reduce_max(time.perf_counter() - t0, world)
         s2.close()
         if rank == 0:
-            line["e2e"] = {"value": world * cells * args.steps / sec, "unit": UNIT,
+            line["e2e"] = {"value": world * cells * 2 * args.steps / sec, "unit": UNIT,
                            "h2d_bytes_per_step": n * 8, "d2h_bytes_per_step": n * 8,
                            "path": "cbns_upload_Q (pinned) + cbns_step + cbns_download_Q (pinned), per step; "
-                                   "two handles on two host threads, %d + %d steps" % tuple(share),
+                                   "two handles on two host threads, %d steps each" % args.steps,
                            "sequential_one_handle": world * cells * args.steps / seq}
     s.close()
 
