@@ -74,7 +74,7 @@ size_t tile_count(long long ex, long long ey, long long ez, int rows = TILE_Y) {
 
 // Byte offsets of everything a solve's arena holds (see cbns_create).
 struct ArenaLayout {
-  size_t oQ, oQp, oStage, oPrim, oF[3], oTv, oFf[3], oTvf, oUf, oPf, oCtl, oDesc, oTi, oTr, oTp, oPart, oOut,
+  size_t oQ, oQp, oStage, oPrim, oF[3], oTv, oFf[3], oTv32, oU32, oP32, oCtl, oDesc, oTi, oTr, oTp, oPart, oOut,
       total;
 };
 
@@ -95,10 +95,10 @@ ArenaLayout arena_layout(const SolveDev& s, bool mixed, size_t n_int, size_t n_r
     for (int d = 0; d < 3; ++d) L.oF[d] = take(sizeof(double) * NEQ * (size_t)s.IV);
     L.oTv = take(sizeof(double) * kViscTerms * (size_t)s.RV);
   } else {
-    L.oUf = take(NEQ * fV);  // U4 (4 values per cell), then UE
-    L.oPf = take(9 * fV);    // PA and PB (4 values per cell each), then mu
+    L.oU32 = take(NEQ * fV);  // U4 (4 values per cell), then UE
+    L.oP32 = take(9 * fV);    // PA and PB (4 values per cell each), then mu
     for (int d = 0; d < 3; ++d) L.oFf[d] = take(sizeof(float) * NEQ * (size_t)s.IV);
-    L.oTvf = take(sizeof(float4) * 3 * (size_t)s.RV);
+    L.oTv32 = take(sizeof(float4) * 3 * (size_t)s.RV);
   }
   L.oCtl = take(sizeof(SolveCtl));
   L.oDesc = take(sizeof(SolveDev));
@@ -247,7 +247,7 @@ cbns_status cbns_create(const cbns_params* p, uint32_t IM, uint32_t JM, uint32_t
   s.mixed = mixed ? 1 : 0;
   const ArenaLayout L = arena_layout(s, mixed, t_int.size(), t_ring.size(), t_pad.size(), h->nparts);
   const size_t off = L.total;
-  const size_t oQ = L.oQ, oQp = L.oQp, oStage = L.oStage, oPrim = L.oPrim, oUf = L.oUf, oPf = L.oPf;
+  const size_t oQ = L.oQ, oQp = L.oQp, oStage = L.oStage, oPrim = L.oPrim, oU32 = L.oU32, oP32 = L.oP32;
   const size_t oCtl = L.oCtl, oDesc = L.oDesc, oTi = L.oTi, oTr = L.oTr, oTp = L.oTp, oPart = L.oPart,
                oOut = L.oOut;
   const size_t *oF = L.oF, *oFf = L.oFf;
@@ -276,16 +276,16 @@ cbns_status cbns_create(const cbns_params* p, uint32_t IM, uint32_t JM, uint32_t
     s.PA = s.PB = nullptr;
     s.muf = nullptr;
   } else {
-    s.U4 = (float4*)(A + oUf);
+    s.U4 = (float4*)(A + oU32);
     s.UE = (float*)(s.U4 + s.V);
-    s.PA = (float4*)(A + oPf);
+    s.PA = (float4*)(A + oP32);
     s.PB = s.PA + s.V;
     s.muf = (float*)(s.PB + s.V);
     for (int d = 0; d < 3; ++d) {
       s.Ff[d] = (float*)(A + oFf[d]);
       s.F[d] = nullptr;
     }
-    s.Tvg = (float4*)(A + L.oTvf);
+    s.Tvg = (float4*)(A + L.oTv32);
     s.Tv = nullptr;
   }
   const cbns_params& P = h->params;
