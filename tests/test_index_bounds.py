@@ -65,10 +65,14 @@ def test_stage_kernels_stay_in_bounds(shape):
         assert lo >= 0 and hi < g["V"]
     lo, hi = span(lambda i, j, k: ring_off(g, i, j, k), *ring, [0])
     assert lo >= 0 and hi < g["RV"]
-    # k_update: viscous flux stencil at interior cells, +-2 ring strides
-    for st in [1, g["rx"], g["rx"] * g["ry"]]:
+    # k_update: viscous flux stencil at interior cells, +-2 ring strides.  Binary64:
+    # term t at t*RV + r (9 blocks); FP32-mixed: the terms differenced along d
+    # grouped in block d of 3, one float4 at d*RV + r.
+    for d, st in enumerate([1, g["rx"], g["rx"] * g["ry"]]):
         lo, hi = span(lambda i, j, k: ring_off(g, i, j, k), *interior, [-2 * st, 2 * st])
         assert lo >= 0 and hi < g["RV"]
+        assert d * g["RV"] + lo >= d * g["RV"] and d * g["RV"] + hi < 3 * g["RV"]
+        assert 8 * g["RV"] + hi < 9 * g["RV"]
     # k_update ghost images: i + IM when i < NG, i - IM when i >= IM - NG (per axis)
     for i in range(IM):
         for img in [i] + ([i + IM] if i < NG else []) + ([i - IM] if i >= IM - NG else []):
