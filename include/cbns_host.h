@@ -51,7 +51,9 @@ cbns_status cbns_host_read_bin(const char* fname, uint32_t IM, uint32_t JM, uint
 /* output_vtk_xml (src/output_vtk_xml.cpp:22-48) with Block3d::output_vtr and
  * output_vtm (src/Block3d.cpp:396-500): <dir>/<fname><rank %03d>.vtr (ASCII
  * RectilinearGrid, CellData rho u v w p, "%e ") and, on rank 0, <dir>/<fname>.vtm.
- * Primitive arrays are in the padded get_idx layout. */
+ * Primitive arrays are in the padded get_idx layout.  The text is formatted on
+ * every host core (CBNS_HOST_THREADS=n to limit it) and written in order, so the
+ * file does not depend on the thread count. */
 cbns_status cbns_host_output_vtk_xml(const char* dir, const char* fname, int rank, uint32_t num_blocks,
                                      uint32_t IM, uint32_t JM, uint32_t KM, const double* x,
                                      const double* y, const double* z, const double* rho,
