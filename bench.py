@@ -145,6 +145,16 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
+def workload_config(N):
+    """The `config` both arms print: the same workload, so the two lines compare
+    like for like (where each arm runs is in its `placement` key)."""
+    from cbns3d_cart_mpi_gb300._abi import NEQ, NG
+    return {"workload": "taylor-green vortex %d^3 FP64, Re 1600, Ma 0.1, CFL 0.5" % N, "grid": [N, N, N],
+            "precision": "fp64",
+            "l2": "state 2x%.0f MB per step, larger than the 129 MB L2; no flush" % (
+                NEQ * (N + 2 * NG) ** 3 * 8 / 1e6)}
+
+
 def cpu_sample(N, steps):
     """The oracle's CPU restatement of the reference on `steps` steps of the N^3
     workload, all host threads; returns (cell-steps/s, threads, seconds)."""
@@ -161,6 +171,17 @@ def cpu_sample(N, steps):
     th = num_threads()
     b.close()
     return N ** 3 * steps / sec, th, sec
+
+
+def ncu_counts():
+    """Per-launch figures from the committed ncu summaries (profiles/traffic.json):
+    DRAM bytes per launch at 256^3 and binary64 instructions per face."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(path) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
 
 
 def run_reference(args, rank, world):
@@ -185,8 +206,8 @@ def run_reference(args, rank, world):
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sec / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "taylor-green vortex %d^3 FP64, Re 1600, Ma 0.1, CFL 0.5" % N, "grid": [N, N, N],
-                   "parallelism": "host threads (OpenMP over k-planes)"},
+        "config": workload_config(N),
+        "placement": "host cores (%d OpenMP threads over k-planes)" % th,
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": th, "kind": "port",
                          "sample": "%d warm-up + %d timed full RK3 steps of the %d^3 workload" % (
                              args.warmup, args.steps, N)},
@@ -205,8 +226,8 @@ def run_ours(args, rank, world, local):
 
     from cbns3d_cart_mpi_gb300 import build as pkg_build
     from cbns3d_cart_mpi_gb300._abi import NEQ, NG, tgv_params
-    from cbns3d_cart_mpi_gb300.solver import Solver, initial_condition, probe_peak
-    from cbns3d_cart_mpi_gb300.workload import kernel_flops, mixed_update_bytes, state_bytes_per_step
+    from cbns3d_cart_mpi_gb300.solver import Solver, initial_condition
+    from cbns3d_cart_mpi_gb300.workload import kernel_flops, mixed_update_bytes, probe_peak, state_bytes_per_step
 
     pkg_build.build()
     os.environ["CBNS_DEVICE"] = str(local)
@@ -248,11 +269,8 @@ def run_ours(args, rank, world, local):
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "taylor-green vortex %d^3 FP64, Re 1600, Ma 0.1, CFL 0.5 (one solve per GPU)" % N,
-                       "grid": [N, N, N], "precision": "fp64",
-                       "parallelism": "replicas" if world > 1 else "single GPU",
-                       "l2": "state 2x%.0f MB per step, larger than the 129 MB L2; no flush" % (
-                           NEQ * (N + 2 * NG) ** 3 * 8 / 1e6)},
+            "config": workload_config(N),
+            "placement": ("%d replicas, one solve per GPU" % world) if world > 1 else "one solve on one GPU",
             "clocks": clocks,
             "gpu_launches": launches_per_step * args.steps,
         }
@@ -267,28 +285,32 @@ def run_ours(args, rank, world, local):
         dom = max(prof, key=lambda k: prof[k][1])
         if dom.startswith("inviscid_"):
             # One kernel template per direction with equal shares (29.1% each); the
-            # x-direction launch is the one whose DRAM traffic profiles/ records.
+            # x-direction launch is the one whose ncu counts are recorded.
             dom = "inviscid_x"
         per_launch_ms = prof[dom][1] / prof[dom][0]
         flops = kernel_flops(dom, N, N, N)
         achieved = flops / (per_launch_ms * 1e-3) * 1e-12
         peak = probe_peak(fp64=True)
-        traffic = None
-        tpath = os.path.join(ROOT, "profiles", "traffic.json")
-        if os.path.exists(tpath):
-            with open(tpath) as f:
-                traffic = json.load(f).get(dom)
+        counts = ncu_counts()
+        traffic = counts.get(dom)
         line["roofline"] = {
             "bound": "fp64-pipe", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
             "frac": achieved / peak, "traffic": traffic,
             "peak_source": "binary64 FMA throughput measured live on this GPU (cbns_probe_peak); "
                            "MEASURED_PEAKS.json holds no FP64 figure",
             "algorithmic_flops_per_launch": flops,
-            "flop_count": "reference's own op count per face/cell (tests/golden/opcount.txt)",
-            "note": "achieved counts the reference's FLOPs; the kernel issues fewer binary64 instructions "
-                    "than that count, so frac can exceed 1; its FP64-pipe utilisation (ncu) is in "
-                    "profiles/inviscid_fp64_tgv160.md",
+            "flop_count": "reference's own op count per face (tests/golden/opcount.txt) x N^3 distinct "
+                          "periodic faces; a division counts 1",
+            "note": "frac counts the reference's FLOPs against the FMA peak and can exceed 1; pipe_frac is "
+                    "the binary64 instructions the kernel issues (ncu) over the pipe's measured issue rate",
         }
+        inst = counts.get(dom + "_fp64_inst_per_face")
+        if inst:
+            # Binary64 instructions issued per second over the probe's FMA rate
+            # (peak TFLOP/s / 2 FLOPs per FMA): the FP64 pipe's busy fraction.
+            issued = inst * N ** 3 / (per_launch_ms * 1e-3)
+            line["roofline"]["pipe_frac"] = issued / (peak * 1e12 / 2.0)
+            line["roofline"]["fp64_inst_per_face"] = inst
         step_ms = ms / args.steps
         line["kernels"] = kernels
         line["step_roofline"] = {

@@ -12,8 +12,10 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_DIR = os.path.join(PKG, "lib")
 GPU_LIB = os.path.join(LIB_DIR, "libcbns_gpu.so")
 HOST_LIB = os.path.join(LIB_DIR, "libcbns_host.so")
+PROBE_LIB = os.path.join(LIB_DIR, "libcbns_probe.so")
 
 _gpu = None
+_probe = None
 
 
 class ServerOpts(ctypes.Structure):
@@ -90,7 +92,6 @@ GPU_API = {
     "cbns_batch_stream": (c_vp, [c_vp]),
     "cbns_profile_begin": (c_int, [c_vp]),
     "cbns_profile_end": (c_int, [c_vp, c_vp, c_int, ctypes.POINTER(c_int)]),
-    "cbns_probe_peak": (c_int, [c_int, c_dp]),
     "cbns_diagnostics_noalloc": (c_int, [c_vp, c_u32, c_u32, c_u32, c_d, c_d, c_d, c_vp, c_vp]),
     "cbns_last_error": (ctypes.c_char_p, []),
     "cbns_version": (ctypes.c_char_p, []),
@@ -136,6 +137,19 @@ def host():
                                % HOST_LIB)
         _host = _bind(ctypes.CDLL(HOST_LIB), HOST_API)
     return _host
+
+
+def probe():
+    """The FMA-throughput probe library that bench.py uses for roofline peaks."""
+    global _probe
+    if _probe is None:
+        if not os.path.exists(PROBE_LIB):
+            raise RuntimeError("libcbns_probe.so is not built (%s); run cbns3d_cart_mpi_gb300.build.build()"
+                               % PROBE_LIB)
+        _probe = ctypes.CDLL(PROBE_LIB)
+        _probe.cbns_probe_peak.restype = c_int
+        _probe.cbns_probe_peak.argtypes = [c_int, c_dp]
+    return _probe
 
 
 def last_error():

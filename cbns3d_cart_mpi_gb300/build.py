@@ -1,6 +1,8 @@
 """Build the native parts in-tree, with nvcc and g++ only (no CMake).
 
   lib/libcbns_gpu.so   CUDA kernels + C ABI of include/cbns_gpu.h (sm_103a only)
+  lib/libcbns_probe.so FMA-throughput probe, the roofline denominator bench.py
+                       measures (not part of the product library)
   lib/libcbns_host.so  host C++ of include/cbns_host.h (input.txt, IC, checkpoint, VTK)
   lib/cbns3d_gb300     the Block3d-style driver executable
 
@@ -18,8 +20,8 @@ CSRC = os.path.join(PKG, "csrc")
 LIB = os.path.join(PKG, "lib")
 INCLUDE = os.path.join(ROOT, "include")
 
-GPU_SOURCES = ["cbns_kernels.cu", "cbns_api.cu", "cbns_probe.cu", "cbns_noalloc.cu", "cbns_serve.cu",
-               "cbns_ckpt.cu"]
+GPU_SOURCES = ["cbns_kernels.cu", "cbns_api.cu", "cbns_noalloc.cu", "cbns_serve.cu", "cbns_ckpt.cu"]
+PROBE_SOURCE = "cbns_probe.cu"
 HOST_SOURCES = ["host/cbns_host.cpp"]
 DRIVER_SOURCE = "host/cbns3d_gb300.cpp"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -33,6 +35,7 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompil
               "--expt-relaxed-constexpr"]
 
 GPU_LIB = os.path.join(LIB, "libcbns_gpu.so")
+PROBE_LIB = os.path.join(LIB, "libcbns_probe.so")
 HOST_LIB = os.path.join(LIB, "libcbns_host.so")
 DRIVER = os.path.join(LIB, "cbns3d_gb300")
 
@@ -101,15 +104,19 @@ def build(verbose=False, extra_nvcc=()):
 
     with ThreadPoolExecutor(max_workers=max(2, os.cpu_count() or 2)) as ex:
         gpu_f = [ex.submit(cu_obj, s) for s in GPU_SOURCES]
+        probe_f = ex.submit(cu_obj, PROBE_SOURCE)
         host_f = [ex.submit(cpp_obj, s) for s in HOST_SOURCES]
         drv_f = ex.submit(cpp_obj, DRIVER_SOURCE)
         gpu_objs = [f.result() for f in gpu_f]
         host_objs = [f.result() for f in host_f]
         drv_obj = drv_f.result()
+        probe_obj = probe_f.result()
 
     cudalib = os.path.join(_cuda_home(), "lib64")
     if _stale(GPU_LIB, gpu_objs):
         _atomic(lambda out: [nvcc] + ARCH + ["-shared", "-o", out] + gpu_objs + ["-lcudart"], GPU_LIB)
+    if _stale(PROBE_LIB, [probe_obj]):
+        _atomic(lambda out: [nvcc] + ARCH + ["-shared", "-o", out, probe_obj, "-lcudart"], PROBE_LIB)
     if _stale(HOST_LIB, host_objs):
         _atomic(lambda out: ["g++", "-shared", "-o", out] + host_objs, HOST_LIB)
     if _stale(DRIVER, [drv_obj, GPU_LIB, HOST_LIB]):
@@ -117,7 +124,7 @@ def build(verbose=False, extra_nvcc=()):
                              "-L" + cudalib, "-lcudart", "-pthread", "-Wl,-rpath,$ORIGIN", "-Wl,-rpath," + cudalib],
                 DRIVER)
     if verbose:
-        for p in (GPU_LIB, HOST_LIB, DRIVER):
+        for p in (GPU_LIB, PROBE_LIB, HOST_LIB, DRIVER):
             print(p)
     return GPU_LIB, HOST_LIB, DRIVER
 

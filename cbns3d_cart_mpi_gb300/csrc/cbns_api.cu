@@ -5,6 +5,7 @@
 // tables, plus a CUDA stream.  The host never sees device pointers.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -67,6 +68,15 @@ void append_tiles(std::vector<TileRef>& out, int solve, int ex, int ey, int ez, 
 }
 
 size_t align_up(size_t x) { return (x + 255) & ~size_t(255); }
+
+// Tile coordinates are 16-bit (TileRef): the padded extent along k (one tile
+// per plane) and the tile counts along i and j must stay below 65536.  With
+// 2-row tiles (the smallest the batches use) this caps every extent at
+// 65535 - 2 NG cells along k, and more along i and j; memory runs out far below.
+constexpr uint32_t kMaxExtent = 65535 - 2 * NG;
+bool block_extents_ok(uint32_t IM, uint32_t JM, uint32_t KM) {
+  return IM <= kMaxExtent && JM <= kMaxExtent && KM <= kMaxExtent;
+}
 
 size_t tile_count(long long ex, long long ey, long long ez, int rows = TILE_Y) {
   return (size_t)((ex + TILE_X - 1) / TILE_X) * (size_t)((ey + rows - 1) / rows) * (size_t)ez;
@@ -182,16 +192,22 @@ cbns_status cbns_create(const cbns_params* p, uint32_t IM, uint32_t JM, uint32_t
   if (precision != CBNS_FP64 && precision != CBNS_FP32_MIXED)
     return fail(CBNS_ERR_INVALID_ARG, "cbns_create: unknown precision");
   // The reference's halo exchange sends NG interior layers; a block narrower than
-  // NG would send ghost cells.  Tile coordinates are 16-bit and padded offsets fit
-  // a 31-bit index per array.
+  // NG would send ghost cells.  Above that, the extents are limited by the 16-bit
+  // tile coordinates (block_extents_ok) and by device memory (checked against
+  // cbns_footprint's arena size below); every offset is 64-bit.
   if (IM < (uint32_t)NG || JM < (uint32_t)NG || KM < (uint32_t)NG)
     return fail(CBNS_ERR_BAD_DIMS, "cbns_create: every extent must be >= 4 (NG)");
-  const double vol = (double)(IM + 2 * NG) * (JM + 2 * NG) * (KM + 2 * NG);
-  if (IM > 16384 || JM > 16384 || KM > 16384 || vol * NEQ > 2147483647.0)
-    return fail(CBNS_ERR_BAD_DIMS, "cbns_create: block too large (5*(IM+8)(JM+8)(KM+8) must be < 2^31)");
+  if (!block_extents_ok(IM, JM, KM))
+    return fail(CBNS_ERR_BAD_DIMS, "cbns_create: an extent exceeds " + std::to_string(kMaxExtent) +
+                                       " cells (16-bit tile coordinates)");
   if (!(p->gamma > 1.0) || !(p->Re > 0.0) || !(p->Mach > 0.0) || !(p->Pr > 0.0) || !(p->CFL > 0.0) ||
       !(p->T_inf > 0.0) || p->IM == 0 || p->JM == 0 || p->KM == 0)
     return fail(CBNS_ERR_INVALID_ARG, "cbns_create: parameters out of range (gamma>1, Re, Mach, Pr, CFL, T_inf > 0)");
+  // One GPU holds the whole grid: the spacing (gen_mesh, from p->IM/JM/KM) and the
+  // periodic ghost images (from the block's own extents) must describe one grid.
+  if (p->IM != IM || p->JM != JM || p->KM != KM)
+    return fail(CBNS_ERR_BAD_DIMS, "cbns_create: the block extents must equal the grid's (p->IM, p->JM, p->KM): "
+                                   "one GPU holds the whole periodic grid");
 
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
@@ -231,6 +247,24 @@ cbns_status cbns_create(const cbns_params* p, uint32_t IM, uint32_t JM, uint32_t
   SolveDev& s = h->desc;
   set_extents(s, IM, JM, KM);
 
+  // Arena layout.  Both modes hold the binary64 state (Q, Q_p, staging) and
+  // binary64 primitives; binary64 solves add binary64 face/viscous fluxes,
+  // FP32-mixed solves the binary32 perturbation state, primitives and fluxes.
+  // The size is checked against free device memory before any table is built.
+  const bool mixed = precision == CBNS_FP32_MIXED;
+  s.mixed = mixed ? 1 : 0;
+  h->nparts = kDiagParts;
+  const size_t nt_int = tile_count(IM, JM, KM), nt_ring = tile_count(s.rx, s.ry, s.rz),
+               nt_pad = tile_count(s.nx, s.ny, s.nz);
+  const ArenaLayout L = arena_layout(s, mixed, nt_int, nt_ring, nt_pad, h->nparts);
+  const size_t off = L.total;
+  {
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess && off > free_b)
+      return bail(fail(CBNS_ERR_OUT_OF_MEMORY, "cbns_create: the block needs " + std::to_string(off) +
+                                                   " device bytes, " + std::to_string(free_b) + " are free"));
+    cudaGetLastError();
+  }
   std::vector<TileRef> t_int, t_ring, t_pad;
   append_tiles(t_int, 0, IM, JM, KM);
   append_tiles(t_ring, 0, s.rx, s.ry, s.rz);
@@ -238,15 +272,6 @@ cbns_status cbns_create(const cbns_params* p, uint32_t IM, uint32_t JM, uint32_t
   h->n_int = (int)t_int.size();
   h->n_ring = (int)t_ring.size();
   h->n_pad = (int)t_pad.size();
-  h->nparts = kDiagParts;
-
-  // Arena layout.  Both modes hold the binary64 state (Q, Q_p, staging) and
-  // binary64 primitives; binary64 solves add binary64 face/viscous fluxes,
-  // FP32-mixed solves the binary32 perturbation state, primitives and fluxes.
-  const bool mixed = precision == CBNS_FP32_MIXED;
-  s.mixed = mixed ? 1 : 0;
-  const ArenaLayout L = arena_layout(s, mixed, t_int.size(), t_ring.size(), t_pad.size(), h->nparts);
-  const size_t off = L.total;
   const size_t oQ = L.oQ, oQp = L.oQp, oStage = L.oStage, oPrim = L.oPrim, oU32 = L.oU32, oP32 = L.oP32;
   const size_t oCtl = L.oCtl, oDesc = L.oDesc, oTi = L.oTi, oTr = L.oTr, oTp = L.oTp, oPart = L.oPart,
                oOut = L.oOut;
@@ -642,6 +667,14 @@ cbns_status cbns_batch_create(cbns_handle* const* handles, int n, cbns_batch** o
     if (handles[i]->device != handles[0]->device || handles[i]->precision != handles[0]->precision)
       return fail(CBNS_ERR_INVALID_ARG, "cbns_batch_create: handles differ in device or precision");
   }
+  {
+    // A handle listed twice would put its tiles in the table twice: two CTAs
+    // would update the same cells and control block in every stage.
+    std::vector<cbns_handle*> sorted(handles, handles + n);
+    std::sort(sorted.begin(), sorted.end());
+    if (std::adjacent_find(sorted.begin(), sorted.end()) != sorted.end())
+      return fail(CBNS_ERR_INVALID_ARG, "cbns_batch_create: a handle appears more than once");
+  }
   cbns_batch* b = new cbns_batch();
   auto bail = [&](cbns_status st) {
     cbns_batch_destroy(b);
@@ -822,7 +855,8 @@ cbns_status cbns_batch_autotune(cbns_batch* b, int reps, double* ms_out, int cap
 
 cbns_status cbns_footprint(uint32_t IM, uint32_t JM, uint32_t KM, int precision, uint64_t* bytes) {
   if (!bytes) return fail(CBNS_ERR_INVALID_ARG, "cbns_footprint: null output");
-  if (IM < (uint32_t)NG || JM < (uint32_t)NG || KM < (uint32_t)NG) return fail(CBNS_ERR_BAD_DIMS, "cbns_footprint");
+  if (IM < (uint32_t)NG || JM < (uint32_t)NG || KM < (uint32_t)NG || !block_extents_ok(IM, JM, KM))
+    return fail(CBNS_ERR_BAD_DIMS, "cbns_footprint: every extent must be in [4, " + std::to_string(kMaxExtent) + "]");
   SolveDev s{};
   set_extents(s, IM, JM, KM);
   ArenaLayout L = arena_layout(s, precision == CBNS_FP32_MIXED, tile_count(IM, JM, KM),

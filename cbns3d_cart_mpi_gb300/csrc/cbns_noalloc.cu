@@ -39,8 +39,11 @@ constexpr int MAX_DEVICES = 64;
 
 static __device__ __align__(256) double g_noalloc_partials[4 * NOALLOC_MAX_CTAS];
 
-// Device address of g_noalloc_partials per device, looked up once per device
-// (with that device current) by the first call made on it.
+// Device address of g_noalloc_partials per device.  Every call made while its
+// stream is not being captured looks the address up again (with the device
+// current), so a context destroyed and recreated in between (cudaDeviceReset)
+// leaves no stale pointer behind; a call inside a stream capture uses the
+// address the last uncaptured call on that device found.
 double* g_scratch_ptr[MAX_DEVICES] = {nullptr};
 std::mutex g_scratch_mu;
 
@@ -175,12 +178,18 @@ extern "C" cbns_status cbns_diagnostics_noalloc(const double* Q_dev, uint32_t IM
                                            cudaGetErrorString(e));
   if (dev < 0 || dev >= MAX_DEVICES)
     return noalloc_fail(CBNS_ERR_NO_DEVICE, "cbns_diagnostics_noalloc: device index out of range");
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(st, &cap) != cudaSuccess) {
+    cudaGetLastError();
+    cap = cudaStreamCaptureStatusActive;  // unknown: keep to the address already found
+  }
   double* scratch = nullptr;
   {
-    // One-time set-up on this device (the device is current): the host-side name
+    // Set-up on this device (the device is current): the host-side name
     // g_noalloc_partials is not a device address, so look the address up.
     std::lock_guard<std::mutex> lock(g_scratch_mu);
-    if (!g_scratch_ptr[dev]) {
+    if (!g_scratch_ptr[dev] || cap == cudaStreamCaptureStatusNone) {
       void* p = nullptr;
       e = cudaGetSymbolAddress(&p, g_noalloc_partials);
       if (e != cudaSuccess)
@@ -190,7 +199,6 @@ extern "C" cbns_status cbns_diagnostics_noalloc(const double* Q_dev, uint32_t IM
     }
     scratch = g_scratch_ptr[dev];
   }
-  cudaStream_t st = (cudaStream_t)stream;
   k_noalloc_partials<<<(int)nctas, NOALLOC_THREADS, 0, st>>>(Q_dev, (int)IM, (int)JM, (int)KM, 1.0 / dx, 1.0 / dy,
                                                              1.0 / dz, scratch);
   k_noalloc_finish<<<1, 1024, 0, st>>>(scratch, (int)nctas, 1.0 / (double)ncell, out_dev);

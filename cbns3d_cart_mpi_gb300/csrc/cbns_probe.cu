@@ -1,4 +1,6 @@
 // cbns_probe.cu — pipe-throughput probes used as roofline denominators.
+// Built as its own library (lib/libcbns_probe.so) for the benchmark; the
+// product library does not contain it.
 //
 // The binary64 stencil kernels are bound by the FP64 pipe, whose peak no
 // vendor table gives for this part, so it is measured here: each thread runs
@@ -54,6 +56,8 @@ cbns_status probe(int iters, double* tflops) {
 
 }  // namespace
 
+// Measured FMA throughput of the current device in TFLOP/s (2 FLOPs per FMA),
+// binary64 when fp64 != 0 else binary32.
 extern "C" cbns_status cbns_probe_peak(int fp64, double* tflops) {
   if (!tflops) return CBNS_ERR_INVALID_ARG;
   return fp64 ? probe<double>(4096, tflops) : probe<float>(65536, tflops);

@@ -26,6 +26,7 @@
 #include <map>
 #include <memory>
 #include <mutex>
+#include <new>
 #include <string>
 #include <thread>
 #include <vector>
@@ -83,18 +84,28 @@ struct cbns_server {
 
 namespace {
 
-void retire(cbns_server* sv, Request* r, int status, const std::string& err) {
-  // Worker thread, without the lock: read results, free the solve.
+void retire(cbns_server* sv, Request* r, int status, std::string err) {
+  // Worker thread, without the lock: read results, free the solve.  A read that
+  // fails retires the request with that read's status and error text instead.
   if (r->h) {
     if (status == CBNS_OK || status == CBNS_ERR_NONPHYSICAL) {
       double dt_last = 0.0;
-      cbns_get_time(r->h, &r->t_final, &dt_last);
-      if (status == CBNS_OK) {
-        cbns_diagnostics(r->h, &r->ke, &r->enstrophy);
-        if (r->keep_state) {
-          r->result.resize((size_t)CBNS_NEQ * (r->IM + 2 * CBNS_NG) * (r->JM + 2 * CBNS_NG) * (r->KM + 2 * CBNS_NG));
-          cbns_download_Q(r->h, r->result.data());
+      cbns_status st = cbns_get_time(r->h, &r->t_final, &dt_last);
+      if (st == CBNS_OK && status == CBNS_OK) st = cbns_diagnostics(r->h, &r->ke, &r->enstrophy);
+      if (st == CBNS_OK && status == CBNS_OK && r->keep_state) {
+        try {
+          r->result.resize((size_t)CBNS_NEQ * (r->IM + 2 * CBNS_NG) * (r->JM + 2 * CBNS_NG) *
+                           (r->KM + 2 * CBNS_NG));
+          st = cbns_download_Q(r->h, r->result.data());
+        } catch (const std::bad_alloc&) {
+          st = CBNS_ERR_OUT_OF_MEMORY;
+          cbns::set_last_error("retire: no host memory for the final state");
         }
+      }
+      if (st != CBNS_OK) {
+        status = st;
+        err = cbns_last_error();
+        std::vector<double>().swap(r->result);
       }
     }
     cbns_destroy(r->h);
@@ -236,6 +247,11 @@ cbns_status serve_fail(cbns_status st, const std::string& msg) {
 }
 
 cbns_status submit(cbns_server* sv, Request* r, uint64_t* id) {
+  if (r->params.IM != r->IM || r->params.JM != r->JM || r->params.KM != r->KM) {
+    delete r;
+    return serve_fail(CBNS_ERR_BAD_DIMS, "cbns_server_submit: the extents must equal the grid's (p->IM, p->JM, "
+                                         "p->KM): one GPU holds the whole periodic grid");
+  }
   uint64_t fp = 0;
   cbns_status st = cbns_footprint(r->IM, r->JM, r->KM, sv->opts.precision, &fp);
   if (st != CBNS_OK) {

@@ -323,13 +323,6 @@ class Server:
         return {f: getattr(st, f) for f, _ in _lib.ServerStats._fields_}
 
 
-def probe_peak(fp64=True):
-    """Measured FMA throughput of the current GPU, TFLOP/s (2 FLOPs per FMA)."""
-    tf = ctypes.c_double()
-    _check(_lib.gpu().cbns_probe_peak(1 if fp64 else 0, ctypes.byref(tf)), "cbns_probe_peak")
-    return tf.value
-
-
 # --- host pieces (include/cbns_host.h) ----------------------------------------
 
 def read_input(path="input.txt"):

@@ -18,21 +18,26 @@ FLOPS_DT_PER_CELL = 31           # calc_dt, per cell (plus a data-dependent re-a
 NG, NGV = 4, 2
 
 
-def faces_per_direction(IM, JM, KM, d):
-    """Faces the reference computes per direction: (IM+1)*JM*KM for x, etc."""
+def faces_per_direction(IM, JM, KM, d, periodic=False):
+    """Faces per direction.  The reference computes (IM+1)*JM*KM for x (faces
+    -1/2 .. IM-1/2), etc.; on a periodic grid the last face is the first, so the
+    distinct faces (what the GPU computes) are IM*JM*KM (periodic=True)."""
     ext = [IM, JM, KM]
-    ext[d] += 1
+    if not periodic:
+        ext[d] += 1
     return ext[0] * ext[1] * ext[2]
 
 
-def kernel_flops(name, IM, JM, KM):
-    """Algorithmic FLOPs of one launch of the named kernel (one solve)."""
+def kernel_flops(name, IM, JM, KM, periodic=True):
+    """Algorithmic FLOPs of one launch of the named kernel (one solve): the
+    reference's op count per unit times the units, with the distinct periodic
+    faces by default (periodic=False counts the faces the reference computes)."""
     cells = IM * JM * KM
     ring = (IM + 2 * NGV) * (JM + 2 * NGV) * (KM + 2 * NGV)
     padded = (IM + 2 * NG) * (JM + 2 * NG) * (KM + 2 * NG)
     if name.startswith("inviscid_"):
         d = "xyz".index(name[-1])
-        return FLOPS_PER_FACE * faces_per_direction(IM, JM, KM, d)
+        return FLOPS_PER_FACE * faces_per_direction(IM, JM, KM, d, periodic)
     if name == "viscous":
         return (FLOPS_VISC_TERMS_PER_RING + FLOPS_VISC_FLUX_PER_RING) * ring
     if name == "update":
@@ -43,8 +48,10 @@ def kernel_flops(name, IM, JM, KM):
 
 
 def flops_per_step(IM, JM, KM):
-    """Algorithmic FLOPs of one RK3 step (3 stages + calc_dt)."""
-    stage = sum(kernel_flops(n, IM, JM, KM) for n in ("inviscid_x", "inviscid_y", "inviscid_z", "viscous", "update"))
+    """Algorithmic FLOPs of one RK3 step (3 stages + calc_dt), as the reference
+    executes it (its (N+1) N^2 faces per direction)."""
+    stage = sum(kernel_flops(n, IM, JM, KM, periodic=False)
+                for n in ("inviscid_x", "inviscid_y", "inviscid_z", "viscous", "update"))
     return 3 * stage + kernel_flops("dt_reduce", IM, JM, KM)
 
 
@@ -68,3 +75,16 @@ def mixed_update_bytes(IM, JM, KM):
     """Average compulsory bytes of one FP32-mixed update launch over the three stages."""
     return sum(MIXED_UPDATE_BYTES_PER_CELL.values()) / 3.0 * IM * JM * KM
 
+
+
+def probe_peak(fp64=True):
+    """Measured FMA throughput of the current GPU, TFLOP/s (2 FLOPs per FMA): the
+    pipe peak the roofline divides by (libcbns_probe.so, built beside the product
+    library but not part of it)."""
+    import ctypes
+    from . import _lib
+    tf = ctypes.c_double()
+    st = _lib.probe().cbns_probe_peak(1 if fp64 else 0, ctypes.byref(tf))
+    if st != 0:
+        raise RuntimeError("cbns_probe_peak failed with status %d" % st)
+    return tf.value

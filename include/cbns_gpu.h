@@ -283,10 +283,6 @@ typedef struct cbns_kernel_time {
 cbns_status cbns_profile_begin(cbns_handle* h);
 cbns_status cbns_profile_end(cbns_handle* h, cbns_kernel_time* out, int cap, int* n);
 
-/* Measured FMA throughput of the current device in TFLOP/s (2 FLOPs per FMA),
- * binary64 when fp64 != 0 else binary32: the pipe peaks the roofline uses. */
-cbns_status cbns_probe_peak(int fp64, double* tflops);
-
 /* No counterpart in the reference.  Kinetic energy and enstrophy, as
  * cbns_diagnostics computes them, of a conserved state the caller already holds
  * in its own device memory, computed without allocating anything.  For callers
@@ -302,7 +298,10 @@ cbns_status cbns_probe_peak(int fp64, double* tflops);
  * covering 16384 cells, so IM*JM*KM may be at most 67,108,864 (e.g. 406^3);
  * larger blocks are rejected with CBNS_ERR_BAD_DIMS.  The first call on a device
  * looks up the array's device address (cudaGetSymbolAddress) with that device
- * current; make that first call before any stream capture.  All calls share the
+ * current; make that first call before any stream capture.  Later calls outside
+ * a capture look it up again, so the address stays valid after a
+ * cudaDeviceReset; a call inside a capture uses the address found before the
+ * capture began.  All calls share the
  * one scratch array: calls whose kernels may overlap on the GPU (unordered
  * streams) race and must be serialised by the caller. */
 cbns_status cbns_diagnostics_noalloc(const double* Q_dev, uint32_t IM, uint32_t JM, uint32_t KM, double dx,

@@ -25,6 +25,7 @@ import os
 import shutil
 import subprocess
 import sys
+import tempfile
 
 import numpy as np
 
@@ -37,7 +38,9 @@ from cbns3d_cart_mpi_gb300.params import write_input_txt  # noqa: E402
 from oracle.build import build_ref  # noqa: E402
 from oracle.oracle import diagnostics, read_state, write_state  # noqa: E402
 
-WORK = os.path.join(ROOT, "_work", "golden_runs")
+# Run directories of the reference harness: a fresh temporary directory per
+# invocation of this script, removed by the operating system's temp cleanup.
+WORK = tempfile.mkdtemp(prefix="cbns_golden_runs_")
 
 
 def interior(Q):

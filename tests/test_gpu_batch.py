@@ -85,3 +85,15 @@ def test_each_solve_stops_at_its_own_t_end():
         t, _ = s.time()
         if te < 1:
             assert abs(t - te) < 1e-5 + 1e-15 and t + 1e-5 > te
+
+
+def test_batch_rejects_a_handle_listed_twice():
+    """A handle listed twice would put its tiles in the table twice, and two CTAs
+    would update the same cells and control block in every stage."""
+    from cbns3d_cart_mpi_gb300._abi import CBNS_ERR_INVALID_ARG
+    from cbns3d_cart_mpi_gb300.solver import Batch, CbnsError
+    solves = make("fp64")
+    with pytest.raises(CbnsError) as e:
+        Batch([solves[0], solves[1], solves[0]])
+    assert e.value.status == CBNS_ERR_INVALID_ARG
+    assert "more than once" in str(e.value)

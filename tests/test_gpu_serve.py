@@ -54,24 +54,46 @@ def test_device_initial_condition_matches_host():
     np.testing.assert_allclose(a.download_Q(), b.download_Q(), rtol=1e-14, atol=1e-15)
 
 
+# A request long enough (about 340 steps of 32^3) that later ones arrive while it runs.
+LONG = dict(N=32, JM=32, KM=32, Re=1200.0, Mach=0.1, t_end=1.0, seed=7)
+
+
 @pytest.mark.parametrize("precision", ["fp64", "fp32_mixed"])
 def test_results_same_alone_and_in_the_mix(precision):
+    """Two requests start; once the server has stepped them for a round, two more
+    arrive.  The late ones must be admitted after the first ones and before the
+    long one is done (their work overlaps on the device: at least three requests
+    active at once), and every result must be bitwise its solo result."""
     from cbns3d_cart_mpi_gb300.solver import Server
-    ref = [solo(r, precision) for r in REQS]
+    reqs = [LONG, REQS[1], REQS[2], REQS[3]]
+    ref = [solo(r, precision) for r in reqs]
     sv = Server(precision=precision, steps_per_round=7)
-    ids = [sv.submit_tgv(params(r), seed=r["seed"], amp=1e-3, nmodes=16, kmax=4, keep_state=True) for r in REQS[:2]]
-    time.sleep(0.05)  # the next two arrive while the first two run
+    ids = [sv.submit_tgv(params(r), seed=r["seed"], amp=1e-3, nmodes=16, kmax=4, keep_state=True)
+           for r in reqs[:2]]
+    t0 = time.time()
+    while sv.stats()["rounds"] < 1:  # the first two are on the device
+        assert time.time() - t0 < 60.0, "the server did not start a round"
+        time.sleep(0.001)
     ids += [sv.submit_tgv(params(r), seed=r["seed"], amp=1e-3, nmodes=16, kmax=4, keep_state=True)
-            for r in REQS[2:]]
-    for rid, r, (Qref, nref) in zip(ids, REQS, ref):
+            for r in reqs[2:]]
+    infos = []
+    for rid, r, (Qref, nref) in zip(ids, reqs, ref):
         info = sv.wait(rid, timeout=120.0)
         assert info["status"] == CBNS_OK, info
         assert info["steps"] == nref
         assert abs(info["t_final"] - r["t_end"]) < 1e-5 + 1e-15
         Q = sv.result(rid, shape(params(r)))
         assert np.array_equal(Q, Qref), r
+        infos.append(info)
+    long_info = infos[0]
+    for late in infos[2:]:
+        assert long_info["admit_s"] < late["admit_s"] < long_info["done_s"], (long_info, late)
     st = sv.stats()
+    assert st["peak_active"] >= 3, st
     assert st["completed"] == 4 and st["failed"] == 0
+    print(precision, "long request admitted %.4f done %.4f; late requests admitted %s; peak active %d" % (
+        long_info["admit_s"], long_info["done_s"], [round(x["admit_s"], 4) for x in infos[2:]],
+        st["peak_active"]))
     sv.close()
 
 

@@ -264,3 +264,42 @@ def test_opcount_constants_match_record(golden_dir):
     assert rec["calc_primitive_per_padded_cell"] == w.FLOPS_PRIM_PER_PADDED
     assert round(rec["calc_dt_per_cell"]) == w.FLOPS_DT_PER_CELL
     assert abs(w.flops_per_step(256, 256, 256) / 256 ** 3 - 15198.25) < 0.1
+
+
+def test_block_size_limit_follows_memory_not_a_31_bit_index():
+    """Offsets are 64-bit, so a block is limited by device memory (cbns_create
+    compares cbns_footprint's arena size with the free bytes) and by the 16-bit
+    tile coordinates, not by 5 (N+8)^3 < 2^31 (N ~ 745).  The arena of a 768^3
+    block fits the 280 GB a GB300 offers in both precisions, 1024^3 does not."""
+    from cbns3d_cart_mpi_gb300.solver import CbnsError, footprint
+    hbm = 280e9
+    per_cell = {}
+    for prec in ("fp64", "fp32_mixed"):
+        fp768 = footprint(768, 768, 768, prec)
+        assert fp768 < hbm, (prec, fp768)
+        assert footprint(1024, 1024, 1024, prec) > hbm
+        per_cell[prec] = fp768 / 776 ** 3
+        # grows with the padded volume: about 380 bytes per padded cell
+        assert 300 < per_cell[prec] < 420, per_cell
+    # 745^3 and 746^3 straddle the old 31-bit limit; both are accepted now.
+    assert footprint(746, 746, 746) > footprint(745, 745, 745)
+    # Tile coordinates are 16-bit: 65535 - 2 NG cells along an axis is the most.
+    footprint(65527, 4, 4)
+    with pytest.raises(CbnsError):
+        footprint(65528, 4, 4)
+    with pytest.raises(CbnsError):
+        footprint(4, 4, 70000)
+
+
+def test_create_rejects_block_extents_other_than_the_grid():
+    """One GPU holds the whole periodic grid: cbns_create takes the spacing from
+    p->IM/JM/KM and the periodic images from the block's extents, so the two must
+    agree.  The check runs before any device call, so it answers on a host
+    without a GPU too."""
+    from cbns3d_cart_mpi_gb300 import _lib
+    from cbns3d_cart_mpi_gb300._abi import CBNS_ERR_BAD_DIMS
+    p = tgv_params(16, JM=12, KM=20)
+    h = ctypes.c_void_p()
+    st = _lib.gpu().cbns_create(ctypes.byref(p), 16, 12, 21, 0, ctypes.byref(h))
+    assert st == CBNS_ERR_BAD_DIMS and not h.value
+    assert "whole periodic grid" in _lib.last_error()

@@ -9,6 +9,8 @@ through the C ABI and checks both results against cbns_diagnostics (the
 handle-based entry point) to the 1e-13 relative tolerance the diagnostics tests
 use.  The output is poisoned with NaN before each call, so each call must write
 it; the second call also exercises the scratch array left over from the first.
+Free device memory (cudaMemGetInfo) is the same before and after further calls
+made once the first call has set up its device, so the calls allocate nothing.
 """
 import ctypes
 import math
@@ -42,7 +44,8 @@ def test_noalloc_diagnostics_matches_handle_entry_point():
     stream = torch.cuda.current_stream(dev)
     dx, dy, dz = 2.0 * math.pi / IM, 2.0 * math.pi / JM, 2.0 * math.pi / KM
     lib = _lib.gpu()
-    for call in range(2):
+
+    def call_and_check(call):
         out_dev.fill_(float("nan"))
         st = lib.cbns_diagnostics_noalloc(ctypes.c_void_p(Q_dev.data_ptr()), IM, JM, KM, dx, dy, dz,
                                           ctypes.c_void_p(out_dev.data_ptr()), ctypes.c_void_p(stream.cuda_stream))
@@ -51,6 +54,17 @@ def test_noalloc_diagnostics_matches_handle_entry_point():
         ke, en = out_dev.tolist()
         assert abs(ke - ke_ref) <= 1e-13 * abs(ke_ref), (call, ke, ke_ref)
         assert abs(en - en_ref) <= 1e-13 * abs(en_ref), (call, en, en_ref)
+
+    for call in range(2):
+        call_and_check(call)
+    # The device is set up (symbol address looked up, kernels loaded): further
+    # calls must leave free device memory unchanged.
+    torch.cuda.synchronize()
+    free_before = torch.cuda.mem_get_info(dev)[0]
+    for call in range(2, 6):
+        call_and_check(call)
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info(dev)[0] == free_before
 
 
 def test_noalloc_diagnostics_rejects_what_it_cannot_hold():
