@@ -13,10 +13,10 @@ ours:       W untimed steps, then K steps timed with CUDA events on the solve's
                 giving the dominant kernel's roofline against the FP64 FMA peak
                 measured live by cbns_probe_peak;
               * e2e: K steps through the C ABI with host buffers: upload Q from
-                pinned memory, one step, download Q, every step, on two handles
-                driven by two host threads, K steps each (one handle's copies
-                overlap the other's kernels); the one-handle sequential loop of
-                K steps beside it;
+                pinned memory, one step, download Q, every step, through the
+                asynchronous entry points of one handle (copies on its second
+                stream under the neighbouring steps' kernels); the synchronous
+                calls timed beside it;
               * cpu_baseline: the oracle's CPU restatement of the reference (all
                 host threads) on a bounded sample of the same workload.
 reference:  the reference algorithm on the host cores (the oracle's restatement,
@@ -31,7 +31,6 @@ import statistics
 import subprocess
 import sys
 import tempfile
-import threading
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
@@ -53,6 +52,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-mixed", action="store_true", help="skip the FP32-mixed leg")
+    ap.add_argument("--no-large", action="store_true", help="skip the 512^3 / 768^3 FP32-mixed blocks")
     return ap.parse_args()
 
 
@@ -381,47 +381,67 @@ def run_ours(args, rank, world, local):
 
     # e2e: host buffers through the C ABI, copies inside the timed region.  Every
     # step uploads its input state from pinned host memory, steps, and downloads
-    # its result.  Each C-ABI call synchronises its handle's stream, so two
-    # handles on two host threads, K steps each, keep one handle's copies in
-    # flight under the other's kernels; the one-handle sequential loop of K steps
-    # is reported beside it.
+    # its result, through the asynchronous entry points of one handle: the copies
+    # run on the handle's second stream under the neighbouring steps' kernels, and
+    # the timed region ends when cbns_wait has seen the last download land.  The
+    # synchronous calls (each waits for its own copy) are timed beside it.
     if not args.no_e2e:
         n = int(np.prod(s.shape))
-        s2 = Solver(p)
-        pinned = [torch.empty(n, dtype=torch.float64, pin_memory=True).numpy() for _ in range(4)]
-        jobs = [(s, pinned[0], pinned[1]), (s2, pinned[2], pinned[3])]
-        for h, hin, hout in jobs:
-            hin[:] = Q0.reshape(-1)
-            h.upload_Q(hin, 0.0)
-            h.step()
-            h.download_Q(out=hout.reshape(h.shape))
-
-        def e2e_steps(h, hin, hout, k):
-            for _ in range(k):
-                h.upload_Q(hin, 0.0)
-                h.step()
-                h.download_Q(out=hout.reshape(h.shape))
-
+        hin, hout = s.pinned_state(), s.pinned_state()
+        hin[...] = Q0
+        s.upload_Q_async(hin, 0.0)
+        s.step_async()
+        s.download_Q_async(hout)
+        s.wait()
         barrier(world)
         t0 = time.perf_counter()
-        e2e_steps(s, pinned[0], pinned[1], args.steps)
-        seq = reduce_max(time.perf_counter() - t0, world)
-        barrier(world)
-        threads = [threading.Thread(target=e2e_steps, args=(h, hin, hout, args.steps)) for h, hin, hout in jobs]
-        t0 = time.perf_counter()
-        for t in threads:
-            t.start()
-        for t in threads:
-            t.join()
+        for _ in range(args.steps):
+            s.upload_Q_async(hin, 0.0)
+            s.step_async()
+            s.download_Q_async(hout)
+        s.wait()
         sec = reduce_max(time.perf_counter() - t0, world)
-        s2.close()
+        barrier(world)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            s.upload_Q(hin, 0.0)
+            s.step()
+            s.download_Q(out=hout)
+        seq = reduce_max(time.perf_counter() - t0, world)
         if rank == 0:
-            line["e2e"] = {"value": world * cells * 2 * args.steps / sec, "unit": UNIT,
+            line["e2e"] = {"value": world * cells * args.steps / sec, "unit": UNIT,
                            "h2d_bytes_per_step": n * 8, "d2h_bytes_per_step": n * 8,
-                           "path": "cbns_upload_Q (pinned) + cbns_step + cbns_download_Q (pinned), per step; "
-                                   "two handles on two host threads, %d steps each" % args.steps,
-                           "sequential_one_handle": world * cells * args.steps / seq}
+                           "path": "cbns_upload_Q_async (pinned) + cbns_step_async + cbns_download_Q_async (pinned) "
+                                   "per step on one handle, %d steps, then cbns_wait" % args.steps,
+                           "synchronous_calls": world * cells * args.steps / seq}
     s.close()
+
+    # Blocks above the old 31-bit-index limit (N ~ 745): FP32-mixed at 512^3 and
+    # 768^3 (about 195 GB of device memory), state built on the device.
+    if not args.no_large and rank == 0:
+        large = []
+        for NL in (512, 768):
+            pl = tgv_params(NL, t_end=2.0)
+            try:
+                sl = Solver(pl, precision="fp32_mixed")
+            except Exception as e:  # not enough device memory on this GPU
+                large.append({"N": NL, "skipped": str(e)[:200]})
+                continue
+            sl.init_tgv()
+            lstream = torch.cuda.ExternalStream(sl.stream)
+            sl.run(2)
+            torch.cuda.synchronize()
+            l0 = torch.cuda.Event(enable_timing=True)
+            l1 = torch.cuda.Event(enable_timing=True)
+            l0.record(lstream)
+            nl = sl.run(3)
+            l1.record(lstream)
+            l1.synchronize()
+            lms = l0.elapsed_time(l1) / nl
+            large.append({"N": NL, "precision": "fp32_mixed", "steps": nl, "ms_per_step": lms,
+                          "value": NL ** 3 / (lms * 1e-3), "device_bytes": sl.info()["device_bytes"]})
+            sl.close()
+        line["large_blocks"] = large
 
     if rank == 0 and world == 1 and not args.no_cpu_baseline:  # the host baseline is an N=1 figure
         v, th, sec = cpu_sample(N, args.cpu_steps)

@@ -64,6 +64,11 @@ GPU_API = {
     "cbns_stage": (c_int, [c_vp, c_d, c_int]),
     "cbns_step": (c_int, [c_vp, c_d, c_dp, c_dp]),
     "cbns_run": (c_int, [c_vp, c_u32, c_d, ctypes.POINTER(c_u32)]),
+    "cbns_upload_Q_async": (c_int, [c_vp, c_vp, c_d]),
+    "cbns_step_async": (c_int, [c_vp, c_d]),
+    "cbns_download_Q_async": (c_int, [c_vp, c_vp]),
+    "cbns_wait": (c_int, [c_vp, c_dp, c_dp]),
+    "cbns_poll": (c_int, [c_vp, ctypes.POINTER(c_int)]),
     "cbns_get_time": (c_int, [c_vp, c_dp, c_dp]),
     "cbns_diagnostics": (c_int, [c_vp, c_dp, c_dp]),
     "cbns_check_state": (c_int, [c_vp]),

@@ -29,8 +29,9 @@ cudaError_t launch_dt(const SolveDev* d, int nsolves, const TileRef* tiles, int 
 cudaError_t launch_dt_raw(const SolveDev* d, int sidx, const TileRef* tiles, int ntiles, double* out,
                           bool mixed, const LaunchCfg& cfg, cudaStream_t st, Profiler* pf);
 cudaError_t launch_set_dt(const SolveDev* d, int sidx, double dt, cudaStream_t st);
-cudaError_t launch_stage(const SolveDev* d, const TileRef* tiles, int ntiles, const TileRef* ring_tiles,
-                         int nring, int stage, const LaunchCfg& cfg, bool mixed, cudaStream_t st, Profiler* pf);
+cudaError_t launch_reset_ctl(SolveCtl* ctl, double t, double t_end, cudaStream_t st);
+cudaError_t launch_stage(const SolveDev* d, const StageTables& T, int stage, const LaunchCfg& cfg, bool mixed,
+                         cudaStream_t st, Profiler* pf);
 cudaError_t launch_diag(const SolveDev* d, int sidx, const TileRef* tiles, int ntiles, double* partials,
                         int nparts, double inv_n, double* out, cudaStream_t st, Profiler* pf);
 }  // namespace cbns
@@ -82,10 +83,47 @@ size_t tile_count(long long ex, long long ey, long long ez, int rows = TILE_Y) {
   return (size_t)((ex + TILE_X - 1) / TILE_X) * (size_t)((ey + rows - 1) / rows) * (size_t)ez;
 }
 
+// Face columns of the face kernels for direction D of a block: the extent
+// along D cut into ceil(E / faces) columns of near-equal length, for every
+// block of 32 lines and every position of the third axis.  Entries of one
+// warp-group (CTA) are neighbouring line blocks of one column position.
+int march_faces_per_column() {
+  static int n = 0;
+  if (n == 0) {
+    const char* e = std::getenv("CBNS_MARCH_FACES");
+    n = e ? std::atoi(e) : kMarchFaces;
+    if (n < 1 || n > 65535) n = kMarchFaces;
+  }
+  return n;
+}
+
+size_t march_count(int D, long long IM, long long JM, long long KM) {
+  const long long lines = D == 0 ? JM : IM, E = D == 0 ? IM : (D == 1 ? JM : KM), third = D == 2 ? JM : KM;
+  const long long per = march_faces_per_column();
+  return (size_t)((lines + 31) / 32) * (size_t)((E + per - 1) / per) * (size_t)third;
+}
+
+void append_march(std::vector<MarchRef>& out, int solve, int D, int IM, int JM, int KM) {
+  const int lines = D == 0 ? JM : IM, E = D == 0 ? IM : (D == 1 ? JM : KM), third = D == 2 ? JM : KM;
+  const int per = march_faces_per_column();
+  const int ncol = (E + per - 1) / per;
+  const int base = E / ncol, extra = E % ncol;
+  const int nblk = (lines + 31) / 32;
+  for (int c = 0; c < third; ++c) {
+    int first = 0;
+    for (int q = 0; q < ncol; ++q) {
+      const int count = base + (q < extra ? 1 : 0);
+      for (int b = 0; b < nblk; ++b)
+        out.push_back(MarchRef{(uint16_t)solve, (uint16_t)b, (uint16_t)c, (uint16_t)first, (uint16_t)count, 0});
+      first += count;
+    }
+  }
+}
+
 // Byte offsets of everything a solve's arena holds (see cbns_create).
 struct ArenaLayout {
-  size_t oQ, oQp, oStage, oPrim, oF[3], oTv, oFf[3], oTv32, oU32, oP32, oCtl, oDesc, oTi, oTr, oTp, oPart, oOut,
-      total;
+  size_t oQ, oQp, oStage, oPrim, oF[3], oTv, oFf[3], oTv32, oU32, oP32, oCtl, oDesc, oTi, oTr, oTp, oM[3], oPart,
+      oOut, total;
 };
 
 ArenaLayout arena_layout(const SolveDev& s, bool mixed, size_t n_int, size_t n_ring, size_t n_pad, int nparts) {
@@ -115,6 +153,7 @@ ArenaLayout arena_layout(const SolveDev& s, bool mixed, size_t n_int, size_t n_r
   L.oTi = take(sizeof(TileRef) * n_int);
   L.oTr = take(sizeof(TileRef) * n_ring);
   L.oTp = take(sizeof(TileRef) * n_pad);
+  for (int d = 0; d < 3; ++d) L.oM[d] = take(sizeof(MarchRef) * march_count(d, s.IM, s.JM, s.KM));
   L.oPart = take(sizeof(double) * 4 * nparts);
   L.oOut = take(sizeof(double) * 8);
   L.total = off;
@@ -172,7 +211,14 @@ cbns_status cbns_destroy(cbns_handle* h) {
   if (!h) return CBNS_OK;
   cudaSetDevice(h->device);
   if (h->stream) cudaStreamSynchronize(h->stream);
+  if (h->up_stream) cudaStreamSynchronize(h->up_stream);
+  if (h->down_stream) cudaStreamSynchronize(h->down_stream);
   if (h->step_graph) cudaGraphExecDestroy(h->step_graph);
+  if (h->d_stage_out) cudaFree(h->d_stage_out);
+  for (cudaEvent_t ev : {h->ev_in_ready, h->ev_in_free, h->ev_out_ready, h->ev_out_free})
+    if (ev) cudaEventDestroy(ev);
+  if (h->up_stream) cudaStreamDestroy(h->up_stream);
+  if (h->down_stream) cudaStreamDestroy(h->down_stream);
   if (h->arena) cudaFree(h->arena);
   if (h->h_ctl) cudaFreeHost(h->h_ctl);
   if (h->h_out) cudaFreeHost(h->h_out);
@@ -272,6 +318,11 @@ cbns_status cbns_create(const cbns_params* p, uint32_t IM, uint32_t JM, uint32_t
   h->n_int = (int)t_int.size();
   h->n_ring = (int)t_ring.size();
   h->n_pad = (int)t_pad.size();
+  std::vector<MarchRef> t_march[3];
+  for (int d = 0; d < 3; ++d) {
+    append_march(t_march[d], 0, d, IM, JM, KM);
+    h->n_march[d] = (int)t_march[d].size();
+  }
   const size_t oQ = L.oQ, oQp = L.oQp, oStage = L.oStage, oPrim = L.oPrim, oU32 = L.oU32, oP32 = L.oP32;
   const size_t oCtl = L.oCtl, oDesc = L.oDesc, oTi = L.oTi, oTr = L.oTr, oTp = L.oTp, oPart = L.oPart,
                oOut = L.oOut;
@@ -344,6 +395,7 @@ cbns_status cbns_create(const cbns_params* p, uint32_t IM, uint32_t JM, uint32_t
   h->d_tiles_int = (TileRef*)(A + oTi);
   h->d_tiles_ring = (TileRef*)(A + oTr);
   h->d_tiles_pad = (TileRef*)(A + oTp);
+  for (int d = 0; d < 3; ++d) h->d_march[d] = (MarchRef*)(A + L.oM[d]);
   h->d_partials = (double*)(A + oPart);
   h->d_out = (double*)(A + oOut);
 
@@ -362,6 +414,10 @@ cbns_status cbns_create(const cbns_params* p, uint32_t IM, uint32_t JM, uint32_t
                            h->stream)) != cudaSuccess ||
       (e = cudaMemcpyAsync(h->d_ctl, h->h_ctl, sizeof(SolveCtl), cudaMemcpyHostToDevice, h->stream)) != cudaSuccess)
     return bail(cuda_fail(e, "cudaMemcpyAsync(setup)"));
+  for (int d = 0; d < 3; ++d)
+    if ((e = cudaMemcpyAsync(h->d_march[d], t_march[d].data(), sizeof(MarchRef) * t_march[d].size(),
+                             cudaMemcpyHostToDevice, h->stream)) != cudaSuccess)
+      return bail(cuda_fail(e, "cudaMemcpyAsync(setup)"));
   if ((e = cudaStreamSynchronize(h->stream)) != cudaSuccess) return bail(cuda_fail(e, "cudaStreamSynchronize"));
   *out = h;
   return CBNS_OK;
@@ -453,8 +509,9 @@ cbns_status cbns_calc_dt(cbns_handle* h, double* dt) {
 }
 
 static cbns_status enqueue_stage(cbns_handle* h, int stage) {
-  CBNS_CUDA(launch_stage(h->d_desc, h->d_tiles_int, h->n_int, h->d_tiles_ring, h->n_ring, stage, LaunchCfg{},
-                         h->desc.mixed != 0, h->stream, h->pf()));
+  const StageTables T{h->d_tiles_int, h->n_int, h->d_tiles_ring, h->n_ring,
+                      {h->d_march[0], h->d_march[1], h->d_march[2]}, {h->n_march[0], h->n_march[1], h->n_march[2]}};
+  CBNS_CUDA(launch_stage(h->d_desc, T, stage, LaunchCfg{}, h->desc.mixed != 0, h->stream, h->pf()));
   return CBNS_OK;
 }
 
@@ -490,6 +547,27 @@ cbns_status cbns_step(cbns_handle* h, double t_end, double* dt_out, double* t_ou
   return h->h_ctl->active ? CBNS_OK : CBNS_FINISHED;
 }
 
+// The step of enqueue_step captured as a CUDA graph for this t_end (rebuilt when
+// t_end changes).
+static cbns_status ensure_step_graph(cbns_handle* h, double t_end) {
+  if (h->step_graph && h->graph_t_end == t_end) return CBNS_OK;
+  if (h->step_graph) {
+    cudaGraphExecDestroy(h->step_graph);
+    h->step_graph = nullptr;
+  }
+  cudaGraph_t g;
+  CBNS_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+  cbns_status st = enqueue_step(h, t_end, true);
+  cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+  if (st != CBNS_OK) return st;
+  if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+  e = cudaGraphInstantiate(&h->step_graph, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+  h->graph_t_end = t_end;
+  return CBNS_OK;
+}
+
 cbns_status cbns_run(cbns_handle* h, uint32_t nsteps, double t_end, uint32_t* steps_done) {
   cbns_status st = check_handle(h, "cbns_run");
   if (st != CBNS_OK) return st;
@@ -500,21 +578,8 @@ cbns_status cbns_run(cbns_handle* h, uint32_t nsteps, double t_end, uint32_t* st
     // Profiling: direct launches, each bracketed by events.
     for (uint32_t n = 0; n < nsteps; ++n)
       if ((st = enqueue_step(h, t_end, true)) != CBNS_OK) return st;
-  } else if (!h->step_graph || h->graph_t_end != t_end) {
-    if (h->step_graph) {
-      cudaGraphExecDestroy(h->step_graph);
-      h->step_graph = nullptr;
-    }
-    cudaGraph_t g;
-    CBNS_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-    st = enqueue_step(h, t_end, true);
-    cudaError_t e = cudaStreamEndCapture(h->stream, &g);
-    if (st != CBNS_OK) return st;
-    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
-    e = cudaGraphInstantiate(&h->step_graph, g, 0);
-    cudaGraphDestroy(g);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
-    h->graph_t_end = t_end;
+  } else if ((st = ensure_step_graph(h, t_end)) != CBNS_OK) {
+    return st;
   }
   if (!h->prof.on)
     for (uint32_t n = 0; n < nsteps; ++n) CBNS_CUDA(cudaGraphLaunch(h->step_graph, h->stream));
@@ -522,6 +587,110 @@ cbns_status cbns_run(cbns_handle* h, uint32_t nsteps, double t_end, uint32_t* st
   CBNS_CUDA(cudaStreamSynchronize(h->stream));
   if (steps_done) *steps_done = h->h_ctl->steps - start;
   if (h->h_ctl->status) return fail(CBNS_ERR_NONPHYSICAL, "cbns_run: non-physical state (rho <= 0, p <= 0 or NaN)");
+  return CBNS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Asynchronous entry points.  Work goes to three streams of the handle: kernels
+// on h->stream, host-to-device copies on h->up_stream and device-to-host copies
+// on h->down_stream, ordered by events, through two staging buffers (uploads
+// through d_stage, downloads through d_stage_out).  The upload of the next
+// state then runs under the current step's kernels, and the download of a
+// result under the next step's.
+
+static cbns_status ensure_async(cbns_handle* h) {
+  if (h->down_stream) return CBNS_OK;
+  const size_t bytes = sizeof(double) * NEQ * (size_t)h->desc.V;
+  cudaError_t e = cudaMalloc(&h->d_stage_out, bytes);
+  if (e != cudaSuccess) {
+    h->d_stage_out = nullptr;
+    return cuda_fail(e, "cudaMalloc(download staging)");
+  }
+  h->arena_bytes += bytes;
+  for (cudaEvent_t* ev : {&h->ev_in_ready, &h->ev_in_free, &h->ev_out_ready, &h->ev_out_free})
+    CBNS_CUDA(cudaEventCreateWithFlags(ev, cudaEventDisableTiming));
+  CBNS_CUDA(cudaStreamCreateWithFlags(&h->up_stream, cudaStreamNonBlocking));
+  CBNS_CUDA(cudaStreamCreateWithFlags(&h->down_stream, cudaStreamNonBlocking));
+  // Both staging buffers start free.
+  CBNS_CUDA(cudaEventRecord(h->ev_in_free, h->stream));
+  CBNS_CUDA(cudaEventRecord(h->ev_out_free, h->stream));
+  return CBNS_OK;
+}
+
+cbns_status cbns_upload_Q_async(cbns_handle* h, const double* Q, double t) {
+  cbns_status st = check_handle(h, "cbns_upload_Q_async");
+  if (st != CBNS_OK) return st;
+  if (!Q) return fail(CBNS_ERR_INVALID_ARG, "cbns_upload_Q_async: null Q");
+  if ((st = ensure_async(h)) != CBNS_OK) return st;
+  const SolveDev& s = h->desc;
+  // upload stream: wait until the last upload's transpose has read the staging
+  // buffer, then copy the host state into it
+  CBNS_CUDA(cudaStreamWaitEvent(h->up_stream, h->ev_in_free, 0));
+  CBNS_CUDA(cudaMemcpyAsync(h->d_stage, Q, sizeof(double) * NEQ * (size_t)s.V, cudaMemcpyHostToDevice,
+                            h->up_stream));
+  CBNS_CUDA(cudaEventRecord(h->ev_in_ready, h->up_stream));
+  // compute stream: the start-up sequence of cbns_upload_Q once the copy is in
+  CBNS_CUDA(cudaStreamWaitEvent(h->stream, h->ev_in_ready, 0));
+  CBNS_CUDA(launch_layout(h->d_desc, 0, h->d_stage, s.Q, true, s.V, h->stream, nullptr));
+  CBNS_CUDA(cudaEventRecord(h->ev_in_free, h->stream));
+  CBNS_CUDA(launch_prepare(h->d_desc, h->d_tiles_pad, h->n_pad, h->stream, nullptr));
+  CBNS_CUDA(launch_reset_ctl(h->d_ctl, t, h->params.t_end, h->stream));
+  return CBNS_OK;
+}
+
+cbns_status cbns_step_async(cbns_handle* h, double t_end) {
+  cbns_status st = check_handle(h, "cbns_step_async");
+  if (st != CBNS_OK) return st;
+  if ((st = ensure_step_graph(h, t_end)) != CBNS_OK) return st;
+  CBNS_CUDA(cudaGraphLaunch(h->step_graph, h->stream));
+  return CBNS_OK;
+}
+
+cbns_status cbns_download_Q_async(cbns_handle* h, double* Q) {
+  cbns_status st = check_handle(h, "cbns_download_Q_async");
+  if (st != CBNS_OK) return st;
+  if (!Q) return fail(CBNS_ERR_INVALID_ARG, "cbns_download_Q_async: null output");
+  if ((st = ensure_async(h)) != CBNS_OK) return st;
+  const SolveDev& s = h->desc;
+  // compute stream: wait until the last download has left the staging buffer,
+  // then transpose the current state into it
+  CBNS_CUDA(cudaStreamWaitEvent(h->stream, h->ev_out_free, 0));
+  CBNS_CUDA(launch_layout(h->d_desc, 0, s.Q, h->d_stage_out, false, s.V, h->stream, nullptr));
+  CBNS_CUDA(cudaEventRecord(h->ev_out_ready, h->stream));
+  // download stream: the device-to-host copy, overlapping later kernels
+  CBNS_CUDA(cudaStreamWaitEvent(h->down_stream, h->ev_out_ready, 0));
+  CBNS_CUDA(cudaMemcpyAsync(Q, h->d_stage_out, sizeof(double) * NEQ * (size_t)s.V, cudaMemcpyDeviceToHost,
+                            h->down_stream));
+  CBNS_CUDA(cudaEventRecord(h->ev_out_free, h->down_stream));
+  return CBNS_OK;
+}
+
+cbns_status cbns_wait(cbns_handle* h, double* dt_last, double* t_cur) {
+  cbns_status st = check_handle(h, "cbns_wait");
+  if (st != CBNS_OK) return st;
+  CBNS_CUDA(cudaMemcpyAsync(h->h_ctl, h->d_ctl, sizeof(SolveCtl), cudaMemcpyDeviceToHost, h->stream));
+  CBNS_CUDA(cudaStreamSynchronize(h->stream));
+  if (h->up_stream) CBNS_CUDA(cudaStreamSynchronize(h->up_stream));
+  if (h->down_stream) CBNS_CUDA(cudaStreamSynchronize(h->down_stream));
+  if (dt_last) *dt_last = h->h_ctl->dt;
+  if (t_cur) *t_cur = h->h_ctl->t_cur;
+  if (h->h_ctl->status) return fail(CBNS_ERR_NONPHYSICAL, "cbns_wait: non-physical state (rho <= 0, p <= 0 or NaN)");
+  return h->h_ctl->active ? CBNS_OK : CBNS_FINISHED;
+}
+
+cbns_status cbns_poll(cbns_handle* h, int* done) {
+  cbns_status st = check_handle(h, "cbns_poll");
+  if (st != CBNS_OK) return st;
+  if (!done) return fail(CBNS_ERR_INVALID_ARG, "cbns_poll: null output");
+  cudaError_t e = cudaStreamQuery(h->stream);
+  if (e == cudaSuccess && h->up_stream) e = cudaStreamQuery(h->up_stream);
+  if (e == cudaSuccess && h->down_stream) e = cudaStreamQuery(h->down_stream);
+  if (e == cudaErrorNotReady) {
+    *done = 0;
+    return CBNS_OK;
+  }
+  if (e != cudaSuccess) return cuda_fail(e, "cbns_poll");
+  *done = 1;
   return CBNS_OK;
 }
 
@@ -618,9 +787,10 @@ static cbns_status batch_enqueue_step(cbns_batch* b) {
   const int ri = rows_index(b->cfg.tile_rows);
   const int n = (int)b->handles.size();
   CBNS_CUDA(launch_dt(b->d_descs, n, b->d_int[ri], b->n_int[ri], 0.0, false, b->mixed, b->cfg, b->stream, nullptr));
+  const StageTables T{b->d_int[ri], b->n_int[ri], b->d_ring[ri], b->n_ring[ri],
+                      {b->d_march[0], b->d_march[1], b->d_march[2]}, {b->n_march[0], b->n_march[1], b->n_march[2]}};
   for (int st = 1; st <= 3; ++st)
-    CBNS_CUDA(launch_stage(b->d_descs, b->d_int[ri], b->n_int[ri], b->d_ring[ri], b->n_ring[ri], st, b->cfg,
-                           b->mixed, b->stream, nullptr));
+    CBNS_CUDA(launch_stage(b->d_descs, T, st, b->cfg, b->mixed, b->stream, nullptr));
   return CBNS_OK;
 }
 
@@ -691,12 +861,14 @@ cbns_status cbns_batch_create(cbns_handle* const* handles, int n, cbns_batch** o
     return bail(cuda_fail(e, "cudaStreamCreate(batch)"));
   std::vector<SolveDev> descs(n);
   std::vector<TileRef> ti[3], tr[3];
+  std::vector<MarchRef> tm[3];
   for (int i = 0; i < n; ++i) {
     const SolveDev& s = handles[i]->desc;
     descs[i] = s;
     for (int r = 0; r < 3; ++r) {
       append_tiles(ti[r], i, s.IM, s.JM, s.KM, kRowsOptions[r]);
       append_tiles(tr[r], i, s.rx, s.ry, s.rz, kRowsOptions[r]);
+      append_march(tm[r], i, r, s.IM, s.JM, s.KM);  // r: direction
     }
   }
   size_t off = 0;
@@ -705,10 +877,11 @@ cbns_status cbns_batch_create(cbns_handle* const* handles, int n, cbns_batch** o
     off += align_up(bytes);
     return o;
   };
-  size_t oD = take(sizeof(SolveDev) * n), oI[3], oR[3];
+  size_t oD = take(sizeof(SolveDev) * n), oI[3], oR[3], oM[3];
   for (int r = 0; r < 3; ++r) {
     oI[r] = take(sizeof(TileRef) * ti[r].size());
     oR[r] = take(sizeof(TileRef) * tr[r].size());
+    oM[r] = take(sizeof(MarchRef) * tm[r].size());
   }
   if ((e = cudaMalloc(&b->arena, off)) != cudaSuccess) return bail(cuda_fail(e, "cudaMalloc(batch)"));
   b->d_descs = (SolveDev*)(b->arena + oD);
@@ -720,6 +893,11 @@ cbns_status cbns_batch_create(cbns_handle* const* handles, int n, cbns_batch** o
     b->d_ring[r] = (TileRef*)(b->arena + oR[r]);
     b->n_int[r] = (int)ti[r].size();
     b->n_ring[r] = (int)tr[r].size();
+    b->d_march[r] = (MarchRef*)(b->arena + oM[r]);
+    b->n_march[r] = (int)tm[r].size();
+    if ((e = cudaMemcpyAsync(b->d_march[r], tm[r].data(), sizeof(MarchRef) * tm[r].size(), cudaMemcpyHostToDevice,
+                             b->stream)) != cudaSuccess)
+      return bail(cuda_fail(e, "cudaMemcpyAsync(batch columns)"));
     if ((e = cudaMemcpyAsync(b->d_int[r], ti[r].data(), sizeof(TileRef) * ti[r].size(), cudaMemcpyHostToDevice,
                              b->stream)) != cudaSuccess ||
         (e = cudaMemcpyAsync(b->d_ring[r], tr[r].data(), sizeof(TileRef) * tr[r].size(), cudaMemcpyHostToDevice,

@@ -222,6 +222,19 @@ struct TileRef {
   uint16_t tk;
 };
 
+// Work of the face kernels: one warp walks a column of `count` consecutive
+// faces normal to D, starting at face `first`, for 32 lines of cells side by
+// side (lane l on line 32*blk + l).  The lines run along i for D = 1, 2 (k = c
+// for D = 1, j = c for D = 2) and along j for D = 0 (k = c).
+struct MarchRef {
+  uint16_t solve;
+  uint16_t blk;
+  uint16_t c;
+  uint16_t first;
+  uint16_t count;
+  uint16_t pad;
+};
+
 __host__ __device__ inline long long pad_off(const SolveDev& s, int i, int j, int k) {
   return (long long)(i + NG) + (long long)s.nx * ((long long)(j + NG) + (long long)s.ny * (k + NG));
 }
@@ -233,6 +246,21 @@ __host__ __device__ inline long long int_off(const SolveDev& s, int i, int j, in
 }
 
 enum Domain { DOM_INTERIOR = 0, DOM_RING = 1, DOM_PADDED = 2 };
+
+// The work tables of one stage: interior tiles (update), NGV-ring tiles
+// (viscous terms) and, per direction, the face columns of the face kernels.
+struct StageTables {
+  const TileRef* tiles;
+  int ntiles;
+  const TileRef* ring;
+  int nring;
+  const MarchRef* march[3];
+  int nmarch[3];
+};
+
+// Faces per column of the face kernels: a direction's extent E is cut into
+// ceil(E / kMarchFaces) columns of near-equal length.
+constexpr int kMarchFaces = 32;
 
 // Launch shape of the stage and dt kernels: tile rows (CTA = 32 x tile_rows
 // threads) and, when > 0, a persistent grid of max_ctas CTAs walking the table.

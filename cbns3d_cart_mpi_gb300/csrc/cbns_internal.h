@@ -39,6 +39,8 @@ struct cbns_handle {
   cbns::TileRef* d_tiles_ring = nullptr;
   cbns::TileRef* d_tiles_pad = nullptr;
   int n_int = 0, n_ring = 0, n_pad = 0;
+  cbns::MarchRef* d_march[3] = {nullptr, nullptr, nullptr};  // face columns per direction
+  int n_march[3] = {0, 0, 0};
   double* d_stage = nullptr;
   double* d_partials = nullptr;
   int nparts = 0;
@@ -47,6 +49,13 @@ struct cbns_handle {
   double* h_out = nullptr;    // pinned
   char* h_chunk[2] = {nullptr, nullptr};           // pinned checkpoint chunks (cbns_ckpt.cu)
   cudaEvent_t ev_chunk[2] = {nullptr, nullptr};
+  // Asynchronous entry points (cbns_*_async): an upload and a download stream
+  // beside the compute stream and a second staging buffer, so one state's host
+  // copies overlap another's kernels.  Created on the first asynchronous call.
+  cudaStream_t up_stream = nullptr;
+  cudaStream_t down_stream = nullptr;
+  double* d_stage_out = nullptr;
+  cudaEvent_t ev_in_ready = nullptr, ev_in_free = nullptr, ev_out_ready = nullptr, ev_out_free = nullptr;
   cudaGraphExec_t step_graph = nullptr;
   double graph_t_end = 0.0;
   cbns::Profiler prof;
@@ -64,6 +73,8 @@ struct cbns_batch {
   cbns::TileRef* d_ring[3] = {nullptr, nullptr, nullptr};
   int n_int[3] = {0, 0, 0};
   int n_ring[3] = {0, 0, 0};
+  cbns::MarchRef* d_march[3] = {nullptr, nullptr, nullptr};  // face columns per direction
+  int n_march[3] = {0, 0, 0};
   int sm_count = 0;
   cbns::LaunchCfg cfg;  // tile_rows, max_ctas (= ctas_per_sm * sm_count, 0 = one CTA per tile)
   int ctas_per_sm = 0;

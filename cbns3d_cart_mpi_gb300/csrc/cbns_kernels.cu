@@ -35,6 +35,7 @@
 
 #include <cmath>
 #include <cstdint>
+#include <cstdlib>
 
 #include "cbns_device.cuh"
 #include "cbns_modes.h"
@@ -385,6 +386,16 @@ __global__ void k_dt_raw(const SolveDev* __restrict__ solves, int sidx, double* 
   ctl->smax_bits = 0ull;
 }
 
+// The control block of a solve restarting at time t (the asynchronous upload:
+// no host buffer is read while earlier work may still be queued).
+__global__ void k_reset_ctl(SolveCtl* __restrict__ ctl, double t, double t_end) {
+  SolveCtl c{};
+  c.t_cur = t;
+  c.t_end = t_end;
+  c.active = 1;
+  *ctl = c;
+}
+
 // Explicit dt for a single stage called from the host (cbns_stage).
 __global__ void k_set_dt(const SolveDev* __restrict__ solves, int sidx, double dt) {
   SolveCtl* ctl = solves[sidx].ctl;
@@ -509,15 +520,24 @@ __device__ __forceinline__ void weno_divide10(const Weno<double> (&w)[10], const
 // lf_flux (src/lf_flux.cpp:32-99) takes the reconstructed conserved states.
 // Binary64; the FP32-mixed faces are face_flux_x2 below.
 
-template <int D, typename R>
-__device__ __forceinline__ void face_flux(const SolveDev& s, const R* __restrict__ U, long long c,
-                                          R (&out)[NEQ]) {
-  static_assert(sizeof(R) == 8, "binary64 faces; FP32-mixed faces are face_flux_x2");
+// The stencil of one binary64 face normal to D: the conserved state of the six
+// cells c-3 .. c+2 (W[m][n], field n of cell c-3+m) and, of the two cells
+// either side (l = c - st, r = c), sqrt(rho), H and the velocity.
+struct FaceSide {
+  double sr, h, u, v, w;
+};
+
+__device__ __forceinline__ FaceSide face_side(const SolveDev& s, long long o) {
+  const PrimSet<double>& P = s.pd;
+  return FaceSide{P.srho[o], P.H[o], P.u[o], P.v[o], P.w[o]};
+}
+
+template <int D>
+__device__ __forceinline__ void face_core(const SolveDev& s, const double (&W)[6][NEQ], const FaceSide& Ls,
+                                          const FaceSide& Rs, double (&out)[NEQ]) {
+  using R = double;
   constexpr int T1 = (D + 1) % 3;
   constexpr int T2 = (D + 2) % 3;
-  const long long st = D == 0 ? 1ll : (D == 1 ? (long long)s.nx : (long long)s.nx * s.ny);
-  const long long V = s.V;
-  const long long cl = c - st;
   const Consts<R>& C = consts_of<R>(s);
   const R gam1 = C.gam1, gamma = C.gamma;
 
@@ -525,10 +545,8 @@ __device__ __forceinline__ void face_flux(const SolveDev& s, const R* __restrict
   // (sqrt(rho_L) f_L + sqrt(rho_R) f_R) / (sqrt(rho_L) + sqrt(rho_R)) = f_R + wL (f_L - f_R).
   R Uv[3], HH;
   {
-    // sqrt(rho), u, v, w, H of the cells either side (l: c - st, r: c)
-    const PrimSet<double>& P = s.pd;
-    const R sl = P.srho[cl], sr = P.srho[c], hl = P.H[cl], hr = P.H[c];
-    const R ul = P.u[cl], ur = P.u[c], vl = P.v[cl], vr = P.v[c], wl = P.w[cl], wr = P.w[c];
+    const R sl = Ls.sr, sr = Rs.sr, hl = Ls.h, hr = Rs.h;
+    const R ul = Ls.u, ur = Rs.u, vl = Ls.v, vr = Rs.v, wl = Ls.w, wr = Rs.w;
     const R wL = div_(sl, sl + sr);
     Uv[0] = fma_(wL, ul - ur, ur);
     Uv[1] = fma_(wL, vl - vr, vr);
@@ -549,8 +567,7 @@ __device__ __forceinline__ void face_flux(const SolveDev& s, const R* __restrict
   R w[NEQ][6];
 #pragma unroll
   for (int m = 0; m < 6; ++m) {
-    const long long o = c + (m - 3) * st;
-    const R f0 = U[o], f1 = U[V + o], f2 = U[2 * V + o], f3 = U[3 * V + o], f4 = U[4 * V + o];
+    const R f0 = W[m][0], f1 = W[m][1], f2 = W[m][2], f3 = W[m][3], f4 = W[m][4];
     const R fm[3] = {f1, f2, f3};
     const R t = fma_(-Uv[2], f3, fma_(-Uv[1], f2, fma_(-Uv[0], f1, fma_(hq2, f0, f4))));
     const R A = K * t;
@@ -630,6 +647,23 @@ __device__ __forceinline__ void face_flux(const SolveDev& s, const R* __restrict
   }
   // rho q_n H = q_n (E + p).
   out[4] = fma_(-alpha, ER - EL, fma_(vR[D], ER + pR, vL[D] * (EL + pL)));
+}
+
+// One face from memory: the six stencil cells of U and the two sides' primitives.
+template <int D, typename R>
+__device__ __forceinline__ void face_flux(const SolveDev& s, const R* __restrict__ U, long long c,
+                                          R (&out)[NEQ]) {
+  static_assert(sizeof(R) == 8, "binary64 faces; FP32-mixed faces are face_flux_x2");
+  const long long st = D == 0 ? 1ll : (D == 1 ? (long long)s.nx : (long long)s.nx * s.ny);
+  const long long V = s.V;
+  double W[6][NEQ];
+#pragma unroll
+  for (int m = 0; m < 6; ++m) {
+    const long long o = c + (m - 3) * st;
+#pragma unroll
+    for (int n = 0; n < NEQ; ++n) W[m][n] = U[n * V + o];
+  }
+  face_core<D>(s, W, face_side(s, c - st), face_side(s, c), out);
 }
 
 // ---------------------------------------------------------------------------
@@ -859,6 +893,135 @@ __global__ void __maxnreg__(128) k_inviscid(const SolveDev* __restrict__ solves,
 #pragma unroll
     for (int n = 0; n < NEQ; ++n) F[n * s.IV + fo] = f[n];
   }
+}
+
+// Binary64 faces marching along D: each thread walks a column of consecutive
+// faces normal to D and keeps the six-cell stencil, so a face loads one new
+// cell (five conserved values) and the primitives of its high side instead of
+// six cells and both sides.  The loads of the next face are issued before the
+// current face is computed.  The arithmetic is face_core's, so the fluxes are
+// bitwise those of k_inviscid.
+//   VAR 1, 2: the stencil in registers (2: capped at 168 registers);
+//   VAR 3:    the stencil in a per-warp ring of 8 cells in shared memory, the
+//             next cell copied in by cp.async (no register held while in flight).
+constexpr int kRing = 8;  // ring slots per lane (7 needed: 6 stencil cells + the next)
+constexpr int kRingBytesPerWarp = kRing * NEQ * 32 * (int)sizeof(double);
+
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+template <int D, int VAR>
+__device__ __forceinline__ void march_faces(const SolveDev* __restrict__ solves, const MarchRef* __restrict__ refs,
+                                            int nrefs, int stage) {
+  extern __shared__ double ring_mem[];
+  const int lane = (int)(threadIdx.x & 31);
+  const int wpb = (int)(blockDim.x >> 5);
+  double* ring = ring_mem + (size_t)(threadIdx.x >> 5) * (kRing * NEQ * 32) + lane;  // [slot][n] stride 32
+  for (int e = blockIdx.x * wpb + (int)(threadIdx.x >> 5); e < nrefs; e += gridDim.x * wpb) {
+    const MarchRef r = refs[e];
+    const SolveDev& s = solves[r.solve];
+    if (!s.ctl->active) continue;
+    const int line = 32 * r.blk + lane;
+    if (line >= (D == 0 ? s.JM : s.IM)) continue;
+    const int i = D == 0 ? r.first : line;
+    const int j = D == 0 ? line : (D == 1 ? r.first : r.c);
+    const int k = D == 2 ? r.first : r.c;
+    const long long st = D == 0 ? 1ll : (D == 1 ? (long long)s.nx : (long long)s.nx * s.ny);
+    const long long fst = D == 0 ? 1ll : (D == 1 ? (long long)s.IM : (long long)s.IM * s.JM);
+    const long long V = s.V, IV = s.IV;
+    const double* __restrict__ U = stage == 1 ? s.Q : s.Qp;
+    double* __restrict__ F = s.F[D];
+    long long c = pad_off(s, i, j, k);
+    long long fo = int_off(s, i, j, k);
+    FaceSide Ls = face_side(s, c - st);
+    FaceSide Ns = face_side(s, c);
+    const int nf = (int)r.count;
+    if constexpr (VAR == 3) {
+      // Cells of the column are numbered q = 0, 1, ... from c - 3 st; cell q
+      // sits in slot q % kRing.  Face f reads cells f .. f+5.
+#pragma unroll
+      for (int q = 0; q < 6; ++q)
+#pragma unroll
+        for (int n = 0; n < NEQ; ++n) cp_async8(ring + (q * NEQ + n) * 32, U + n * V + c + (q - 3) * st);
+      cp_async_commit();
+      for (int f = 0; f < nf; ++f) {
+        cp_async_wait_all();
+        if (f + 1 < nf) {
+          const int q = f + 6;
+#pragma unroll
+          for (int n = 0; n < NEQ; ++n)
+            cp_async8(ring + ((q & (kRing - 1)) * NEQ + n) * 32, U + n * V + c + 3 * st);
+          cp_async_commit();
+        }
+        const FaceSide Rs = Ns;
+        if (f + 1 < nf) Ns = face_side(s, c + st);
+        double W[6][NEQ];
+#pragma unroll
+        for (int m = 0; m < 6; ++m)
+#pragma unroll
+          for (int n = 0; n < NEQ; ++n) W[m][n] = ring[(((f + m) & (kRing - 1)) * NEQ + n) * 32];
+        double out[NEQ];
+        face_core<D>(s, W, Ls, Rs, out);
+#pragma unroll
+        for (int n = 0; n < NEQ; ++n) F[n * IV + fo] = out[n];
+        Ls = Rs;
+        c += st;
+        fo += fst;
+      }
+      cp_async_wait_all();
+    } else {
+      double W[6][NEQ];
+#pragma unroll
+      for (int m = 0; m < 5; ++m)
+#pragma unroll
+        for (int n = 0; n < NEQ; ++n) W[m][n] = U[n * V + c + (m - 3) * st];
+      double Nx[NEQ];
+#pragma unroll
+      for (int n = 0; n < NEQ; ++n) Nx[n] = U[n * V + c + 2 * st];
+      for (int f = 0; f < nf; ++f) {
+#pragma unroll
+        for (int n = 0; n < NEQ; ++n) W[5][n] = Nx[n];
+        const FaceSide Rs = Ns;
+        if (f + 1 < nf) {
+#pragma unroll
+          for (int n = 0; n < NEQ; ++n) Nx[n] = U[n * V + c + 3 * st];
+          Ns = face_side(s, c + st);
+        }
+        double out[NEQ];
+        face_core<D>(s, W, Ls, Rs, out);
+#pragma unroll
+        for (int n = 0; n < NEQ; ++n) F[n * IV + fo] = out[n];
+#pragma unroll
+        for (int m = 0; m < 5; ++m)
+#pragma unroll
+          for (int n = 0; n < NEQ; ++n) W[m][n] = W[m + 1][n];
+        Ls = Rs;
+        c += st;
+        fo += fst;
+      }
+    }
+  }
+}
+
+template <int D>
+__global__ void __launch_bounds__(kMaxThreads) k_inviscid_march(const SolveDev* __restrict__ solves,
+                                                                 const MarchRef* __restrict__ refs, int nrefs,
+                                                                 int stage) {
+  march_faces<D, 1>(solves, refs, nrefs, stage);
+}
+template <int D>
+__global__ void __maxnreg__(168) k_inviscid_march168(const SolveDev* __restrict__ solves,
+                                                      const MarchRef* __restrict__ refs, int nrefs, int stage) {
+  march_faces<D, 2>(solves, refs, nrefs, stage);
+}
+template <int D>
+__global__ void __maxnreg__(128) k_inviscid_march_ring(const SolveDev* __restrict__ solves,
+                                                        const MarchRef* __restrict__ refs, int nrefs, int stage) {
+  march_faces<D, 3>(solves, refs, nrefs, stage);
 }
 
 // ---------------------------------------------------------------------------
@@ -1332,14 +1495,36 @@ cudaError_t launch_dt_raw(const SolveDev* d, int sidx, const TileRef* tiles, int
   return cudaGetLastError();
 }
 
+cudaError_t launch_reset_ctl(SolveCtl* ctl, double t, double t_end, cudaStream_t st) {
+  k_reset_ctl<<<1, 1, 0, st>>>(ctl, t, t_end);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_set_dt(const SolveDev* d, int sidx, double dt, cudaStream_t st) {
   k_set_dt<<<1, 1, 0, st>>>(d, sidx, dt);
   return cudaGetLastError();
 }
 
+// Face columns (one per warp) of the marching face kernels: CTAs of
+// cfg.tile_rows warps, persistent when cfg.max_ctas is set.
+static int march_grid(int nmarch, const LaunchCfg& cfg) {
+  return grid_for((nmarch + cfg.tile_rows - 1) / cfg.tile_rows, cfg.max_ctas);
+}
+
+static int face_march_mode() {
+  static int mode = -1;
+  if (mode < 0) {
+    const char* e = std::getenv("CBNS_FACE_MARCH");
+    mode = e ? std::atoi(e) : 1;
+  }
+  return mode;
+}
+
 template <typename R>
-static void stage_ty(const SolveDev* d, const TileRef* tiles, int ntiles, const TileRef* ring_tiles, int nring,
-                     int stage, const LaunchCfg& cfg, cudaStream_t st, Profiler* pf) {
+static void stage_ty(const SolveDev* d, const StageTables& T, int stage, const LaunchCfg& cfg, cudaStream_t st,
+                     Profiler* pf) {
+  const TileRef* tiles = T.tiles;
+  const int ntiles = T.ntiles;
   const int g = grid_for(ntiles, cfg.max_ctas);
   const int nt = 32 * cfg.tile_rows;
   if constexpr (sizeof(R) == 4) {
@@ -1347,13 +1532,42 @@ static void stage_ty(const SolveDev* d, const TileRef* tiles, int ntiles, const 
     CBNS_LAUNCH(pf, KID_INVISCID_X, st, (k_inviscid_x2<0><<<g, nt2, 0, st>>>(d, tiles, ntiles)));
     CBNS_LAUNCH(pf, KID_INVISCID_Y, st, (k_inviscid_x2<1><<<g, nt2, 0, st>>>(d, tiles, ntiles)));
     CBNS_LAUNCH(pf, KID_INVISCID_Z, st, (k_inviscid_x2<2><<<g, nt2, 0, st>>>(d, tiles, ntiles)));
+  } else if (face_march_mode() == 1) {
+    CBNS_LAUNCH(pf, KID_INVISCID_X, st,
+                (k_inviscid_march<0><<<march_grid(T.nmarch[0], cfg), nt, 0, st>>>(d, T.march[0], T.nmarch[0], stage)));
+    CBNS_LAUNCH(pf, KID_INVISCID_Y, st,
+                (k_inviscid_march<1><<<march_grid(T.nmarch[1], cfg), nt, 0, st>>>(d, T.march[1], T.nmarch[1], stage)));
+    CBNS_LAUNCH(pf, KID_INVISCID_Z, st,
+                (k_inviscid_march<2><<<march_grid(T.nmarch[2], cfg), nt, 0, st>>>(d, T.march[2], T.nmarch[2], stage)));
+  } else if (face_march_mode() == 2) {
+    CBNS_LAUNCH(pf, KID_INVISCID_X, st,
+                (k_inviscid_march168<0><<<march_grid(T.nmarch[0], cfg), nt, 0, st>>>(d, T.march[0], T.nmarch[0], stage)));
+    CBNS_LAUNCH(pf, KID_INVISCID_Y, st,
+                (k_inviscid_march168<1><<<march_grid(T.nmarch[1], cfg), nt, 0, st>>>(d, T.march[1], T.nmarch[1], stage)));
+    CBNS_LAUNCH(pf, KID_INVISCID_Z, st,
+                (k_inviscid_march168<2><<<march_grid(T.nmarch[2], cfg), nt, 0, st>>>(d, T.march[2], T.nmarch[2], stage)));
+  } else if (face_march_mode() == 3) {
+    static bool attr = false;
+    const int smem = cfg.tile_rows * kRingBytesPerWarp;
+    if (!attr) {
+      cudaFuncSetAttribute(k_inviscid_march_ring<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, 8 * kRingBytesPerWarp);
+      cudaFuncSetAttribute(k_inviscid_march_ring<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 8 * kRingBytesPerWarp);
+      cudaFuncSetAttribute(k_inviscid_march_ring<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 8 * kRingBytesPerWarp);
+      attr = true;
+    }
+    CBNS_LAUNCH(pf, KID_INVISCID_X, st,
+                (k_inviscid_march_ring<0><<<march_grid(T.nmarch[0], cfg), nt, smem, st>>>(d, T.march[0], T.nmarch[0], stage)));
+    CBNS_LAUNCH(pf, KID_INVISCID_Y, st,
+                (k_inviscid_march_ring<1><<<march_grid(T.nmarch[1], cfg), nt, smem, st>>>(d, T.march[1], T.nmarch[1], stage)));
+    CBNS_LAUNCH(pf, KID_INVISCID_Z, st,
+                (k_inviscid_march_ring<2><<<march_grid(T.nmarch[2], cfg), nt, smem, st>>>(d, T.march[2], T.nmarch[2], stage)));
   } else {
     CBNS_LAUNCH(pf, KID_INVISCID_X, st, (k_inviscid<0, R><<<g, nt, 0, st>>>(d, tiles, ntiles, stage)));
     CBNS_LAUNCH(pf, KID_INVISCID_Y, st, (k_inviscid<1, R><<<g, nt, 0, st>>>(d, tiles, ntiles, stage)));
     CBNS_LAUNCH(pf, KID_INVISCID_Z, st, (k_inviscid<2, R><<<g, nt, 0, st>>>(d, tiles, ntiles, stage)));
   }
   CBNS_LAUNCH(pf, KID_VISCOUS, st,
-              (k_viscous<R><<<grid_for(nring, cfg.max_ctas), nt, 0, st>>>(d, ring_tiles, nring)));
+              (k_viscous<R><<<grid_for(T.nring, cfg.max_ctas), nt, 0, st>>>(d, T.ring, T.nring)));
   if constexpr (sizeof(R) == 4) {
     CBNS_LAUNCH(pf, KID_UPDATE, st, (k_update_f32<<<g, nt, 0, st>>>(d, tiles, ntiles, stage)));
   } else {
@@ -1361,11 +1575,11 @@ static void stage_ty(const SolveDev* d, const TileRef* tiles, int ntiles, const 
   }
 }
 
-cudaError_t launch_stage(const SolveDev* d, const TileRef* tiles, int ntiles, const TileRef* ring_tiles,
-                         int nring, int stage, const LaunchCfg& cfg, bool mixed, cudaStream_t st, Profiler* pf) {
-  if (ntiles == 0) return cudaSuccess;
-  if (mixed) stage_ty<float>(d, tiles, ntiles, ring_tiles, nring, stage, cfg, st, pf);
-  else stage_ty<double>(d, tiles, ntiles, ring_tiles, nring, stage, cfg, st, pf);
+cudaError_t launch_stage(const SolveDev* d, const StageTables& T, int stage, const LaunchCfg& cfg, bool mixed,
+                         cudaStream_t st, Profiler* pf) {
+  if (T.ntiles == 0) return cudaSuccess;
+  if (mixed) stage_ty<float>(d, T, stage, cfg, st, pf);
+  else stage_ty<double>(d, T, stage, cfg, st, pf);
   return cudaGetLastError();
 }
 

@@ -137,6 +137,48 @@ class Solver:
         st = _check(_lib.gpu().cbns_step(self._h, te, ctypes.byref(dt), ctypes.byref(t)), "cbns_step")
         return None if st == CBNS_FINISHED else (dt.value, t.value)
 
+    # Asynchronous forms (cbns_*_async): each call enqueues and returns; the host
+    # arrays must stay alive and untouched until wait().  Page-locked arrays
+    # (pinned_state) let the copies overlap the kernels.
+    def upload_Q_async(self, Q, t=None):
+        if not (isinstance(Q, np.ndarray) and Q.dtype == np.float64 and Q.flags.c_contiguous):
+            raise ValueError("upload_Q_async needs a C-contiguous float64 array that stays alive until wait()")
+        if Q.size != int(np.prod(self.shape)):
+            raise ValueError("Q has %d values, %d expected" % (Q.size, int(np.prod(self.shape))))
+        _check(_lib.gpu().cbns_upload_Q_async(self._h, _ptr(Q), self.params.t_cur if t is None else t),
+               "cbns_upload_Q_async")
+
+    def step_async(self, t_end=None):
+        te = self.params.t_end if t_end is None else t_end
+        _check(_lib.gpu().cbns_step_async(self._h, te), "cbns_step_async")
+
+    def download_Q_async(self, out):
+        if not (isinstance(out, np.ndarray) and out.dtype == np.float64 and out.flags.c_contiguous
+                and out.size == int(np.prod(self.shape))):
+            raise ValueError("download_Q_async needs a C-contiguous float64 array of the state's size")
+        _check(_lib.gpu().cbns_download_Q_async(self._h, _ptr(out)), "cbns_download_Q_async")
+
+    def wait(self):
+        """Wait for everything enqueued; returns (dt, t_cur), or None once finished."""
+        dt, t = ctypes.c_double(), ctypes.c_double()
+        st = _check(_lib.gpu().cbns_wait(self._h, ctypes.byref(dt), ctypes.byref(t)), "cbns_wait")
+        return None if st == CBNS_FINISHED else (dt.value, t.value)
+
+    def poll(self):
+        done = ctypes.c_int()
+        _check(_lib.gpu().cbns_poll(self._h, ctypes.byref(done)), "cbns_poll")
+        return bool(done.value)
+
+    def pinned_state(self):
+        """A page-locked host array of the state's shape (torch's pinned allocator;
+        the solver keeps the owning tensor alive as long as itself)."""
+        import torch
+        t = torch.empty(int(np.prod(self.shape)), dtype=torch.float64, pin_memory=True)
+        if not hasattr(self, "_pins"):
+            self._pins = []
+        self._pins.append(t)
+        return t.numpy().reshape(self.shape)
+
     def run(self, nsteps, t_end=None):
         done = ctypes.c_uint32()
         te = self.params.t_end if t_end is None else t_end

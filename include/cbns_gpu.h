@@ -139,13 +139,43 @@ cbns_status cbns_stage(cbns_handle* h, double dt, int stage);
 /* One iteration of the time loop of src/cbns3d.cpp:176-241: returns
  * CBNS_FINISHED without stepping if t_cur + 1e-5 > t_end (Block3d::is_finished),
  * else dt = calc_dt() clipped to t_end - t_cur, t_cur += dt, three stages.
- * dt_out / t_out may be NULL (then the call does not wait for the device). */
+ * dt_out / t_out may be NULL.  The call waits for the step (cbns_step_async
+ * does not). */
 cbns_status cbns_step(cbns_handle* h, double t_end, double* dt_out, double* t_out);
 
 /* nsteps iterations of cbns_step as a replayed CUDA graph with the
  * is_finished test, dt and t_cur kept on the device; steps taken go to
  * *steps_done (may be NULL). */
 cbns_status cbns_run(cbns_handle* h, uint32_t nsteps, double t_end, uint32_t* steps_done);
+
+/* Asynchronous forms of cbns_upload_Q, cbns_step and cbns_download_Q, for a
+ * Block3d-style driver that keeps one handle and wants the host copies of one
+ * state to overlap the kernels of the next step (the loop of
+ * src/cbns3d.cpp:176-241 with get_Q/checkpoint output between steps).  Each
+ * call only enqueues work and returns:
+ *   cbns_upload_Q_async    the host copy of Q, then the start-up sequence of
+ *                          cbns_upload_Q; t_cur = t;
+ *   cbns_step_async        one step of cbns_step (the is_finished test, dt,
+ *                          three stages), as a replayed CUDA graph;
+ *   cbns_download_Q_async  the current Q into a host array.
+ * Work runs in call order.  Host copies go to two more streams of the handle
+ * (one per direction), through staging buffers of their own (the first
+ * asynchronous call allocates one more state-sized device buffer,
+ * NEQ*IM_G*JM_G*KM_G doubles), so a download overlaps the steps enqueued after
+ * it and an upload overlaps the steps enqueued before it.  Q must stay valid and unchanged (upload) or
+ * untouched (download) until cbns_wait returns; pass page-locked host memory
+ * (cudaMallocHost / cudaHostRegister) for the copies to overlap: with pageable
+ * memory the call still works but returns only once its copy is done.
+ * cbns_wait waits for everything enqueued on the handle and returns the status
+ * cbns_step would (CBNS_FINISHED once t_end is reached, CBNS_ERR_NONPHYSICAL
+ * after a bad state), with the last dt and t_cur (either may be NULL).
+ * cbns_poll sets *done to 1 when nothing enqueued is still running, without
+ * waiting. */
+cbns_status cbns_upload_Q_async(cbns_handle* h, const double* Q, double t);
+cbns_status cbns_step_async(cbns_handle* h, double t_end);
+cbns_status cbns_download_Q_async(cbns_handle* h, double* Q);
+cbns_status cbns_wait(cbns_handle* h, double* dt_last, double* t_cur);
+cbns_status cbns_poll(cbns_handle* h, int* done);
 
 /* Current simulated time and last dt, read from the device. */
 cbns_status cbns_get_time(cbns_handle* h, double* t_cur, double* dt_last);
