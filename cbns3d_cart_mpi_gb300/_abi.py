@@ -23,11 +23,13 @@ CBNS_ERR_NO_DEVICE = -7
 CBNS_ERR_IO = -8
 CBNS_ERR_FORMAT = -9
 CBNS_ERR_CANCELLED = -10
+CBNS_ERR_BOUNDS = -11
 
 STATUS_NAMES = {
     0: "CBNS_OK", 1: "CBNS_FINISHED", -1: "CBNS_ERR_INVALID_ARG", -2: "CBNS_ERR_BAD_DIMS",
     -3: "CBNS_ERR_CUDA", -4: "CBNS_ERR_OUT_OF_MEMORY", -5: "CBNS_ERR_NONPHYSICAL",
     -6: "CBNS_ERR_TIMEOUT", -7: "CBNS_ERR_NO_DEVICE", -8: "CBNS_ERR_IO", -9: "CBNS_ERR_FORMAT", -10: "CBNS_ERR_CANCELLED",
+    -11: "CBNS_ERR_BOUNDS",
 }
 
 CBNS_FP64 = 0

@@ -124,13 +124,15 @@ def _bind(lib, table):
 
 
 def gpu():
-    """The GPU library; raises if it has not been built (no fallback exists)."""
+    """The GPU library; raises if it has not been built (no fallback exists).
+    CBNS_GPU_LIB may name another build of it (the bounds-checked test build)."""
     global _gpu
     if _gpu is None:
-        if not os.path.exists(GPU_LIB):
-            raise RuntimeError("libcbns_gpu.so is not built (%s); run cbns3d_cart_mpi_gb300.build.build() "
-                               "or __graft_entry__.build()" % GPU_LIB)
-        _gpu = _bind(ctypes.CDLL(GPU_LIB), GPU_API)
+        path = os.environ.get("CBNS_GPU_LIB") or GPU_LIB
+        if not os.path.exists(path):
+            raise RuntimeError("%s is not built; run cbns3d_cart_mpi_gb300.build.build() "
+                               "or __graft_entry__.build()" % path)
+        _gpu = _bind(ctypes.CDLL(path), GPU_API)
     return _gpu
 
 

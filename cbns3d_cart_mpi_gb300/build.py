@@ -35,6 +35,9 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompil
               "--expt-relaxed-constexpr"]
 
 GPU_LIB = os.path.join(LIB, "libcbns_gpu.so")
+# The same library with every kernel index checked against its array
+# (-DCBNS_BOUNDS_CHECK): a test build, loaded through CBNS_GPU_LIB.
+CHECKED_GPU_LIB = os.path.join(LIB, "libcbns_gpu_checked.so")
 PROBE_LIB = os.path.join(LIB, "libcbns_probe.so")
 HOST_LIB = os.path.join(LIB, "libcbns_host.so")
 DRIVER = os.path.join(LIB, "cbns3d_gb300")
@@ -127,6 +130,30 @@ def build(verbose=False, extra_nvcc=()):
         for p in (GPU_LIB, PROBE_LIB, HOST_LIB, DRIVER):
             print(p)
     return GPU_LIB, HOST_LIB, DRIVER
+
+
+def build_checked():
+    """The bounds-checked GPU library (every global index of the kernels checked
+    against its array; misses reported as CBNS_ERR_BOUNDS, never a trap)."""
+    os.makedirs(LIB, exist_ok=True)
+    objdir = os.path.join(LIB, "obj_checked")
+    os.makedirs(objdir, exist_ok=True)
+    hdrs = _headers()
+    nvcc = _nvcc()
+    flags = ARCH + NVCC_FLAGS + ["-DCBNS_BOUNDS_CHECK"]
+
+    def cu_obj(src):
+        path = os.path.join(CSRC, src)
+        obj = os.path.join(objdir, os.path.basename(src) + ".o")
+        if _stale(obj, [path] + hdrs + [__file__]):
+            _atomic(lambda out: [nvcc] + flags + ["-c", path, "-o", out], obj)
+        return obj
+
+    with ThreadPoolExecutor(max_workers=max(2, os.cpu_count() or 2)) as ex:
+        objs = [f.result() for f in [ex.submit(cu_obj, s) for s in GPU_SOURCES]]
+    if _stale(CHECKED_GPU_LIB, objs):
+        _atomic(lambda out: [nvcc] + ARCH + ["-shared", "-o", out] + objs + ["-lcudart"], CHECKED_GPU_LIB)
+    return CHECKED_GPU_LIB
 
 
 if __name__ == "__main__":

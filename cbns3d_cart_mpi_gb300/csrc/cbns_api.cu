@@ -53,6 +53,13 @@ cbns_status cuda_fail(cudaError_t e, const char* what) {
   return CBNS_ERR_CUDA;
 }
 
+// The error a solve's device status word stands for (0: none).
+cbns_status ctl_fail(int status, const char* fn) {
+  if (status & kStatusBounds)
+    return fail(CBNS_ERR_BOUNDS, std::string(fn) + ": a kernel index left its array (bounds-checked build)");
+  return fail(CBNS_ERR_NONPHYSICAL, std::string(fn) + ": non-physical state (rho <= 0, p <= 0 or NaN)");
+}
+
 #define CBNS_CUDA(call)                                   \
   do {                                                    \
     cudaError_t e_ = (call);                              \
@@ -83,47 +90,10 @@ size_t tile_count(long long ex, long long ey, long long ez, int rows = TILE_Y) {
   return (size_t)((ex + TILE_X - 1) / TILE_X) * (size_t)((ey + rows - 1) / rows) * (size_t)ez;
 }
 
-// Face columns of the face kernels for direction D of a block: the extent
-// along D cut into ceil(E / faces) columns of near-equal length, for every
-// block of 32 lines and every position of the third axis.  Entries of one
-// warp-group (CTA) are neighbouring line blocks of one column position.
-int march_faces_per_column() {
-  static int n = 0;
-  if (n == 0) {
-    const char* e = std::getenv("CBNS_MARCH_FACES");
-    n = e ? std::atoi(e) : kMarchFaces;
-    if (n < 1 || n > 65535) n = kMarchFaces;
-  }
-  return n;
-}
-
-size_t march_count(int D, long long IM, long long JM, long long KM) {
-  const long long lines = D == 0 ? JM : IM, E = D == 0 ? IM : (D == 1 ? JM : KM), third = D == 2 ? JM : KM;
-  const long long per = march_faces_per_column();
-  return (size_t)((lines + 31) / 32) * (size_t)((E + per - 1) / per) * (size_t)third;
-}
-
-void append_march(std::vector<MarchRef>& out, int solve, int D, int IM, int JM, int KM) {
-  const int lines = D == 0 ? JM : IM, E = D == 0 ? IM : (D == 1 ? JM : KM), third = D == 2 ? JM : KM;
-  const int per = march_faces_per_column();
-  const int ncol = (E + per - 1) / per;
-  const int base = E / ncol, extra = E % ncol;
-  const int nblk = (lines + 31) / 32;
-  for (int c = 0; c < third; ++c) {
-    int first = 0;
-    for (int q = 0; q < ncol; ++q) {
-      const int count = base + (q < extra ? 1 : 0);
-      for (int b = 0; b < nblk; ++b)
-        out.push_back(MarchRef{(uint16_t)solve, (uint16_t)b, (uint16_t)c, (uint16_t)first, (uint16_t)count, 0});
-      first += count;
-    }
-  }
-}
-
 // Byte offsets of everything a solve's arena holds (see cbns_create).
 struct ArenaLayout {
-  size_t oQ, oQp, oStage, oPrim, oF[3], oTv, oFf[3], oTv32, oU32, oP32, oCtl, oDesc, oTi, oTr, oTp, oM[3], oPart,
-      oOut, total;
+  size_t oQ, oQp, oStage, oPrim, oF[3], oTv, oFf[3], oTv32, oU32, oP32, oCtl, oDesc, oTi, oTr, oTp, oPart, oOut,
+      total;
 };
 
 ArenaLayout arena_layout(const SolveDev& s, bool mixed, size_t n_int, size_t n_ring, size_t n_pad, int nparts) {
@@ -153,7 +123,6 @@ ArenaLayout arena_layout(const SolveDev& s, bool mixed, size_t n_int, size_t n_r
   L.oTi = take(sizeof(TileRef) * n_int);
   L.oTr = take(sizeof(TileRef) * n_ring);
   L.oTp = take(sizeof(TileRef) * n_pad);
-  for (int d = 0; d < 3; ++d) L.oM[d] = take(sizeof(MarchRef) * march_count(d, s.IM, s.JM, s.KM));
   L.oPart = take(sizeof(double) * 4 * nparts);
   L.oOut = take(sizeof(double) * 8);
   L.total = off;
@@ -318,11 +287,7 @@ cbns_status cbns_create(const cbns_params* p, uint32_t IM, uint32_t JM, uint32_t
   h->n_int = (int)t_int.size();
   h->n_ring = (int)t_ring.size();
   h->n_pad = (int)t_pad.size();
-  std::vector<MarchRef> t_march[3];
-  for (int d = 0; d < 3; ++d) {
-    append_march(t_march[d], 0, d, IM, JM, KM);
-    h->n_march[d] = (int)t_march[d].size();
-  }
+
   const size_t oQ = L.oQ, oQp = L.oQp, oStage = L.oStage, oPrim = L.oPrim, oU32 = L.oU32, oP32 = L.oP32;
   const size_t oCtl = L.oCtl, oDesc = L.oDesc, oTi = L.oTi, oTr = L.oTr, oTp = L.oTp, oPart = L.oPart,
                oOut = L.oOut;
@@ -395,7 +360,6 @@ cbns_status cbns_create(const cbns_params* p, uint32_t IM, uint32_t JM, uint32_t
   h->d_tiles_int = (TileRef*)(A + oTi);
   h->d_tiles_ring = (TileRef*)(A + oTr);
   h->d_tiles_pad = (TileRef*)(A + oTp);
-  for (int d = 0; d < 3; ++d) h->d_march[d] = (MarchRef*)(A + L.oM[d]);
   h->d_partials = (double*)(A + oPart);
   h->d_out = (double*)(A + oOut);
 
@@ -414,10 +378,7 @@ cbns_status cbns_create(const cbns_params* p, uint32_t IM, uint32_t JM, uint32_t
                            h->stream)) != cudaSuccess ||
       (e = cudaMemcpyAsync(h->d_ctl, h->h_ctl, sizeof(SolveCtl), cudaMemcpyHostToDevice, h->stream)) != cudaSuccess)
     return bail(cuda_fail(e, "cudaMemcpyAsync(setup)"));
-  for (int d = 0; d < 3; ++d)
-    if ((e = cudaMemcpyAsync(h->d_march[d], t_march[d].data(), sizeof(MarchRef) * t_march[d].size(),
-                             cudaMemcpyHostToDevice, h->stream)) != cudaSuccess)
-      return bail(cuda_fail(e, "cudaMemcpyAsync(setup)"));
+
   if ((e = cudaStreamSynchronize(h->stream)) != cudaSuccess) return bail(cuda_fail(e, "cudaStreamSynchronize"));
   *out = h;
   return CBNS_OK;
@@ -509,8 +470,7 @@ cbns_status cbns_calc_dt(cbns_handle* h, double* dt) {
 }
 
 static cbns_status enqueue_stage(cbns_handle* h, int stage) {
-  const StageTables T{h->d_tiles_int, h->n_int, h->d_tiles_ring, h->n_ring,
-                      {h->d_march[0], h->d_march[1], h->d_march[2]}, {h->n_march[0], h->n_march[1], h->n_march[2]}};
+  const StageTables T{h->d_tiles_int, h->n_int, h->d_tiles_ring, h->n_ring};
   CBNS_CUDA(launch_stage(h->d_desc, T, stage, LaunchCfg{}, h->desc.mixed != 0, h->stream, h->pf()));
   return CBNS_OK;
 }
@@ -543,7 +503,7 @@ cbns_status cbns_step(cbns_handle* h, double t_end, double* dt_out, double* t_ou
   CBNS_CUDA(cudaStreamSynchronize(h->stream));
   if (dt_out) *dt_out = h->h_ctl->dt;
   if (t_out) *t_out = h->h_ctl->t_cur;
-  if (h->h_ctl->status) return fail(CBNS_ERR_NONPHYSICAL, "cbns_step: non-physical state (rho <= 0, p <= 0 or NaN)");
+  if (h->h_ctl->status) return ctl_fail(h->h_ctl->status, "cbns_step");
   return h->h_ctl->active ? CBNS_OK : CBNS_FINISHED;
 }
 
@@ -586,7 +546,7 @@ cbns_status cbns_run(cbns_handle* h, uint32_t nsteps, double t_end, uint32_t* st
   CBNS_CUDA(cudaMemcpyAsync(h->h_ctl, h->d_ctl, sizeof(SolveCtl), cudaMemcpyDeviceToHost, h->stream));
   CBNS_CUDA(cudaStreamSynchronize(h->stream));
   if (steps_done) *steps_done = h->h_ctl->steps - start;
-  if (h->h_ctl->status) return fail(CBNS_ERR_NONPHYSICAL, "cbns_run: non-physical state (rho <= 0, p <= 0 or NaN)");
+  if (h->h_ctl->status) return ctl_fail(h->h_ctl->status, "cbns_run");
   return CBNS_OK;
 }
 
@@ -674,7 +634,7 @@ cbns_status cbns_wait(cbns_handle* h, double* dt_last, double* t_cur) {
   if (h->down_stream) CBNS_CUDA(cudaStreamSynchronize(h->down_stream));
   if (dt_last) *dt_last = h->h_ctl->dt;
   if (t_cur) *t_cur = h->h_ctl->t_cur;
-  if (h->h_ctl->status) return fail(CBNS_ERR_NONPHYSICAL, "cbns_wait: non-physical state (rho <= 0, p <= 0 or NaN)");
+  if (h->h_ctl->status) return ctl_fail(h->h_ctl->status, "cbns_wait");
   return h->h_ctl->active ? CBNS_OK : CBNS_FINISHED;
 }
 
@@ -722,12 +682,12 @@ cbns_status cbns_check_state(cbns_handle* h) {
   if (st != CBNS_OK) return st;
   CBNS_CUDA(cudaMemcpyAsync(h->h_ctl, h->d_ctl, sizeof(SolveCtl), cudaMemcpyDeviceToHost, h->stream));
   CBNS_CUDA(cudaStreamSynchronize(h->stream));
-  if (h->h_ctl->status) {
+  if (const int bits = h->h_ctl->status) {
     h->h_ctl->status = 0;
     CBNS_CUDA(cudaMemcpyAsync(&h->d_ctl->status, &h->h_ctl->status, sizeof(int), cudaMemcpyHostToDevice,
                               h->stream));
     CBNS_CUDA(cudaStreamSynchronize(h->stream));
-    return fail(CBNS_ERR_NONPHYSICAL, "non-physical state (rho <= 0, p <= 0 or NaN) met since the last check");
+    return ctl_fail(bits, "cbns_check_state (since the last check)");
   }
   return CBNS_OK;
 }
@@ -787,8 +747,7 @@ static cbns_status batch_enqueue_step(cbns_batch* b) {
   const int ri = rows_index(b->cfg.tile_rows);
   const int n = (int)b->handles.size();
   CBNS_CUDA(launch_dt(b->d_descs, n, b->d_int[ri], b->n_int[ri], 0.0, false, b->mixed, b->cfg, b->stream, nullptr));
-  const StageTables T{b->d_int[ri], b->n_int[ri], b->d_ring[ri], b->n_ring[ri],
-                      {b->d_march[0], b->d_march[1], b->d_march[2]}, {b->n_march[0], b->n_march[1], b->n_march[2]}};
+  const StageTables T{b->d_int[ri], b->n_int[ri], b->d_ring[ri], b->n_ring[ri]};
   for (int st = 1; st <= 3; ++st)
     CBNS_CUDA(launch_stage(b->d_descs, T, st, b->cfg, b->mixed, b->stream, nullptr));
   return CBNS_OK;
@@ -861,14 +820,12 @@ cbns_status cbns_batch_create(cbns_handle* const* handles, int n, cbns_batch** o
     return bail(cuda_fail(e, "cudaStreamCreate(batch)"));
   std::vector<SolveDev> descs(n);
   std::vector<TileRef> ti[3], tr[3];
-  std::vector<MarchRef> tm[3];
   for (int i = 0; i < n; ++i) {
     const SolveDev& s = handles[i]->desc;
     descs[i] = s;
     for (int r = 0; r < 3; ++r) {
       append_tiles(ti[r], i, s.IM, s.JM, s.KM, kRowsOptions[r]);
       append_tiles(tr[r], i, s.rx, s.ry, s.rz, kRowsOptions[r]);
-      append_march(tm[r], i, r, s.IM, s.JM, s.KM);  // r: direction
     }
   }
   size_t off = 0;
@@ -877,11 +834,10 @@ cbns_status cbns_batch_create(cbns_handle* const* handles, int n, cbns_batch** o
     off += align_up(bytes);
     return o;
   };
-  size_t oD = take(sizeof(SolveDev) * n), oI[3], oR[3], oM[3];
+  size_t oD = take(sizeof(SolveDev) * n), oI[3], oR[3];
   for (int r = 0; r < 3; ++r) {
     oI[r] = take(sizeof(TileRef) * ti[r].size());
     oR[r] = take(sizeof(TileRef) * tr[r].size());
-    oM[r] = take(sizeof(MarchRef) * tm[r].size());
   }
   if ((e = cudaMalloc(&b->arena, off)) != cudaSuccess) return bail(cuda_fail(e, "cudaMalloc(batch)"));
   b->d_descs = (SolveDev*)(b->arena + oD);
@@ -893,11 +849,7 @@ cbns_status cbns_batch_create(cbns_handle* const* handles, int n, cbns_batch** o
     b->d_ring[r] = (TileRef*)(b->arena + oR[r]);
     b->n_int[r] = (int)ti[r].size();
     b->n_ring[r] = (int)tr[r].size();
-    b->d_march[r] = (MarchRef*)(b->arena + oM[r]);
-    b->n_march[r] = (int)tm[r].size();
-    if ((e = cudaMemcpyAsync(b->d_march[r], tm[r].data(), sizeof(MarchRef) * tm[r].size(), cudaMemcpyHostToDevice,
-                             b->stream)) != cudaSuccess)
-      return bail(cuda_fail(e, "cudaMemcpyAsync(batch columns)"));
+
     if ((e = cudaMemcpyAsync(b->d_int[r], ti[r].data(), sizeof(TileRef) * ti[r].size(), cudaMemcpyHostToDevice,
                              b->stream)) != cudaSuccess ||
         (e = cudaMemcpyAsync(b->d_ring[r], tr[r].data(), sizeof(TileRef) * tr[r].size(), cudaMemcpyHostToDevice,
@@ -952,12 +904,12 @@ cbns_status cbns_batch_run(cbns_batch* b, uint32_t nsteps, uint32_t* steps_out) 
     CBNS_CUDA(cudaMemcpyAsync(&b->h_ctl[i], b->handles[i]->d_ctl, sizeof(SolveCtl), cudaMemcpyDeviceToHost,
                               b->stream));
   CBNS_CUDA(cudaStreamSynchronize(b->stream));
-  bool bad = false;
+  int bits = 0;
   for (int i = 0; i < n; ++i) {
     if (steps_out) steps_out[i] = b->h_ctl[i].steps - b->start_steps[i];
-    bad = bad || b->h_ctl[i].status != 0;
+    bits |= b->h_ctl[i].status;
   }
-  if (bad) return fail(CBNS_ERR_NONPHYSICAL, "cbns_batch_run: a solve met a non-physical state");
+  if (bits) return ctl_fail(bits, "cbns_batch_run (a solve of the batch)");
   return CBNS_OK;
 }
 

@@ -149,6 +149,26 @@ __host__ __device__ inline const Consts<float>& consts_of<float>(const SolveDev&
   return s.cf;
 }
 
+// Bits of SolveCtl::status.
+constexpr int kStatusNonphysical = 1;  // a stage produced rho <= 0, p <= 0 or a NaN
+constexpr int kStatusBounds = 2;       // bounds-checked build: an index left its array
+
+// Element i of an array of n elements that belongs to solve s.  Every global
+// access of the stage kernels goes through here.  Built with CBNS_BOUNDS_CHECK,
+// an index outside [0, n) sets the solve's kStatusBounds bit and the access goes
+// to element 0 instead: no access outside the array is made and nothing traps,
+// so the host reads the bit after the launch.  Otherwise it is plain indexing.
+template <class T>
+__device__ __forceinline__ T& at(const SolveDev& s, T* base, long long n, long long i) {
+#ifdef CBNS_BOUNDS_CHECK
+  if (i < 0 || i >= n) {
+    atomicOr(&s.ctl->status, kStatusBounds);
+    i = 0;
+  }
+#endif
+  return base[i];
+}
+
 // Fill cd and cf from the binary64 parameters (host side, once per solve).
 inline void fill_consts(SolveDev& s) {
   Consts<double>& c = s.cd;
@@ -222,19 +242,6 @@ struct TileRef {
   uint16_t tk;
 };
 
-// Work of the face kernels: one warp walks a column of `count` consecutive
-// faces normal to D, starting at face `first`, for 32 lines of cells side by
-// side (lane l on line 32*blk + l).  The lines run along i for D = 1, 2 (k = c
-// for D = 1, j = c for D = 2) and along j for D = 0 (k = c).
-struct MarchRef {
-  uint16_t solve;
-  uint16_t blk;
-  uint16_t c;
-  uint16_t first;
-  uint16_t count;
-  uint16_t pad;
-};
-
 __host__ __device__ inline long long pad_off(const SolveDev& s, int i, int j, int k) {
   return (long long)(i + NG) + (long long)s.nx * ((long long)(j + NG) + (long long)s.ny * (k + NG));
 }
@@ -247,20 +254,14 @@ __host__ __device__ inline long long int_off(const SolveDev& s, int i, int j, in
 
 enum Domain { DOM_INTERIOR = 0, DOM_RING = 1, DOM_PADDED = 2 };
 
-// The work tables of one stage: interior tiles (update), NGV-ring tiles
-// (viscous terms) and, per direction, the face columns of the face kernels.
+// The work tables of one stage: interior tiles (face and update kernels) and
+// NGV-ring tiles (viscous terms).
 struct StageTables {
   const TileRef* tiles;
   int ntiles;
   const TileRef* ring;
   int nring;
-  const MarchRef* march[3];
-  int nmarch[3];
 };
-
-// Faces per column of the face kernels: a direction's extent E is cut into
-// ceil(E / kMarchFaces) columns of near-equal length.
-constexpr int kMarchFaces = 32;
 
 // Launch shape of the stage and dt kernels: tile rows (CTA = 32 x tile_rows
 // threads) and, when > 0, a persistent grid of max_ctas CTAs walking the table.

@@ -39,8 +39,6 @@ struct cbns_handle {
   cbns::TileRef* d_tiles_ring = nullptr;
   cbns::TileRef* d_tiles_pad = nullptr;
   int n_int = 0, n_ring = 0, n_pad = 0;
-  cbns::MarchRef* d_march[3] = {nullptr, nullptr, nullptr};  // face columns per direction
-  int n_march[3] = {0, 0, 0};
   double* d_stage = nullptr;
   double* d_partials = nullptr;
   int nparts = 0;
@@ -73,8 +71,6 @@ struct cbns_batch {
   cbns::TileRef* d_ring[3] = {nullptr, nullptr, nullptr};
   int n_int[3] = {0, 0, 0};
   int n_ring[3] = {0, 0, 0};
-  cbns::MarchRef* d_march[3] = {nullptr, nullptr, nullptr};  // face columns per direction
-  int n_march[3] = {0, 0, 0};
   int sm_count = 0;
   cbns::LaunchCfg cfg;  // tile_rows, max_ctas (= ctas_per_sm * sm_count, 0 = one CTA per tile)
   int ctas_per_sm = 0;

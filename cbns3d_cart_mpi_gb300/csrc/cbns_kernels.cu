@@ -35,7 +35,6 @@
 
 #include <cmath>
 #include <cstdint>
-#include <cstdlib>
 
 #include "cbns_device.cuh"
 #include "cbns_modes.h"
@@ -112,14 +111,15 @@ __device__ __forceinline__ Prims64 prims64(const SolveDev& s, double r, double r
 __device__ __forceinline__ void store_prims(const SolveDev& s, long long o, double r, double ru,
                                             double rv, double rw, double E) {
   const Prims64 q = prims64(s, r, ru, rv, rw, E);
-  s.pd.rho[o] = r;
-  s.pd.u[o] = q.u;
-  s.pd.v[o] = q.v;
-  s.pd.w[o] = q.w;
-  s.pd.p[o] = q.p;
-  s.pd.T[o] = q.T;
-  s.pd.srho[o] = q.sr;
-  s.pd.H[o] = q.H;
+  const long long V = s.V;
+  at(s, s.pd.rho, V, o) = r;
+  at(s, s.pd.u, V, o) = q.u;
+  at(s, s.pd.v, V, o) = q.v;
+  at(s, s.pd.w, V, o) = q.w;
+  at(s, s.pd.p, V, o) = q.p;
+  at(s, s.pd.T, V, o) = q.T;
+  at(s, s.pd.srho, V, o) = q.sr;
+  at(s, s.pd.H, V, o) = q.H;
 }
 
 // FP32-mixed: the binary32 perturbation state and primitives of a binary64 state.
@@ -161,10 +161,10 @@ __device__ __forceinline__ MixedCell mixed_cell(const SolveDev& s, const double 
 // The packed binary32 state and primitives of one cell: four 16-byte stores and
 // one 4-byte store.
 __device__ __forceinline__ void store_mixed(const SolveDev& s, long long o, const MixedCell& m) {
-  s.U4[o] = make_float4(m.U[0], m.U[1], m.U[2], m.U[3]);
-  s.UE[o] = m.U[4];
-  s.PA[o] = make_float4(m.u, m.v, m.w, m.T);
-  s.PB[o] = make_float4(m.rho, m.p, m.srho, m.H);
+  at(s, s.U4, s.V, o) = make_float4(m.U[0], m.U[1], m.U[2], m.U[3]);
+  at(s, s.UE, s.V, o) = m.U[4];
+  at(s, s.PA, s.V, o) = make_float4(m.u, m.v, m.w, m.T);
+  at(s, s.PB, s.V, o) = make_float4(m.rho, m.p, m.srho, m.H);
 }
 
 __global__ void k_aos_to_soa(const SolveDev* __restrict__ solves, int sidx, const double* __restrict__ aos,
@@ -173,7 +173,7 @@ __global__ void k_aos_to_soa(const SolveDev* __restrict__ solves, int sidx, cons
   for (long long o = blockIdx.x * (long long)blockDim.x + threadIdx.x; o < s.V;
        o += (long long)gridDim.x * blockDim.x) {
 #pragma unroll
-    for (int n = 0; n < NEQ; ++n) soa[n * s.V + o] = aos[NEQ * o + n];
+    for (int n = 0; n < NEQ; ++n) at(s, soa, NEQ * s.V, n * s.V + o) = at(s, aos, NEQ * s.V, NEQ * o + n);
   }
 }
 
@@ -183,7 +183,7 @@ __global__ void k_soa_to_aos(const SolveDev* __restrict__ solves, int sidx, cons
   for (long long o = blockIdx.x * (long long)blockDim.x + threadIdx.x; o < s.V;
        o += (long long)gridDim.x * blockDim.x) {
 #pragma unroll
-    for (int n = 0; n < NEQ; ++n) aos[NEQ * o + n] = soa[n * s.V + o];
+    for (int n = 0; n < NEQ; ++n) at(s, aos, NEQ * s.V, NEQ * o + n) = at(s, soa, NEQ * s.V, n * s.V + o);
   }
 }
 
@@ -200,18 +200,18 @@ __global__ void k_prepare(const SolveDev* __restrict__ solves, const TileRef* __
     const long long src = pad_off(s, wrap(tc.i, s.IM), wrap(tc.j, s.JM), wrap(tc.k, s.KM));
     double q[NEQ];
 #pragma unroll
-    for (int n = 0; n < NEQ; ++n) q[n] = s.Q[n * s.V + src];
+    for (int n = 0; n < NEQ; ++n) q[n] = at(s, s.Q, NEQ * s.V, n * s.V + src);
 #pragma unroll
     for (int n = 0; n < NEQ; ++n) {
-      s.Q[n * s.V + o] = q[n];
-      s.Qp[n * s.V + o] = q[n];
+      at(s, s.Q, NEQ * s.V, n * s.V + o) = q[n];
+      at(s, s.Qp, NEQ * s.V, n * s.V + o) = q[n];
     }
     store_prims(s, o, q[0], q[1], q[2], q[3], q[4]);
     if (s.mixed) store_mixed(s, o, mixed_cell(s, q));
     const bool interior = tc.i >= 0 && tc.i < s.IM && tc.j >= 0 && tc.j < s.JM && tc.k >= 0 && tc.k < s.KM;
     if (interior) {
-      s.pd.mu[o] = 1.0;
-      if (s.mixed) s.muf[o] = 1.0f;
+      at(s, s.pd.mu, s.V, o) = 1.0;
+      if (s.mixed) at(s, s.muf, s.V, o) = 1.0f;
     }
   }
 }
@@ -250,11 +250,12 @@ __global__ void k_init_tgv(const SolveDev* __restrict__ solves, int sidx, const 
     const double p = p_inf + (cos(2.0 * xl) + cos(2.0 * yl)) * (cos(2.0 * zl) + 2.0) / 16.0;
     const double r = s.gM2 * p;
     const long long o = pad_off(s, tc.i, tc.j, tc.k);
-    s.Q[o] = r;
-    s.Q[s.V + o] = r * u;
-    s.Q[2 * s.V + o] = r * v;
-    s.Q[3 * s.V + o] = r * w;
-    s.Q[4 * s.V + o] = p / s.gam1 + 0.5 * r * (u * u + v * v + w * w);
+    const long long n5 = NEQ * s.V;
+    at(s, s.Q, n5, o) = r;
+    at(s, s.Q, n5, s.V + o) = r * u;
+    at(s, s.Q, n5, 2 * s.V + o) = r * v;
+    at(s, s.Q, n5, 3 * s.V + o) = r * w;
+    at(s, s.Q, n5, 4 * s.V + o) = p / s.gam1 + 0.5 * r * (u * u + v * v + w * w);
   }
 }
 
@@ -267,7 +268,9 @@ __global__ void k_prims_double(const SolveDev* __restrict__ solves, const TileRe
     const SolveDev& s = solves[tc.s];
     if (tc.i >= s.IM + NG || tc.j >= s.JM + NG) continue;
     const long long o = pad_off(s, tc.i, tc.j, tc.k);
-    store_prims(s, o, s.Q[o], s.Q[s.V + o], s.Q[2 * s.V + o], s.Q[3 * s.V + o], s.Q[4 * s.V + o]);
+    const long long n5 = NEQ * s.V;
+    store_prims(s, o, at(s, s.Q, n5, o), at(s, s.Q, n5, s.V + o), at(s, s.Q, n5, 2 * s.V + o),
+                at(s, s.Q, n5, 3 * s.V + o), at(s, s.Q, n5, 4 * s.V + o));
   }
 }
 
@@ -292,15 +295,16 @@ __device__ __forceinline__ R dt_speed(const SolveDev& s, long long o) {
   const Consts<R>& C = consts_of<R>(s);
   R rr, uu, vv, ww, pp, mu;
   if constexpr (sizeof(R) == 4) {
-    const float4 a = s.PA[o], b = s.PB[o];
+    const float4 a = at(s, s.PA, s.V, o), b = at(s, s.PB, s.V, o);
     rr = b.x, uu = a.x, vv = a.y, ww = a.z;
     pp = C.p_ref + b.y;
-    mu = s.muf[o];
+    mu = at(s, s.muf, s.V, o);
   } else {
     const PrimSet<double>& P = s.pd;
-    rr = P.rho[o], uu = P.u[o], vv = P.v[o], ww = P.w[o];
-    pp = P.p[o];
-    mu = P.mu[o];
+    const long long V = s.V;
+    rr = at(s, P.rho, V, o), uu = at(s, P.u, V, o), vv = at(s, P.v, V, o), ww = at(s, P.w, V, o);
+    pp = at(s, P.p, V, o);
+    mu = at(s, P.mu, V, o);
   }
   const R gp = C.gamma * pp;
   const R z = rsqrt(gp * rr);
@@ -469,7 +473,7 @@ __device__ __forceinline__ void weno5_pair(const R (&v)[6], Weno<R>& L, Weno<R>&
 // half lies in about [1e-150, 1e150] (biased exponent 525 .. 1520, tested on the
 // integer pipe), which keeps every partial product and partial reciprocal in
 // the normal range; otherwise each quotient is divided on its own.  (The
-// binary32 faces multiply by per-face reciprocals: face_flux_x2.)
+// binary32 faces multiply by per-face reciprocals: face_core_x2.)
 __device__ __forceinline__ void weno_divide10(const Weno<double> (&w)[10], const double (&base)[10],
                                               double (&r)[10]) {
   // Two halves of five: prefix products within each half, one reciprocal of the
@@ -518,7 +522,7 @@ __device__ __forceinline__ void weno_divide10(const Weno<double> (&w)[10], const
 //   E = H s + U_D c d + q^2/2 r1 + U_t1 r3 + U_t2 r4.
 // The Roe average (ratio = sqrt(rho_R/rho_L)) is formed from per-cell sqrt(rho).
 // lf_flux (src/lf_flux.cpp:32-99) takes the reconstructed conserved states.
-// Binary64; the FP32-mixed faces are face_flux_x2 below.
+// Binary64; the FP32-mixed faces are face_core_x2 below.
 
 // The stencil of one binary64 face normal to D: the conserved state of the six
 // cells c-3 .. c+2 (W[m][n], field n of cell c-3+m) and, of the two cells
@@ -529,7 +533,8 @@ struct FaceSide {
 
 __device__ __forceinline__ FaceSide face_side(const SolveDev& s, long long o) {
   const PrimSet<double>& P = s.pd;
-  return FaceSide{P.srho[o], P.H[o], P.u[o], P.v[o], P.w[o]};
+  const long long V = s.V;
+  return FaceSide{at(s, P.srho, V, o), at(s, P.H, V, o), at(s, P.u, V, o), at(s, P.v, V, o), at(s, P.w, V, o)};
 }
 
 template <int D>
@@ -653,7 +658,7 @@ __device__ __forceinline__ void face_core(const SolveDev& s, const double (&W)[6
 template <int D, typename R>
 __device__ __forceinline__ void face_flux(const SolveDev& s, const R* __restrict__ U, long long c,
                                           R (&out)[NEQ]) {
-  static_assert(sizeof(R) == 8, "binary64 faces; FP32-mixed faces are face_flux_x2");
+  static_assert(sizeof(R) == 8, "binary64 faces; FP32-mixed faces are face_core_x2");
   const long long st = D == 0 ? 1ll : (D == 1 ? (long long)s.nx : (long long)s.nx * s.ny);
   const long long V = s.V;
   double W[6][NEQ];
@@ -661,7 +666,7 @@ __device__ __forceinline__ void face_flux(const SolveDev& s, const R* __restrict
   for (int m = 0; m < 6; ++m) {
     const long long o = c + (m - 3) * st;
 #pragma unroll
-    for (int n = 0; n < NEQ; ++n) W[m][n] = U[n * V + o];
+    for (int n = 0; n < NEQ; ++n) W[m][n] = at(s, U, NEQ * V, n * V + o);
   }
   face_core<D>(s, W, face_side(s, c - st), face_side(s, c), out);
 }
@@ -730,27 +735,37 @@ __device__ __forceinline__ void weno5_pair_x2(const f2 (&v)[6], f2& numL, f2& de
                 fma2(k56, d3, mul2(mk13, d4)), fma2(two, d2, d3), fma2(two, d2, mul2(mhalf, d1)), numRn, denR);
 }
 
-template <int D>
-__device__ __forceinline__ void face_flux_x2(const SolveDev& s, long long c0, long long c1, f2 (&out)[NEQ]) {
+// The side of a face the Roe average takes from a cell, for both lanes:
+// velocity, sqrt(rho) and total enthalpy.
+struct SideX2 {
+  f2 u, v, w, sr, h;
+};
+
+__device__ __forceinline__ SideX2 side_x2(const float4& a0, const float4& b0, const float4& a1, const float4& b1) {
+  return SideX2{lanes(a0.x, a1.x), lanes(a0.y, a1.y), lanes(a0.z, a1.z), lanes(b0.z, b1.z), lanes(b0.w, b1.w)};
+}
+
+// Two binary32 faces normal to D in the lanes of f2: the Roe sides L and R of
+// each face and, through cell(m, f), the perturbation state f[0..4] of stencil
+// cell m = 0..5 (cells c-3 .. c+2 of each face's high cell c).
+template <int D, class CellFn>
+__device__ __forceinline__ void face_core_x2(const Consts<float>& C, const SideX2& Ls, const SideX2& Rs, CellFn cell,
+                                             f2 (&out)[NEQ]) {
   constexpr int T1 = (D + 1) % 3;
   constexpr int T2 = (D + 2) % 3;
-  const long long st = D == 0 ? 1ll : (D == 1 ? (long long)s.nx : (long long)s.nx * s.ny);
-  const Consts<float>& C = s.cf;
   const f2 gam1 = bc(C.gam1), half = bc(0.5f), mone = bc(-1.0f);
 
   // Roe average of the cells either side of each face
   f2 Uv[3], HH;
   {
-    const float4 al0 = s.PA[c0 - st], ar0 = s.PA[c0], bl0 = s.PB[c0 - st], br0 = s.PB[c0];
-    const float4 al1 = s.PA[c1 - st], ar1 = s.PA[c1], bl1 = s.PB[c1 - st], br1 = s.PB[c1];
-    const f2 sl = lanes(bl0.z, bl1.z), sr = lanes(br0.z, br1.z);
+    const f2 sl = Ls.sr, sr = Rs.sr;
     const f2 ssum = add2(sl, sr);
     const f2 wL = lanes(__fdividef(sl.v.x, ssum.v.x), __fdividef(sl.v.y, ssum.v.y));
-    const f2 ur = lanes(ar0.x, ar1.x), vr = lanes(ar0.y, ar1.y), wr = lanes(ar0.z, ar1.z), hr = lanes(br0.w, br1.w);
-    Uv[0] = fma2(wL, sub2(lanes(al0.x, al1.x), ur), ur);
-    Uv[1] = fma2(wL, sub2(lanes(al0.y, al1.y), vr), vr);
-    Uv[2] = fma2(wL, sub2(lanes(al0.z, al1.z), wr), wr);
-    HH = fma2(wL, sub2(lanes(bl0.w, bl1.w), hr), hr);
+    const f2 ur = Rs.u, vr = Rs.v, wr = Rs.w, hr = Rs.h;
+    Uv[0] = fma2(wL, sub2(Ls.u, ur), ur);
+    Uv[1] = fma2(wL, sub2(Ls.v, vr), vr);
+    Uv[2] = fma2(wL, sub2(Ls.w, wr), wr);
+    HH = fma2(wL, sub2(Ls.h, hr), hr);
   }
   const f2 q2 = fma2(Uv[2], Uv[2], fma2(Uv[1], Uv[1], mul2(Uv[0], Uv[0])));
   const f2 hq2 = mul2(half, q2);
@@ -767,10 +782,9 @@ __device__ __forceinline__ void face_flux_x2(const SolveDev& s, long long c0, lo
   f2 w[NEQ][6];
 #pragma unroll
   for (int m = 0; m < 6; ++m) {
-    const long long o0 = c0 + (m - 3) * st, o1 = c1 + (m - 3) * st;
-    const float4 a0 = s.U4[o0], a1 = s.U4[o1];
-    const f2 f0 = lanes(a0.x, a1.x), f1 = lanes(a0.y, a1.y), f2v = lanes(a0.z, a1.z), f3 = lanes(a0.w, a1.w);
-    const f2 f4 = lanes(s.UE[o0], s.UE[o1]);
+    f2 fc[NEQ];
+    cell(m, fc);
+    const f2 f0 = fc[0], f1 = fc[1], f2v = fc[2], f3 = fc[3], f4 = fc[4];
     const f2 fm[3] = {f1, f2v, f3};
     const f2 t = fma2(nU2, f3, fma2(nU1, f2v, fma2(nU0, f1, fma2(hq2, f0, f4))));
     const f2 A = mul2(K, t);
@@ -862,14 +876,28 @@ __global__ void __maxnreg__(128) k_inviscid_x2(const SolveDev* __restrict__ solv
     const bool pair = j + 1 < s.JM;
     const long long c0 = pad_off(s, i, j, k);
     const long long c1 = pair ? c0 + s.nx : c0;
+    const long long st = D == 0 ? 1ll : (D == 1 ? (long long)s.nx : (long long)s.nx * s.ny);
+    const long long V = s.V;
+    const SideX2 Ls = side_x2(at(s, s.PA, V, c0 - st), at(s, s.PB, V, c0 - st), at(s, s.PA, V, c1 - st),
+                              at(s, s.PB, V, c1 - st));
+    const SideX2 Rs = side_x2(at(s, s.PA, V, c0), at(s, s.PB, V, c0), at(s, s.PA, V, c1), at(s, s.PB, V, c1));
+    auto cell = [&](int m, f2(&fc)[NEQ]) {
+      const long long o0 = c0 + (m - 3) * st, o1 = c1 + (m - 3) * st;
+      const float4 a0 = at(s, s.U4, V, o0), a1 = at(s, s.U4, V, o1);
+      fc[0] = lanes(a0.x, a1.x);
+      fc[1] = lanes(a0.y, a1.y);
+      fc[2] = lanes(a0.z, a1.z);
+      fc[3] = lanes(a0.w, a1.w);
+      fc[4] = lanes(at(s, s.UE, V, o0), at(s, s.UE, V, o1));
+    };
     f2 f[NEQ];
-    face_flux_x2<D>(s, c0, c1, f);
+    face_core_x2<D>(s.cf, Ls, Rs, cell, f);
     float* F = s.Ff[D];
     const long long fo = int_off(s, i, j, k);
 #pragma unroll
     for (int n = 0; n < NEQ; ++n) {
-      F[n * s.IV + fo] = f[n].v.x;
-      if (pair) F[n * s.IV + fo + s.IM] = f[n].v.y;
+      at(s, F, NEQ * s.IV, n * s.IV + fo) = f[n].v.x;
+      if (pair) at(s, F, NEQ * s.IV, n * s.IV + fo + s.IM) = f[n].v.y;
     }
   }
 }
@@ -891,137 +919,8 @@ __global__ void __maxnreg__(128) k_inviscid(const SolveDev* __restrict__ solves,
     face_flux<D, R>(s, U, pad_off(s, tc.i, tc.j, tc.k), f);
     const long long fo = int_off(s, tc.i, tc.j, tc.k);
 #pragma unroll
-    for (int n = 0; n < NEQ; ++n) F[n * s.IV + fo] = f[n];
+    for (int n = 0; n < NEQ; ++n) at(s, F, NEQ * s.IV, n * s.IV + fo) = f[n];
   }
-}
-
-// Binary64 faces marching along D: each thread walks a column of consecutive
-// faces normal to D and keeps the six-cell stencil, so a face loads one new
-// cell (five conserved values) and the primitives of its high side instead of
-// six cells and both sides.  The loads of the next face are issued before the
-// current face is computed.  The arithmetic is face_core's, so the fluxes are
-// bitwise those of k_inviscid.
-//   VAR 1, 2: the stencil in registers (2: capped at 168 registers);
-//   VAR 3:    the stencil in a per-warp ring of 8 cells in shared memory, the
-//             next cell copied in by cp.async (no register held while in flight).
-constexpr int kRing = 8;  // ring slots per lane (7 needed: 6 stencil cells + the next)
-constexpr int kRingBytesPerWarp = kRing * NEQ * 32 * (int)sizeof(double);
-
-__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
-  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
-
-template <int D, int VAR>
-__device__ __forceinline__ void march_faces(const SolveDev* __restrict__ solves, const MarchRef* __restrict__ refs,
-                                            int nrefs, int stage) {
-  extern __shared__ double ring_mem[];
-  const int lane = (int)(threadIdx.x & 31);
-  const int wpb = (int)(blockDim.x >> 5);
-  double* ring = ring_mem + (size_t)(threadIdx.x >> 5) * (kRing * NEQ * 32) + lane;  // [slot][n] stride 32
-  for (int e = blockIdx.x * wpb + (int)(threadIdx.x >> 5); e < nrefs; e += gridDim.x * wpb) {
-    const MarchRef r = refs[e];
-    const SolveDev& s = solves[r.solve];
-    if (!s.ctl->active) continue;
-    const int line = 32 * r.blk + lane;
-    if (line >= (D == 0 ? s.JM : s.IM)) continue;
-    const int i = D == 0 ? r.first : line;
-    const int j = D == 0 ? line : (D == 1 ? r.first : r.c);
-    const int k = D == 2 ? r.first : r.c;
-    const long long st = D == 0 ? 1ll : (D == 1 ? (long long)s.nx : (long long)s.nx * s.ny);
-    const long long fst = D == 0 ? 1ll : (D == 1 ? (long long)s.IM : (long long)s.IM * s.JM);
-    const long long V = s.V, IV = s.IV;
-    const double* __restrict__ U = stage == 1 ? s.Q : s.Qp;
-    double* __restrict__ F = s.F[D];
-    long long c = pad_off(s, i, j, k);
-    long long fo = int_off(s, i, j, k);
-    FaceSide Ls = face_side(s, c - st);
-    FaceSide Ns = face_side(s, c);
-    const int nf = (int)r.count;
-    if constexpr (VAR == 3) {
-      // Cells of the column are numbered q = 0, 1, ... from c - 3 st; cell q
-      // sits in slot q % kRing.  Face f reads cells f .. f+5.
-#pragma unroll
-      for (int q = 0; q < 6; ++q)
-#pragma unroll
-        for (int n = 0; n < NEQ; ++n) cp_async8(ring + (q * NEQ + n) * 32, U + n * V + c + (q - 3) * st);
-      cp_async_commit();
-      for (int f = 0; f < nf; ++f) {
-        cp_async_wait_all();
-        if (f + 1 < nf) {
-          const int q = f + 6;
-#pragma unroll
-          for (int n = 0; n < NEQ; ++n)
-            cp_async8(ring + ((q & (kRing - 1)) * NEQ + n) * 32, U + n * V + c + 3 * st);
-          cp_async_commit();
-        }
-        const FaceSide Rs = Ns;
-        if (f + 1 < nf) Ns = face_side(s, c + st);
-        double W[6][NEQ];
-#pragma unroll
-        for (int m = 0; m < 6; ++m)
-#pragma unroll
-          for (int n = 0; n < NEQ; ++n) W[m][n] = ring[(((f + m) & (kRing - 1)) * NEQ + n) * 32];
-        double out[NEQ];
-        face_core<D>(s, W, Ls, Rs, out);
-#pragma unroll
-        for (int n = 0; n < NEQ; ++n) F[n * IV + fo] = out[n];
-        Ls = Rs;
-        c += st;
-        fo += fst;
-      }
-      cp_async_wait_all();
-    } else {
-      double W[6][NEQ];
-#pragma unroll
-      for (int m = 0; m < 5; ++m)
-#pragma unroll
-        for (int n = 0; n < NEQ; ++n) W[m][n] = U[n * V + c + (m - 3) * st];
-      double Nx[NEQ];
-#pragma unroll
-      for (int n = 0; n < NEQ; ++n) Nx[n] = U[n * V + c + 2 * st];
-      for (int f = 0; f < nf; ++f) {
-#pragma unroll
-        for (int n = 0; n < NEQ; ++n) W[5][n] = Nx[n];
-        const FaceSide Rs = Ns;
-        if (f + 1 < nf) {
-#pragma unroll
-          for (int n = 0; n < NEQ; ++n) Nx[n] = U[n * V + c + 3 * st];
-          Ns = face_side(s, c + st);
-        }
-        double out[NEQ];
-        face_core<D>(s, W, Ls, Rs, out);
-#pragma unroll
-        for (int n = 0; n < NEQ; ++n) F[n * IV + fo] = out[n];
-#pragma unroll
-        for (int m = 0; m < 5; ++m)
-#pragma unroll
-          for (int n = 0; n < NEQ; ++n) W[m][n] = W[m + 1][n];
-        Ls = Rs;
-        c += st;
-        fo += fst;
-      }
-    }
-  }
-}
-
-template <int D>
-__global__ void __launch_bounds__(kMaxThreads) k_inviscid_march(const SolveDev* __restrict__ solves,
-                                                                 const MarchRef* __restrict__ refs, int nrefs,
-                                                                 int stage) {
-  march_faces<D, 1>(solves, refs, nrefs, stage);
-}
-template <int D>
-__global__ void __maxnreg__(168) k_inviscid_march168(const SolveDev* __restrict__ solves,
-                                                      const MarchRef* __restrict__ refs, int nrefs, int stage) {
-  march_faces<D, 2>(solves, refs, nrefs, stage);
-}
-template <int D>
-__global__ void __maxnreg__(128) k_inviscid_march_ring(const SolveDev* __restrict__ solves,
-                                                        const MarchRef* __restrict__ refs, int nrefs, int stage) {
-  march_faces<D, 3>(solves, refs, nrefs, stage);
 }
 
 // ---------------------------------------------------------------------------
@@ -1035,8 +934,11 @@ __device__ __forceinline__ R d4v(R m2, R p2, R m1, R p1, R c12h, R c23h) {
   return (m2 - p2) * c12h + (p1 - m1) * c23h;
 }
 template <typename R>
-__device__ __forceinline__ R d4(const R* __restrict__ f, long long o, long long st, R c12h, R c23h) {
-  return d4v<R>(f[o - 2 * st], f[o + 2 * st], f[o - st], f[o + st], c12h, c23h);
+__device__ __forceinline__ R d4(const SolveDev& s, const R* __restrict__ f, long long o, long long st, R c12h,
+                               R c23h) {
+  const long long V = s.V;
+  return d4v<R>(at(s, f, V, o - 2 * st), at(s, f, V, o + 2 * st), at(s, f, V, o - st), at(s, f, V, o + st), c12h,
+                c23h);
 }
 // Register caps: 64 for binary64 (FP64-pipe bound; lower caps measured no
 // faster) and 40 for binary32 (memory bound; 4% faster than at 48, spills at 32).
@@ -1057,7 +959,8 @@ __global__ void __maxnreg__(sizeof(R) == 4 ? 40 : 64) k_viscous(const SolveDev* 
     if constexpr (MIXED) {
       // (u, v, w, T - T_ref) packed: four 16-byte loads per direction
       auto grad = [&](long long st, float c12h, float c23h, float& gu, float& gv, float& gw, float& gT) {
-        const float4 m2 = s.PA[o - 2 * st], p2 = s.PA[o + 2 * st], m1 = s.PA[o - st], p1 = s.PA[o + st];
+        const float4 m2 = at(s, s.PA, s.V, o - 2 * st), p2 = at(s, s.PA, s.V, o + 2 * st),
+                     m1 = at(s, s.PA, s.V, o - st), p1 = at(s, s.PA, s.V, o + st);
         gu = d4v(m2.x, p2.x, m1.x, p1.x, c12h, c23h);
         gv = d4v(m2.y, p2.y, m1.y, p1.y, c12h, c23h);
         gw = d4v(m2.z, p2.z, m1.z, p1.z, c12h, c23h);
@@ -1066,17 +969,17 @@ __global__ void __maxnreg__(sizeof(R) == 4 ? 40 : 64) k_viscous(const SolveDev* 
       grad(1, ax, bx, ux, vx, wx, Tx);
       grad(sy, ay, by, uy, vy, wy, Ty);
       grad(sz, az, bz, uz, vz, wz, Tz);
-      const float4 a = s.PA[o];
+      const float4 a = at(s, s.PA, s.V, o);
       uu = a.x, vv = a.y, ww = a.z;
       Tl = CS.T_ref + a.w;
     } else {
       const PrimSet<double>& P = s.pd;
-      ux = d4<R>(P.u, o, 1, ax, bx), uy = d4<R>(P.u, o, sy, ay, by), uz = d4<R>(P.u, o, sz, az, bz);
-      vx = d4<R>(P.v, o, 1, ax, bx), vy = d4<R>(P.v, o, sy, ay, by), vz = d4<R>(P.v, o, sz, az, bz);
-      wx = d4<R>(P.w, o, 1, ax, bx), wy = d4<R>(P.w, o, sy, ay, by), wz = d4<R>(P.w, o, sz, az, bz);
-      Tx = d4<R>(P.T, o, 1, ax, bx), Ty = d4<R>(P.T, o, sy, ay, by), Tz = d4<R>(P.T, o, sz, az, bz);
-      uu = P.u[o], vv = P.v[o], ww = P.w[o];
-      Tl = P.T[o];
+      ux = d4<R>(s, P.u, o, 1, ax, bx), uy = d4<R>(s, P.u, o, sy, ay, by), uz = d4<R>(s, P.u, o, sz, az, bz);
+      vx = d4<R>(s, P.v, o, 1, ax, bx), vy = d4<R>(s, P.v, o, sy, ay, by), vz = d4<R>(s, P.v, o, sz, az, bz);
+      wx = d4<R>(s, P.w, o, 1, ax, bx), wy = d4<R>(s, P.w, o, sy, ay, by), wz = d4<R>(s, P.w, o, sz, az, bz);
+      Tx = d4<R>(s, P.T, o, 1, ax, bx), Ty = d4<R>(s, P.T, o, sy, ay, by), Tz = d4<R>(s, P.T, o, sz, az, bz);
+      uu = at(s, P.u, s.V, o), vv = at(s, P.v, s.V, o), ww = at(s, P.w, s.V, o);
+      Tl = at(s, P.T, s.V, o);
     }
     const R C = CS.C_T_inf;
     // Sutherland's law, (1 + C) / (T + C) * T^1.5 (src/Block3d.cpp:777), as
@@ -1085,9 +988,9 @@ __global__ void __maxnreg__(sizeof(R) == 4 ? 40 : 64) k_viscous(const SolveDev* 
     const R mu = (((R)1 + C) * (Tl * Tl)) * rsqrt(Tl * (TC * TC));
     if (tc.i >= 0 && tc.i < s.IM && tc.j >= 0 && tc.j < s.JM && tc.k >= 0 && tc.k < s.KM) {
       if constexpr (MIXED) {
-        s.muf[o] = mu;
+        at(s, s.muf, s.V, o) = mu;
       } else {
-        s.pd.mu[o] = mu;
+        at(s, s.pd.mu, s.V, o) = mu;
       }
     }
     const R mr = mu * CS.Re_inv;
@@ -1107,21 +1010,20 @@ __global__ void __maxnreg__(sizeof(R) == 4 ? 40 : 64) k_viscous(const SolveDev* 
     const R ez = uu * txz + vv * tyz + ww * tzz - mk * Tz;
     if constexpr (MIXED) {
       // grouped by differencing direction: Ev, Fv, Gv as one float4 each
-      float4* g = s.Tvg + r;
-      g[0] = make_float4(txx, txy, txz, ex);
-      g[RV] = make_float4(txy, tyy, tyz, ey);
-      g[2 * RV] = make_float4(txz, tyz, tzz, ez);
+      at(s, s.Tvg, 3 * RV, r) = make_float4(txx, txy, txz, ex);
+      at(s, s.Tvg, 3 * RV, RV + r) = make_float4(txy, tyy, tyz, ey);
+      at(s, s.Tvg, 3 * RV, 2 * RV + r) = make_float4(txz, tyz, tzz, ez);
     } else {
-      double* tv = s.Tv + r;
-      tv[TXX * RV] = txx;
-      tv[TYY * RV] = tyy;
-      tv[TZZ * RV] = tzz;
-      tv[TXY * RV] = txy;
-      tv[TXZ * RV] = txz;
-      tv[TYZ * RV] = tyz;
-      tv[EX * RV] = ex;
-      tv[EY * RV] = ey;
-      tv[EZ * RV] = ez;
+      const long long n9 = kViscTerms * RV;
+      at(s, s.Tv, n9, TXX * RV + r) = txx;
+      at(s, s.Tv, n9, TYY * RV + r) = tyy;
+      at(s, s.Tv, n9, TZZ * RV + r) = tzz;
+      at(s, s.Tv, n9, TXY * RV + r) = txy;
+      at(s, s.Tv, n9, TXZ * RV + r) = txz;
+      at(s, s.Tv, n9, TYZ * RV + r) = tyz;
+      at(s, s.Tv, n9, EX * RV + r) = ex;
+      at(s, s.Tv, n9, EY * RV + r) = ey;
+      at(s, s.Tv, n9, EZ * RV + r) = ez;
     }
   }
 }
@@ -1177,17 +1079,19 @@ __device__ __forceinline__ void update_tiles(const SolveDev* __restrict__ solves
     // per direction.
     float dv[4] = {0.0f, 0.0f, 0.0f, 0.0f};
     if constexpr (MIXED) {
-      auto direction = [&](const float4* __restrict__ g, long long st, float c12, float c23) {
-        const float4 m2 = g[-2 * st], p2 = g[2 * st], m1 = g[-st], p1 = g[st];
+      // g: the direction's block of the grouped terms plus this ring point
+      auto direction = [&](long long g, long long st, float c12, float c23) {
+        const long long n3 = 3 * RV;
+        const float4 m2 = at(s, s.Tvg, n3, g - 2 * st), p2 = at(s, s.Tvg, n3, g + 2 * st),
+                     m1 = at(s, s.Tvg, n3, g - st), p1 = at(s, s.Tvg, n3, g + st);
         dv[0] = fmaf(p1.x - m1.x, -c23, fmaf(m2.x - p2.x, -c12, dv[0]));
         dv[1] = fmaf(p1.y - m1.y, -c23, fmaf(m2.y - p2.y, -c12, dv[1]));
         dv[2] = fmaf(p1.z - m1.z, -c23, fmaf(m2.z - p2.z, -c12, dv[2]));
         dv[3] = fmaf(p1.w - m1.w, -c23, fmaf(m2.w - p2.w, -c12, dv[3]));
       };
-      const float4* G = s.Tvg + r;
-      direction(G, 1, CS.c12x, CS.c23x);
-      direction(G + RV, ry, CS.c12y, CS.c23y);
-      direction(G + 2 * RV, rz, CS.c12z, CS.c23z);
+      direction(r, 1, CS.c12x, CS.c23x);
+      direction(RV + r, ry, CS.c12y, CS.c23y);
+      direction(2 * RV + r, rz, CS.c12z, CS.c23z);
     }
     double qn[NEQ];
 #pragma unroll
@@ -1195,33 +1099,37 @@ __device__ __forceinline__ void update_tiles(const SolveDev* __restrict__ solves
       R df;
       if constexpr (MIXED) {
         // the viscous part above, then the inviscid flux differences
-        df = fma_(F0[n * IV + fx] - F0[n * IV + fo], idx, n > 0 ? dv[n - 1] : 0.0f);
-        df = fma_(F1[n * IV + fy] - F1[n * IV + fo], idy, df);
-        df = fma_(F2[n * IV + fz] - F2[n * IV + fo], idz, df);
+        const long long n5 = NEQ * IV;
+        df = fma_(at(s, F0, n5, n * IV + fx) - at(s, F0, n5, n * IV + fo), idx, n > 0 ? dv[n - 1] : 0.0f);
+        df = fma_(at(s, F1, n5, n * IV + fy) - at(s, F1, n5, n * IV + fo), idy, df);
+        df = fma_(at(s, F2, n5, n * IV + fz) - at(s, F2, n5, n * IV + fo), idz, df);
       } else {
         // Inviscid flux differences, then minus the viscous divergence, as one
         // chain of fused multiply-adds with the 1/h-folded weights negated.
-        df = (F0[n * IV + fx] - F0[n * IV + fo]) * idx;
-        df = fma_(F1[n * IV + fy] - F1[n * IV + fo], idy, df);
-        df = fma_(F2[n * IV + fz] - F2[n * IV + fo], idz, df);
+        const long long n5 = NEQ * IV;
+        df = (at(s, F0, n5, n * IV + fx) - at(s, F0, n5, n * IV + fo)) * idx;
+        df = fma_(at(s, F1, n5, n * IV + fy) - at(s, F1, n5, n * IV + fo), idy, df);
+        df = fma_(at(s, F2, n5, n * IV + fz) - at(s, F2, n5, n * IV + fo), idz, df);
         if (n > 0) {
-          const double* vx = s.Tv + visc_term(n, 0) * RV;
-          const double* vy = s.Tv + visc_term(n, 1) * RV;
-          const double* vz = s.Tv + visc_term(n, 2) * RV;
-          df = fma_(vx[r - 2] - vx[r + 2], -CS.c12x, df);
-          df = fma_(vx[r + 1] - vx[r - 1], -CS.c23x, df);
-          df = fma_(vy[r - 2 * ry] - vy[r + 2 * ry], -CS.c12y, df);
-          df = fma_(vy[r + ry] - vy[r - ry], -CS.c23y, df);
-          df = fma_(vz[r - 2 * rz] - vz[r + 2 * rz], -CS.c12z, df);
-          df = fma_(vz[r + rz] - vz[r - rz], -CS.c23z, df);
+          // the term differenced along x, y, z in this equation: its block plus r
+          const long long n9 = kViscTerms * RV;
+          const long long vx = visc_term(n, 0) * RV + r, vy = visc_term(n, 1) * RV + r,
+                          vz = visc_term(n, 2) * RV + r;
+          const double* Tv = s.Tv;
+          df = fma_(at(s, Tv, n9, vx - 2) - at(s, Tv, n9, vx + 2), -CS.c12x, df);
+          df = fma_(at(s, Tv, n9, vx + 1) - at(s, Tv, n9, vx - 1), -CS.c23x, df);
+          df = fma_(at(s, Tv, n9, vy - 2 * ry) - at(s, Tv, n9, vy + 2 * ry), -CS.c12y, df);
+          df = fma_(at(s, Tv, n9, vy + ry) - at(s, Tv, n9, vy - ry), -CS.c23y, df);
+          df = fma_(at(s, Tv, n9, vz - 2 * rz) - at(s, Tv, n9, vz + 2 * rz), -CS.c12z, df);
+          df = fma_(at(s, Tv, n9, vz + rz) - at(s, Tv, n9, vz - rz), -CS.c23z, df);
         }
       }
-      const double q0 = s.Q[n * V + o];
+      const double q0 = at(s, s.Q, NEQ * V, n * V + o);
       if (MIXED && stage != 1) {
         // FP32-mixed stages 2 and 3: the increment c dt df in binary32 (df has
         // binary32 accuracy), the combination of the binary64 states in binary64:
         // 3/4 q0 + 1/4 qp - 1/4 dt df and 1/3 q0 + 2/3 qp - 2/3 dt df.
-        const double qp = s.Qp[n * V + o];
+        const double qp = at(s, s.Qp, NEQ * V, n * V + o);
         const double inc = (double)(cdt * (float)df);
         qn[n] = stage == 2 ? fma(0.75, q0, fma(0.25, qp, -inc)) : fma(1.0 / 3.0, q0, fma(2.0 / 3.0, qp, -inc));
       } else {
@@ -1229,9 +1137,9 @@ __device__ __forceinline__ void update_tiles(const SolveDev* __restrict__ solves
         if (stage == 1) {
           qn[n] = q0 - dt * dfd;
         } else if (stage == 2) {
-          qn[n] = 0.75 * q0 + 0.25 * (s.Qp[n * V + o] - dt * dfd);
+          qn[n] = 0.75 * q0 + 0.25 * (at(s, s.Qp, NEQ * V, n * V + o) - dt * dfd);
         } else {
-          qn[n] = (q0 + 2.0 * (s.Qp[n * V + o] - dt * dfd)) * (1.0 / 3.0);
+          qn[n] = (q0 + 2.0 * (at(s, s.Qp, NEQ * V, n * V + o) - dt * dfd)) * (1.0 / 3.0);
         }
       }
     }
@@ -1242,11 +1150,11 @@ __device__ __forceinline__ void update_tiles(const SolveDev* __restrict__ solves
     MixedCell mc;
     if constexpr (MIXED) {
       mc = mixed_cell(s, qn);
-      if (!(mc.rho > 0.0f) || !(s.cf.p_ref + mc.p > 0.0f)) atomicOr(&ctl->status, 1);
+      if (!(mc.rho > 0.0f) || !(s.cf.p_ref + mc.p > 0.0f)) atomicOr(&ctl->status, kStatusNonphysical);
     } else {
       const Prims64 q = prims64(s, qn[0], qn[1], qn[2], qn[3], qn[4]);
       uu = q.u, vv = q.v, ww = q.w, pp = q.p, TT = q.T, sr = q.sr, HH = q.H;
-      if (!(qn[0] > 0.0) || !(pp > 0.0)) atomicOr(&ctl->status, 1);
+      if (!(qn[0] > 0.0) || !(pp > 0.0)) atomicOr(&ctl->status, kStatusNonphysical);
     }
 
     // The cell itself, then its periodic images in the ghost layers: along each
@@ -1254,19 +1162,21 @@ __device__ __forceinline__ void update_tiles(const SolveDev* __restrict__ solves
     // below 2*NG).  Most cells have none, and take the first branch only.
     auto store = [&](long long d) {
 #pragma unroll
-      for (int n = 0; n < NEQ; ++n) out[n * V + d] = qn[n];
+      for (int n = 0; n < NEQ; ++n) at(s, out, NEQ * V, n * V + d) = qn[n];
       if constexpr (MIXED) {
         store_mixed(s, d, mc);
       } else {
-        double* b = s.pd.rho + d;  // consecutive PrimSet blocks, as in store_mixed
-        b[0] = qn[0];
-        b[V] = uu;
-        b[2 * V] = vv;
-        b[3 * V] = ww;
-        b[4 * V] = pp;
-        b[5 * V] = TT;
-        b[6 * V] = sr;
-        b[7 * V] = HH;
+        // the PrimSet arrays are consecutive blocks of V values from pd.rho
+        double* b = s.pd.rho;
+        const long long n8 = 8 * V;
+        at(s, b, n8, d) = qn[0];
+        at(s, b, n8, V + d) = uu;
+        at(s, b, n8, 2 * V + d) = vv;
+        at(s, b, n8, 3 * V + d) = ww;
+        at(s, b, n8, 4 * V + d) = pp;
+        at(s, b, n8, 5 * V + d) = TT;
+        at(s, b, n8, 6 * V + d) = sr;
+        at(s, b, n8, 7 * V + d) = HH;
       }
     };
     store(o);
@@ -1337,14 +1247,14 @@ __device__ __forceinline__ Comp warp_comp(Comp v) {
   return v;
 }
 
-__device__ __forceinline__ double vel(const double* Q, long long V, long long o, int n) {
-  return Q[n * V + o] / Q[o];
+__device__ __forceinline__ double vel(const SolveDev& s, const double* Q, long long V, long long o, int n) {
+  return at(s, Q, NEQ * V, n * V + o) / at(s, Q, NEQ * V, o);
 }
-__device__ __forceinline__ double dvel(const double* Q, long long V, long long o, long long st, int n,
-                                       double inv_h) {
+__device__ __forceinline__ double dvel(const SolveDev& s, const double* Q, long long V, long long o, long long st,
+                                       int n, double inv_h) {
   const double c12 = 1.0 / 12.0, c23 = 2.0 / 3.0;
-  return ((vel(Q, V, o - 2 * st, n) - vel(Q, V, o + 2 * st, n)) * c12 +
-          (vel(Q, V, o + st, n) - vel(Q, V, o - st, n)) * c23) * inv_h;
+  return ((vel(s, Q, V, o - 2 * st, n) - vel(s, Q, V, o + 2 * st, n)) * c12 +
+          (vel(s, Q, V, o + st, n) - vel(s, Q, V, o - st, n)) * c23) * inv_h;
 }
 
 __global__ void __launch_bounds__(TILE_THREADS) k_diag(const SolveDev* __restrict__ solves, int sidx,
@@ -1359,11 +1269,11 @@ __global__ void __launch_bounds__(TILE_THREADS) k_diag(const SolveDev* __restric
     const long long o = pad_off(s, tc.i, tc.j, tc.k);
     const long long V = s.V, sy = s.nx, sz = (long long)s.nx * s.ny;
     const double* Q = s.Q;
-    const double r = Q[o];
-    const double u = vel(Q, V, o, 1), v = vel(Q, V, o, 2), w = vel(Q, V, o, 3);
-    const double wxc = dvel(Q, V, o, sy, 3, s.inv_dy) - dvel(Q, V, o, sz, 2, s.inv_dz);
-    const double wyc = dvel(Q, V, o, sz, 1, s.inv_dz) - dvel(Q, V, o, 1, 3, s.inv_dx);
-    const double wzc = dvel(Q, V, o, 1, 2, s.inv_dx) - dvel(Q, V, o, sy, 1, s.inv_dy);
+    const double r = at(s, Q, NEQ * V, o);
+    const double u = vel(s, Q, V, o, 1), v = vel(s, Q, V, o, 2), w = vel(s, Q, V, o, 3);
+    const double wxc = dvel(s, Q, V, o, sy, 3, s.inv_dy) - dvel(s, Q, V, o, sz, 2, s.inv_dz);
+    const double wyc = dvel(s, Q, V, o, sz, 1, s.inv_dz) - dvel(s, Q, V, o, 1, 3, s.inv_dx);
+    const double wzc = dvel(s, Q, V, o, 1, 2, s.inv_dx) - dvel(s, Q, V, o, sy, 1, s.inv_dy);
     ke = comp_add(ke, Comp{0.5 * r * (u * u + v * v + w * w), 0.0});
     en = comp_add(en, Comp{0.5 * r * (wxc * wxc + wyc * wyc + wzc * wzc), 0.0});
   }
@@ -1505,21 +1415,6 @@ cudaError_t launch_set_dt(const SolveDev* d, int sidx, double dt, cudaStream_t s
   return cudaGetLastError();
 }
 
-// Face columns (one per warp) of the marching face kernels: CTAs of
-// cfg.tile_rows warps, persistent when cfg.max_ctas is set.
-static int march_grid(int nmarch, const LaunchCfg& cfg) {
-  return grid_for((nmarch + cfg.tile_rows - 1) / cfg.tile_rows, cfg.max_ctas);
-}
-
-static int face_march_mode() {
-  static int mode = -1;
-  if (mode < 0) {
-    const char* e = std::getenv("CBNS_FACE_MARCH");
-    mode = e ? std::atoi(e) : 1;
-  }
-  return mode;
-}
-
 template <typename R>
 static void stage_ty(const SolveDev* d, const StageTables& T, int stage, const LaunchCfg& cfg, cudaStream_t st,
                      Profiler* pf) {
@@ -1532,35 +1427,6 @@ static void stage_ty(const SolveDev* d, const StageTables& T, int stage, const L
     CBNS_LAUNCH(pf, KID_INVISCID_X, st, (k_inviscid_x2<0><<<g, nt2, 0, st>>>(d, tiles, ntiles)));
     CBNS_LAUNCH(pf, KID_INVISCID_Y, st, (k_inviscid_x2<1><<<g, nt2, 0, st>>>(d, tiles, ntiles)));
     CBNS_LAUNCH(pf, KID_INVISCID_Z, st, (k_inviscid_x2<2><<<g, nt2, 0, st>>>(d, tiles, ntiles)));
-  } else if (face_march_mode() == 1) {
-    CBNS_LAUNCH(pf, KID_INVISCID_X, st,
-                (k_inviscid_march<0><<<march_grid(T.nmarch[0], cfg), nt, 0, st>>>(d, T.march[0], T.nmarch[0], stage)));
-    CBNS_LAUNCH(pf, KID_INVISCID_Y, st,
-                (k_inviscid_march<1><<<march_grid(T.nmarch[1], cfg), nt, 0, st>>>(d, T.march[1], T.nmarch[1], stage)));
-    CBNS_LAUNCH(pf, KID_INVISCID_Z, st,
-                (k_inviscid_march<2><<<march_grid(T.nmarch[2], cfg), nt, 0, st>>>(d, T.march[2], T.nmarch[2], stage)));
-  } else if (face_march_mode() == 2) {
-    CBNS_LAUNCH(pf, KID_INVISCID_X, st,
-                (k_inviscid_march168<0><<<march_grid(T.nmarch[0], cfg), nt, 0, st>>>(d, T.march[0], T.nmarch[0], stage)));
-    CBNS_LAUNCH(pf, KID_INVISCID_Y, st,
-                (k_inviscid_march168<1><<<march_grid(T.nmarch[1], cfg), nt, 0, st>>>(d, T.march[1], T.nmarch[1], stage)));
-    CBNS_LAUNCH(pf, KID_INVISCID_Z, st,
-                (k_inviscid_march168<2><<<march_grid(T.nmarch[2], cfg), nt, 0, st>>>(d, T.march[2], T.nmarch[2], stage)));
-  } else if (face_march_mode() == 3) {
-    static bool attr = false;
-    const int smem = cfg.tile_rows * kRingBytesPerWarp;
-    if (!attr) {
-      cudaFuncSetAttribute(k_inviscid_march_ring<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, 8 * kRingBytesPerWarp);
-      cudaFuncSetAttribute(k_inviscid_march_ring<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 8 * kRingBytesPerWarp);
-      cudaFuncSetAttribute(k_inviscid_march_ring<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 8 * kRingBytesPerWarp);
-      attr = true;
-    }
-    CBNS_LAUNCH(pf, KID_INVISCID_X, st,
-                (k_inviscid_march_ring<0><<<march_grid(T.nmarch[0], cfg), nt, smem, st>>>(d, T.march[0], T.nmarch[0], stage)));
-    CBNS_LAUNCH(pf, KID_INVISCID_Y, st,
-                (k_inviscid_march_ring<1><<<march_grid(T.nmarch[1], cfg), nt, smem, st>>>(d, T.march[1], T.nmarch[1], stage)));
-    CBNS_LAUNCH(pf, KID_INVISCID_Z, st,
-                (k_inviscid_march_ring<2><<<march_grid(T.nmarch[2], cfg), nt, smem, st>>>(d, T.march[2], T.nmarch[2], stage)));
   } else {
     CBNS_LAUNCH(pf, KID_INVISCID_X, st, (k_inviscid<0, R><<<g, nt, 0, st>>>(d, tiles, ntiles, stage)));
     CBNS_LAUNCH(pf, KID_INVISCID_Y, st, (k_inviscid<1, R><<<g, nt, 0, st>>>(d, tiles, ntiles, stage)));

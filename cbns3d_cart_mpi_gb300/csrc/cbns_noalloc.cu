@@ -68,15 +68,36 @@ __device__ __forceinline__ Pair warp_pair(Pair v) {
   return v;
 }
 
-// Q in the reference's layout: Q[n + 5*((NG+i) + IM_G*((NG+j) + JM_G*(NG+k)))].
-__device__ __forceinline__ double velocity(const double* Q, long long c, int n) {
-  return Q[NEQ * c + n] / Q[NEQ * c];
+#ifdef CBNS_BOUNDS_CHECK
+// Bounds-checked build: accesses outside an array counted here (and sent to
+// element 0 instead); the entry point reads and clears the count after its
+// kernels.
+static __device__ unsigned long long g_noalloc_misses;
+#endif
+
+// Element i of an array of n elements (plain indexing unless CBNS_BOUNDS_CHECK).
+template <class T>
+__device__ __forceinline__ T& elem(T* base, long long n, long long i) {
+#ifdef CBNS_BOUNDS_CHECK
+  if (i < 0 || i >= n) {
+    atomicAdd(&g_noalloc_misses, 1ull);
+    i = 0;
+  }
+#endif
+  return base[i];
 }
 
-__device__ __forceinline__ double ddir(const double* Q, long long c, long long st, int n, double inv_h) {
+// Q in the reference's layout: Q[n + 5*((NG+i) + IM_G*((NG+j) + JM_G*(NG+k)))],
+// nQ values in all.
+__device__ __forceinline__ double velocity(const double* Q, long long nQ, long long c, int n) {
+  return elem(Q, nQ, NEQ * c + n) / elem(Q, nQ, NEQ * c);
+}
+
+__device__ __forceinline__ double ddir(const double* Q, long long nQ, long long c, long long st, int n,
+                                       double inv_h) {
   const double c12 = 1.0 / 12.0, c23 = 2.0 / 3.0;
-  return ((velocity(Q, c - 2 * st, n) - velocity(Q, c + 2 * st, n)) * c12 +
-          (velocity(Q, c + st, n) - velocity(Q, c - st, n)) * c23) * inv_h;
+  return ((velocity(Q, nQ, c - 2 * st, n) - velocity(Q, nQ, c + 2 * st, n)) * c12 +
+          (velocity(Q, nQ, c + st, n) - velocity(Q, nQ, c - st, n)) * c23) * inv_h;
 }
 
 __global__ void __launch_bounds__(NOALLOC_THREADS)
@@ -86,6 +107,7 @@ __global__ void __launch_bounds__(NOALLOC_THREADS)
   const long long ncell = (long long)IM * JM * KM;
   const long long IM_G = IM + 2 * NG, JM_G = JM + 2 * NG;
   const long long sy = IM_G, sz = IM_G * JM_G;
+  const long long nQ = NEQ * IM_G * JM_G * (long long)(KM + 2 * NG);
   Pair ke{0.0, 0.0}, en{0.0, 0.0};
   const long long first = (long long)blockIdx.x * NOALLOC_CELLS_PER_CTA;
   for (int r = 0; r < NOALLOC_CELLS_PER_THREAD; ++r) {
@@ -95,11 +117,11 @@ __global__ void __launch_bounds__(NOALLOC_THREADS)
     const int j = (int)((q / IM) % JM);
     const int k = (int)(q / ((long long)IM * JM));
     const long long c = (NG + i) + IM_G * ((NG + j) + JM_G * (long long)(NG + k));
-    const double rho = Q[NEQ * c];
-    const double u = velocity(Q, c, 1), v = velocity(Q, c, 2), w = velocity(Q, c, 3);
-    const double ox = ddir(Q, c, sy, 3, inv_dy) - ddir(Q, c, sz, 2, inv_dz);
-    const double oy = ddir(Q, c, sz, 1, inv_dz) - ddir(Q, c, 1, 3, inv_dx);
-    const double oz = ddir(Q, c, 1, 2, inv_dx) - ddir(Q, c, sy, 1, inv_dy);
+    const double rho = elem(Q, nQ, NEQ * c);
+    const double u = velocity(Q, nQ, c, 1), v = velocity(Q, nQ, c, 2), w = velocity(Q, nQ, c, 3);
+    const double ox = ddir(Q, nQ, c, sy, 3, inv_dy) - ddir(Q, nQ, c, sz, 2, inv_dz);
+    const double oy = ddir(Q, nQ, c, sz, 1, inv_dz) - ddir(Q, nQ, c, 1, 3, inv_dx);
+    const double oz = ddir(Q, nQ, c, 1, 2, inv_dx) - ddir(Q, nQ, c, sy, 1, inv_dy);
     ke = pair_add(ke, Pair{0.5 * rho * (u * u + v * v + w * w), 0.0});
     en = pair_add(en, Pair{0.5 * rho * (ox * ox + oy * oy + oz * oz), 0.0});
   }
@@ -116,10 +138,11 @@ __global__ void __launch_bounds__(NOALLOC_THREADS)
       a = pair_add(a, red[0][t]);
       b = pair_add(b, red[1][t]);
     }
-    partials[4 * blockIdx.x + 0] = a.s;
-    partials[4 * blockIdx.x + 1] = a.e;
-    partials[4 * blockIdx.x + 2] = b.s;
-    partials[4 * blockIdx.x + 3] = b.e;
+    const long long np = 4 * NOALLOC_MAX_CTAS;
+    elem(partials, np, 4 * blockIdx.x + 0) = a.s;
+    elem(partials, np, 4 * blockIdx.x + 1) = a.e;
+    elem(partials, np, 4 * blockIdx.x + 2) = b.s;
+    elem(partials, np, 4 * blockIdx.x + 3) = b.e;
   }
 }
 
@@ -128,8 +151,9 @@ __global__ void __launch_bounds__(1024)
   __shared__ Pair red[2][32];
   Pair ke{0.0, 0.0}, en{0.0, 0.0};
   for (int q = threadIdx.x; q < nparts; q += blockDim.x) {
-    ke = pair_add(ke, Pair{partials[4 * q], partials[4 * q + 1]});
-    en = pair_add(en, Pair{partials[4 * q + 2], partials[4 * q + 3]});
+    const long long np = 4 * NOALLOC_MAX_CTAS;
+    ke = pair_add(ke, Pair{elem(partials, np, 4 * q), elem(partials, np, 4 * q + 1)});
+    en = pair_add(en, Pair{elem(partials, np, 4 * q + 2), elem(partials, np, 4 * q + 3)});
   }
   ke = warp_pair(ke);
   en = warp_pair(en);
@@ -205,5 +229,18 @@ extern "C" cbns_status cbns_diagnostics_noalloc(const double* Q_dev, uint32_t IM
   e = cudaGetLastError();
   if (e != cudaSuccess)
     return noalloc_fail(CBNS_ERR_CUDA, std::string("cbns_diagnostics_noalloc: launch: ") + cudaGetErrorString(e));
+#ifdef CBNS_BOUNDS_CHECK
+  // Bounds-checked build only: wait for the kernels and report any access that
+  // left its array.
+  unsigned long long misses = 0;
+  const unsigned long long zero = 0;
+  if ((e = cudaStreamSynchronize(st)) != cudaSuccess ||
+      (e = cudaMemcpyFromSymbol(&misses, g_noalloc_misses, sizeof misses)) != cudaSuccess ||
+      (e = cudaMemcpyToSymbol(g_noalloc_misses, &zero, sizeof zero)) != cudaSuccess)
+    return noalloc_fail(CBNS_ERR_CUDA, std::string("cbns_diagnostics_noalloc: ") + cudaGetErrorString(e));
+  if (misses)
+    return noalloc_fail(CBNS_ERR_BOUNDS, "cbns_diagnostics_noalloc: " + std::to_string(misses) +
+                                             " accesses outside their arrays");
+#endif
   return CBNS_OK;
 }

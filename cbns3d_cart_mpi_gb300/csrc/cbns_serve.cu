@@ -218,7 +218,10 @@ void worker_loop(cbns_server* sv) {
         std::lock_guard<std::mutex> lk(sv->mu);
         cancel = r->cancel;
       }
-      if (c.status) retire(sv, r, CBNS_ERR_NONPHYSICAL, "non-physical state (rho <= 0, p <= 0 or NaN)");
+      if (c.status & cbns::kStatusBounds)
+        retire(sv, r, CBNS_ERR_BOUNDS, "a kernel index left its array (bounds-checked build)");
+      else if (c.status)
+        retire(sv, r, CBNS_ERR_NONPHYSICAL, "non-physical state (rho <= 0, p <= 0 or NaN)");
       else if (cancel) retire(sv, r, CBNS_ERR_CANCELLED, "cancelled");
       else if (!c.active) retire(sv, r, CBNS_OK, "");
       else still.push_back(r);

@@ -43,7 +43,8 @@ typedef enum cbns_status {
   CBNS_ERR_NO_DEVICE = -7,        /* no CUDA device, or not an sm_103 device */
   CBNS_ERR_IO = -8,               /* host file could not be read or written */
   CBNS_ERR_FORMAT = -9,           /* host file is truncated or its dimensions do not match */
-  CBNS_ERR_CANCELLED = -10        /* a serving request was cancelled or its server stopped */
+  CBNS_ERR_CANCELLED = -10,       /* a serving request was cancelled or its server stopped */
+  CBNS_ERR_BOUNDS = -11           /* bounds-checked build only: a kernel index left its array */
 } cbns_status;
 
 typedef enum cbns_precision {
