@@ -1,8 +1,9 @@
 """Serving benchmark: Poisson-arrival solve requests through the continuous-batching server.
 
   python -m cbns3d_cart_mpi_gb300.serve [--rates 0.25,0.5,1] [--requests 24] [--precision fp32_mixed]
+                                        [--grids 32:192:16]
 
-Each request: grid N per axis uniform in {32, 48, ..., 192}, Re log-uniform in
+Each request: grid N per axis uniform in {32, 48, ..., 192} (--grids), Re log-uniform in
 [400, 3200], Ma uniform in [0.05, 0.3], the Taylor-Green state plus a seeded
 solenoidal perturbation (16 modes, |k| <= 4, amplitude 1e-3) built on the
 device, run to t = 1.  Arrivals are a Poisson process at each swept rate
@@ -25,11 +26,11 @@ from .solver import Server
 GRIDS = tuple(range(32, 193, 16))
 
 
-def draw(n, seed):
+def draw(n, seed, grids=GRIDS):
     rng = np.random.default_rng(seed)
     out = []
     for i in range(n):
-        out.append({"N": int(rng.choice(GRIDS)),
+        out.append({"N": int(rng.choice(grids)),
                     "Re": float(math.exp(rng.uniform(math.log(400.0), math.log(3200.0)))),
                     "Mach": float(rng.uniform(0.05, 0.3)), "seed": 5000 + i})
     return out
@@ -77,10 +78,14 @@ def main():
     ap.add_argument("--t-end", type=float, default=1.0)
     ap.add_argument("--steps-per-round", type=int, default=20)
     ap.add_argument("--memory-budget-gb", type=float, default=0.0)
+    ap.add_argument("--grids", default="32:192:16", help="first:last:step of the grid sizes N drawn from")
     args = ap.parse_args()
-    reqs = draw(args.requests, args.seed)
-    out = {"workload": "Poisson solve requests, N in 32..192 step 16, Re log-U[400,3200], Ma U[0.05,0.3], "
-                       "TGV + 1e-3 solenoidal perturbation built on the device, run to t=%g" % args.t_end,
+    g0, g1, gs = (int(x) for x in args.grids.split(":"))
+    grids = tuple(range(g0, g1 + 1, gs))
+    reqs = draw(args.requests, args.seed, grids)
+    out = {"workload": "Poisson solve requests, N in %d..%d step %d, Re log-U[400,3200], Ma U[0.05,0.3], "
+                       "TGV + 1e-3 solenoidal perturbation built on the device, run to t=%g" % (
+                           g0, g1, gs, args.t_end),
            "precision": args.precision, "steps_per_round": args.steps_per_round, "rates": []}
     for k, rate in enumerate(float(x) for x in args.rates.split(",")):
         out["rates"].append(run_rate(rate, reqs, args.precision, args.seed + k, args.t_end, args.steps_per_round,
