@@ -156,6 +156,8 @@ def probe():
         _probe = ctypes.CDLL(PROBE_LIB)
         _probe.cbns_probe_peak.restype = c_int
         _probe.cbns_probe_peak.argtypes = [c_int, c_dp]
+        _probe.cbns_probe_rcp64.restype = c_int
+        _probe.cbns_probe_rcp64.argtypes = [c_vp, c_vp, c_vp, ctypes.c_longlong]
     return _probe
 
 

@@ -490,7 +490,7 @@ __device__ __forceinline__ void weno_divide10(const Weno<double> (&w)[10], const
   const unsigned ea = (unsigned)((unsigned long long)__double_as_longlong(pa[4]) >> 52);
   const unsigned eb = (unsigned)((unsigned long long)__double_as_longlong(pb[4]) >> 52);
   if (ea - 525u < 996u && eb - 525u < 996u) {
-    const double inv = 1.0 / (pa[4] * pb[4]);
+    const double inv = rcp64(pa[4] * pb[4]);
     double ia = inv * pb[4], ib = inv * pa[4];  // 1/pa[4], 1/pb[4]
 #pragma unroll
     for (int n = 4; n > 0; --n) {
@@ -552,7 +552,7 @@ __device__ __forceinline__ void face_core(const SolveDev& s, const double (&W)[6
   {
     const R sl = Ls.sr, sr = Rs.sr, hl = Ls.h, hr = Rs.h;
     const R ul = Ls.u, ur = Rs.u, vl = Ls.v, vr = Rs.v, wl = Ls.w, wr = Rs.w;
-    const R wL = div_(sl, sl + sr);
+    const R wL = sl * rcp64(sl + sr);
     Uv[0] = fma_(wL, ul - ur, ur);
     Uv[1] = fma_(wL, vl - vr, vr);
     Uv[2] = fma_(wL, wl - wr, wr);
@@ -627,7 +627,7 @@ __device__ __forceinline__ void face_core(const SolveDev& s, const double (&W)[6
   // Local Lax-Friedrichs flux (src/lf_flux.cpp:32-99); both 1/rho from one division.
   // The stored flux is twice the reference's: the halves are folded into the
   // flux difference's 0.5/h (an exact power-of-two scaling).
-  const R ip = div_((R)1, rhoL * rhoR);
+  const R ip = rcp64(rhoL * rhoR);
   const R iL = ip * rhoR, iR = ip * rhoL;
   R vL[3], vR[3];
 #pragma unroll

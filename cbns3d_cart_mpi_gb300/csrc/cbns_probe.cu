@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 
 #include "../../include/cbns_gpu.h"
+#include "cbns_device.cuh"
 
 namespace {
 
@@ -61,4 +62,22 @@ cbns_status probe(int iters, double* tflops) {
 extern "C" cbns_status cbns_probe_peak(int fp64, double* tflops) {
   if (!tflops) return CBNS_ERR_INVALID_ARG;
   return fp64 ? probe<double>(4096, tflops) : probe<float>(65536, tflops);
+}
+
+namespace {
+__global__ void k_rcp64(const double* __restrict__ x, double* __restrict__ y, double* __restrict__ ref, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    y[i] = cbns::rcp64(x[i]);
+    ref[i] = 1.0 / x[i];
+  }
+}
+}  // namespace
+
+// The face kernel's reciprocal and the IEEE division 1.0/x of n device values
+// (test of its accuracy); device pointers, synchronous.
+extern "C" cbns_status cbns_probe_rcp64(const double* x, double* y, double* ref, long long n) {
+  if (!x || !y || !ref || n < 0) return CBNS_ERR_INVALID_ARG;
+  if (n == 0) return CBNS_OK;
+  k_rcp64<<<1024, 256>>>(x, y, ref, n);
+  return cudaDeviceSynchronize() == cudaSuccess ? CBNS_OK : CBNS_ERR_CUDA;
 }

@@ -257,3 +257,30 @@ def test_parameter_corners_vs_oracle(Re, Mach, shape, seed):
         dto, to = o.step()
         assert abs(dt - dto) <= 1e-13 * dto, n
     assert_close(interior(s.download_Q()), interior(o.get_Q()), 1e-11, "Re %g Ma %g" % (Re, Mach), tight=1e-13)
+
+
+def test_face_reciprocal_within_one_ulp_of_ieee_division():
+    """The face kernel's reciprocal (Newton-Raphson from the hardware estimate,
+    csrc/cbns_device.cuh rcp64) against CUDA's IEEE 1.0/x on the GPU: at most one
+    ulp apart, over values log-uniform in [1e-150, 1e150] (the range the WENO
+    normalisation's product is admitted to) and uniform in [0.1, 10] (densities,
+    sums of sqrt(rho))."""
+    import ctypes
+
+    import torch
+
+    from cbns3d_cart_mpi_gb300 import _lib
+    rng = np.random.default_rng(7)
+    x = np.concatenate([10.0 ** rng.uniform(-150, 150, 1 << 20), rng.uniform(0.1, 10.0, 1 << 20)])
+    dev = torch.device("cuda", torch.cuda.current_device())
+    xd = torch.from_numpy(x).to(dev)
+    y = torch.empty_like(xd)
+    ref = torch.empty_like(xd)
+    st = _lib.probe().cbns_probe_rcp64(ctypes.c_void_p(xd.data_ptr()), ctypes.c_void_p(y.data_ptr()),
+                                       ctypes.c_void_p(ref.data_ptr()), x.size)
+    assert st == 0
+    yb = y.cpu().numpy().view(np.int64)
+    rb = ref.cpu().numpy().view(np.int64)
+    ulps = np.abs(yb - rb)
+    print("rcp64 vs 1.0/x: max %d ulp, %.3g of values differ" % (ulps.max(), (ulps > 0).mean()))
+    assert ulps.max() <= 1
