@@ -361,13 +361,10 @@ def run_ours(args, rank, world, local):
                 # binary32 arithmetic: its compulsory bytes against the measured HBM peak.
                 hbm, hbm_src = hbm_peak()
                 mbytes = mixed_update_bytes(N, N, N)
-                # ncu measured one stage-1 launch at 256^3; scaled to the three-stage
-                # average by the compulsory bytes (stages 2-3 also read Q_p).
-                t1 = ncu_counts().get("update_f32_stage1")
-                traffic = t1 * mbytes / (251.0 * N ** 3) if (t1 and N == 256) else None
+                # ncu DRAM bytes of the three update launches of one step at 256^3, averaged.
+                traffic = ncu_counts().get("update_f32") if N == 256 else None
                 mroof = {"bound": "hbm", "kernel": mdom, "achieved": mbytes / (mper * 1e-3) * 1e-9, "peak": hbm,
                          "unit": "GB/s", "frac": mbytes / (mper * 1e-3) * 1e-9 / hbm, "traffic": traffic,
-                         "traffic_stage1_measured": t1 if N == 256 else None,
                          "algorithmic_bytes_per_launch": mbytes, "peak_source": hbm_src,
                          "bytes_count": "compulsory bytes per cell by stage (workload.MIXED_UPDATE_BYTES_PER_CELL)"}
             else:

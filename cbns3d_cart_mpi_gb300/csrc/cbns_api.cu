@@ -558,22 +558,25 @@ cbns_status cbns_run(cbns_handle* h, uint32_t nsteps, double t_end, uint32_t* st
 // state then runs under the current step's kernels, and the download of a
 // result under the next step's.
 
+// Each piece is made once; a call that failed part-way resumes where it stopped.
 static cbns_status ensure_async(cbns_handle* h) {
   if (h->down_stream) return CBNS_OK;
-  const size_t bytes = sizeof(double) * NEQ * (size_t)h->desc.V;
-  cudaError_t e = cudaMalloc(&h->d_stage_out, bytes);
-  if (e != cudaSuccess) {
-    h->d_stage_out = nullptr;
-    return cuda_fail(e, "cudaMalloc(download staging)");
+  if (!h->d_stage_out) {
+    const size_t bytes = sizeof(double) * NEQ * (size_t)h->desc.V;
+    cudaError_t e = cudaMalloc(&h->d_stage_out, bytes);
+    if (e != cudaSuccess) {
+      h->d_stage_out = nullptr;
+      return cuda_fail(e, "cudaMalloc(download staging)");
+    }
+    h->arena_bytes += bytes;
   }
-  h->arena_bytes += bytes;
   for (cudaEvent_t* ev : {&h->ev_in_ready, &h->ev_in_free, &h->ev_out_ready, &h->ev_out_free})
-    CBNS_CUDA(cudaEventCreateWithFlags(ev, cudaEventDisableTiming));
-  CBNS_CUDA(cudaStreamCreateWithFlags(&h->up_stream, cudaStreamNonBlocking));
-  CBNS_CUDA(cudaStreamCreateWithFlags(&h->down_stream, cudaStreamNonBlocking));
+    if (!*ev) CBNS_CUDA(cudaEventCreateWithFlags(ev, cudaEventDisableTiming));
+  if (!h->up_stream) CBNS_CUDA(cudaStreamCreateWithFlags(&h->up_stream, cudaStreamNonBlocking));
   // Both staging buffers start free.
   CBNS_CUDA(cudaEventRecord(h->ev_in_free, h->stream));
   CBNS_CUDA(cudaEventRecord(h->ev_out_free, h->stream));
+  CBNS_CUDA(cudaStreamCreateWithFlags(&h->down_stream, cudaStreamNonBlocking));  // last: marks set-up done
   return CBNS_OK;
 }
 
