@@ -52,7 +52,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-mixed", action="store_true", help="skip the FP32-mixed leg")
-    ap.add_argument("--no-large", action="store_true", help="skip the 512^3 / 768^3 FP32-mixed blocks")
+    ap.add_argument("--no-large", action="store_true", help="skip the 512^3 and 768^3 blocks")
     return ap.parse_args()
 
 
@@ -418,29 +418,31 @@ def run_ours(args, rank, world, local):
                            "synchronous_calls": world * cells * args.steps / seq}
     s.close()
 
-    # Blocks above the old 31-bit-index limit (N ~ 745): FP32-mixed at 512^3 and
-    # 768^3 (about 195 GB of device memory), state built on the device.
+    # Larger blocks, state built on the device: binary64 at 512^3 (50 GB), and
+    # FP32-mixed at 512^3 and at 768^3 (165 GB), above the old 31-bit-index limit
+    # (N ~ 745).
     if not args.no_large and rank == 0:
         large = []
-        for NL in (512, 768):
+        for NL, prec in ((512, "fp64"), (512, "fp32_mixed"), (768, "fp32_mixed")):
             pl = tgv_params(NL, t_end=2.0)
             try:
-                sl = Solver(pl, precision="fp32_mixed")
+                sl = Solver(pl, precision=prec)
             except Exception as e:  # not enough device memory on this GPU
-                large.append({"N": NL, "skipped": str(e)[:200]})
+                large.append({"N": NL, "precision": prec, "skipped": str(e)[:200]})
                 continue
             sl.init_tgv()
             lstream = torch.cuda.ExternalStream(sl.stream)
-            sl.run(2)
+            nwarm, ntimed = (1, 2) if prec == "fp64" else (2, 3)
+            sl.run(nwarm)
             torch.cuda.synchronize()
             l0 = torch.cuda.Event(enable_timing=True)
             l1 = torch.cuda.Event(enable_timing=True)
             l0.record(lstream)
-            nl = sl.run(3)
+            nl = sl.run(ntimed)
             l1.record(lstream)
             l1.synchronize()
             lms = l0.elapsed_time(l1) / nl
-            large.append({"N": NL, "precision": "fp32_mixed", "steps": nl, "ms_per_step": lms,
+            large.append({"N": NL, "precision": prec, "steps": nl, "ms_per_step": lms,
                           "value": NL ** 3 / (lms * 1e-3), "device_bytes": sl.info()["device_bytes"]})
             sl.close()
         line["large_blocks"] = large

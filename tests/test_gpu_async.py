@@ -79,3 +79,30 @@ def test_async_reuses_one_pinned_pair_and_reports_finish():
     assert a.wait() is None
     s.close()
     a.close()
+
+
+def test_async_rejects_bad_arguments():
+    """Null handles and buffers come back as CBNS_ERR_INVALID_ARG, before any
+    work is enqueued; the handle stays usable."""
+    import ctypes
+
+    from cbns3d_cart_mpi_gb300 import _lib
+    from cbns3d_cart_mpi_gb300._abi import CBNS_ERR_INVALID_ARG
+    from cbns3d_cart_mpi_gb300.solver import Solver, initial_condition
+    lib = _lib.gpu()
+    p = tgv_params(8, JM=8, KM=9)
+    s = Solver(p)
+    assert lib.cbns_upload_Q_async(None, None, 0.0) == CBNS_ERR_INVALID_ARG
+    assert lib.cbns_upload_Q_async(s._h, None, 0.0) == CBNS_ERR_INVALID_ARG
+    assert lib.cbns_download_Q_async(s._h, None) == CBNS_ERR_INVALID_ARG
+    assert lib.cbns_step_async(None, 1.0) == CBNS_ERR_INVALID_ARG
+    assert lib.cbns_wait(None, None, None) == CBNS_ERR_INVALID_ARG
+    assert lib.cbns_poll(s._h, None) == CBNS_ERR_INVALID_ARG
+    done = ctypes.c_int(-1)
+    assert lib.cbns_poll(s._h, ctypes.byref(done)) == 0 and done.value == 1
+    hin = s.pinned_state()
+    hin[...] = initial_condition(p)
+    s.upload_Q_async(hin, 0.0)
+    s.step_async()
+    assert s.wait() is not None
+    s.close()
