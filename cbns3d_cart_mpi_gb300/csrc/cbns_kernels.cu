@@ -132,6 +132,11 @@ struct MixedCell {
   float rho, u, v, w, p, T, srho, H;
 };
 
+// sqrt(rho) in binary64 for the rare cells below the low-density threshold.
+// Kept out of line so that the common path does not evaluate it: a select
+// between the two square roots would cost every cell a binary64 square root.
+__device__ __noinline__ float low_density_srho(double rho) { return (float)sqrt(rho); }
+
 __device__ __forceinline__ MixedCell mixed_cell(const SolveDev& s, const double (&q)[NEQ]) {
   MixedCell m;
   const Consts<float>& C = s.cf;
@@ -153,7 +158,11 @@ __device__ __forceinline__ MixedCell mixed_cell(const SolveDev& s, const double 
   m.w = ww;
   m.p = pp;
   m.T = C.gM2 * ir * (pp - C.pref_over_rref * rp);
-  m.srho = (r < C.low_rho) ? (float)sqrt(q[0]) : sqrt_(r);
+  if (r < C.low_rho) {
+    m.srho = low_density_srho(q[0]);
+  } else {
+    m.srho = sqrt_(r);
+  }
   m.H = C.gamma_gam1_inv * (C.p_ref + pp) * ir + 0.5f * q2;
   return m;
 }
@@ -1072,6 +1081,9 @@ __device__ __forceinline__ void update_tiles(const SolveDev* __restrict__ solves
     // FP32-mixed stages 2 and 3: the binary32 weight of dt df (1/4 or 2/3 of dt,
     // formed once per step with dt).
     const float cdt = MIXED && stage != 1 ? ctl->cdt[stage - 2] : 0.0f;
+    // FP32-mixed stages 2 and 3: the weights of q0 and qp (one pair per launch,
+    // so each cell evaluates one combination).
+    const double ca = stage == 2 ? 0.75 : 1.0 / 3.0, cb = stage == 2 ? 0.25 : 2.0 / 3.0;
     // FP32-mixed: minus the 4th-order central divergence of the viscous fluxes
     // (src/Block3d.cpp:887-910, calc_viscous_flux_contribution:
     // ((f[-2]-f[+2])/12 + (f[+1]-f[-1])*2/3) / h per direction) of equations
@@ -1131,7 +1143,7 @@ __device__ __forceinline__ void update_tiles(const SolveDev* __restrict__ solves
         // 3/4 q0 + 1/4 qp - 1/4 dt df and 1/3 q0 + 2/3 qp - 2/3 dt df.
         const double qp = at(s, s.Qp, NEQ * V, n * V + o);
         const double inc = (double)(cdt * (float)df);
-        qn[n] = stage == 2 ? fma(0.75, q0, fma(0.25, qp, -inc)) : fma(1.0 / 3.0, q0, fma(2.0 / 3.0, qp, -inc));
+        qn[n] = fma(ca, q0, fma(cb, qp, -inc));
       } else {
         const double dfd = (double)df;
         if (stage == 1) {
