@@ -77,6 +77,22 @@ void append_tiles(std::vector<TileRef>& out, int solve, int ex, int ey, int ez, 
 
 size_t align_up(size_t x) { return (x + 255) & ~size_t(255); }
 
+// Plane tiles of 32 x rows consecutive points of each k-plane of an ex x ey x ez
+// box (the NGV ring of the viscous kernel): the tile number within the plane
+// is split into the 16-bit ti (low) and tj (high) fields.
+void append_plane_tiles(std::vector<TileRef>& out, int solve, int ex, int ey, int ez, int rows = TILE_Y) {
+  const long long per = (long long)TILE_X * rows;
+  const long long n = ((long long)ex * ey + per - 1) / per;
+  for (int k = 0; k < ez; ++k)
+    for (long long q = 0; q < n; ++q)
+      out.push_back(TileRef{(uint16_t)solve, (uint16_t)(q & 0xffff), (uint16_t)(q >> 16), (uint16_t)k});
+}
+
+size_t plane_tile_count(long long ex, long long ey, long long ez, int rows = TILE_Y) {
+  const long long per = (long long)TILE_X * rows;
+  return (size_t)((ex * ey + per - 1) / per) * (size_t)ez;
+}
+
 // Tile coordinates are 16-bit (TileRef): the padded extent along k (one tile
 // per plane) and the tile counts along i and j must stay below 65536.  With
 // 2-row tiles (the smallest the batches use) this caps every extent at
@@ -88,6 +104,19 @@ bool block_extents_ok(uint32_t IM, uint32_t JM, uint32_t KM) {
 
 size_t tile_count(long long ex, long long ey, long long ez, int rows = TILE_Y) {
   return (size_t)((ex + TILE_X - 1) / TILE_X) * (size_t)((ey + rows - 1) / rows) * (size_t)ez;
+}
+
+// The viscous kernel's NGV ring: plane tiles for binary64, row tiles for the
+// binary32 kernel (each walk measured the faster for its precision).
+void append_ring_tiles(std::vector<TileRef>& out, int solve, int ex, int ey, int ez, bool mixed, int rows = TILE_Y) {
+  if (mixed)
+    append_tiles(out, solve, ex, ey, ez, rows);
+  else
+    append_plane_tiles(out, solve, ex, ey, ez, rows);
+}
+
+size_t ring_tile_count(long long ex, long long ey, long long ez, bool mixed) {
+  return mixed ? tile_count(ex, ey, ez) : plane_tile_count(ex, ey, ez);
 }
 
 // Byte offsets of everything a solve's arena holds (see cbns_create).
@@ -269,7 +298,7 @@ cbns_status cbns_create(const cbns_params* p, uint32_t IM, uint32_t JM, uint32_t
   const bool mixed = precision == CBNS_FP32_MIXED;
   s.mixed = mixed ? 1 : 0;
   h->nparts = kDiagParts;
-  const size_t nt_int = tile_count(IM, JM, KM), nt_ring = tile_count(s.rx, s.ry, s.rz),
+  const size_t nt_int = tile_count(IM, JM, KM), nt_ring = ring_tile_count(s.rx, s.ry, s.rz, mixed),
                nt_pad = tile_count(s.nx, s.ny, s.nz);
   const ArenaLayout L = arena_layout(s, mixed, nt_int, nt_ring, nt_pad, h->nparts);
   const size_t off = L.total;
@@ -282,7 +311,7 @@ cbns_status cbns_create(const cbns_params* p, uint32_t IM, uint32_t JM, uint32_t
   }
   std::vector<TileRef> t_int, t_ring, t_pad;
   append_tiles(t_int, 0, IM, JM, KM);
-  append_tiles(t_ring, 0, s.rx, s.ry, s.rz);
+  append_ring_tiles(t_ring, 0, s.rx, s.ry, s.rz, mixed);
   append_tiles(t_pad, 0, s.nx, s.ny, s.nz);
   h->n_int = (int)t_int.size();
   h->n_ring = (int)t_ring.size();
@@ -343,6 +372,7 @@ cbns_status cbns_create(const cbns_params* p, uint32_t IM, uint32_t JM, uint32_t
   s.Re_inv = P.Re_inv;
   s.kappa = -P.Pr_inv * P.gam1_inv / P.Mach2;  // src/Block3d.cpp:766-767
   s.C_T_inf = P.C_T_inf;
+  s.C_T_inf1 = 1.0 + P.C_T_inf;
   s.CFL = P.CFL;
   s.C_dt_v = P.C_dt_v;
   // gen_mesh (src/Block3d.cpp:215-219): spacing from the global grid size.
@@ -828,7 +858,7 @@ cbns_status cbns_batch_create(cbns_handle* const* handles, int n, cbns_batch** o
     descs[i] = s;
     for (int r = 0; r < 3; ++r) {
       append_tiles(ti[r], i, s.IM, s.JM, s.KM, kRowsOptions[r]);
-      append_tiles(tr[r], i, s.rx, s.ry, s.rz, kRowsOptions[r]);
+      append_ring_tiles(tr[r], i, s.rx, s.ry, s.rz, b->mixed, kRowsOptions[r]);
     }
   }
   size_t off = 0;
@@ -992,8 +1022,9 @@ cbns_status cbns_footprint(uint32_t IM, uint32_t JM, uint32_t KM, int precision,
     return fail(CBNS_ERR_BAD_DIMS, "cbns_footprint: every extent must be in [4, " + std::to_string(kMaxExtent) + "]");
   SolveDev s{};
   set_extents(s, IM, JM, KM);
-  ArenaLayout L = arena_layout(s, precision == CBNS_FP32_MIXED, tile_count(IM, JM, KM),
-                               tile_count(s.rx, s.ry, s.rz), tile_count(s.nx, s.ny, s.nz), kDiagParts);
+  const bool mixed = precision == CBNS_FP32_MIXED;
+  ArenaLayout L = arena_layout(s, mixed, tile_count(IM, JM, KM), ring_tile_count(s.rx, s.ry, s.rz, mixed),
+                               tile_count(s.nx, s.ny, s.nz), kDiagParts);
   *bytes = L.total;
   return CBNS_OK;
 }

@@ -136,6 +136,7 @@ struct SolveDev {
   Consts<double> cd;
   Consts<float> cf;
   SolveCtl* ctl;
+  double C_T_inf1;  // 1 + C_T_inf, Sutherland's law (binary64 viscous terms)
 };
 
 template <typename R>
@@ -258,6 +259,13 @@ struct TileRef {
   uint16_t tj;
   uint16_t tk;
 };
+
+// A plane tile: blockDim.x consecutive points of one k-plane of a box of
+// extents ex x ey, numbered p = i + ex j (so every warp is full whatever ex is);
+// the tile number within the plane is ti + 65536 tj, the plane tk.
+__host__ __device__ inline long long plane_tile_first(const TileRef& t, int threads) {
+  return ((long long)t.ti + 65536ll * t.tj) * threads;
+}
 
 __host__ __device__ inline long long pad_off(const SolveDev& s, int i, int j, int k) {
   return (long long)(i + NG) + (long long)s.nx * ((long long)(j + NG) + (long long)s.ny * (k + NG));

@@ -940,7 +940,11 @@ __global__ void __maxnreg__(128) k_inviscid(const SolveDev* __restrict__ solves,
 
 template <typename R>
 __device__ __forceinline__ R d4v(R m2, R p2, R m1, R p1, R c12h, R c23h) {
-  return (m2 - p2) * c12h + (p1 - m1) * c23h;
+  if constexpr (sizeof(R) == 8) {
+    return fma(m2 - p2, c12h, (p1 - m1) * c23h);
+  } else {
+    return (m2 - p2) * c12h + (p1 - m1) * c23h;
+  }
 }
 template <typename R>
 __device__ __forceinline__ R d4(const SolveDev& s, const R* __restrict__ f, long long o, long long st, R c12h,
@@ -956,10 +960,28 @@ __global__ void __maxnreg__(sizeof(R) == 4 ? 40 : 64) k_viscous(const SolveDev* 
                                                                 const TileRef* __restrict__ tiles, int ntiles) {
   constexpr bool MIXED = sizeof(R) == 4;
   for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
-    TileCell tc = tile_cell(tiles[t], -NGV);
+    TileCell tc;
+    if constexpr (MIXED) {
+      // row tiles (32 x rows), the overhang of each row idle
+      tc = tile_cell(tiles[t], -NGV);
+      if (!solves[tc.s].ctl->active) continue;
+      if (tc.i >= solves[tc.s].IM + NGV || tc.j >= solves[tc.s].JM + NGV) continue;
+    } else {
+      // Binary64 (FP64-pipe bound): plane tiles over the NGV ring, consecutive
+      // points of a k-plane, so no lane idles at the end of a row (rx = IM + 4
+      // is rarely a multiple of 32).  Row tiles measured faster for binary32.
+      const TileRef tr = tiles[t];
+      const SolveDev& sp = solves[tr.solve];
+      if (!sp.ctl->active) continue;
+      const long long p = plane_tile_first(tr, (int)blockDim.x) + threadIdx.x;
+      if (p >= (long long)sp.rx * sp.ry) continue;
+      tc.s = tr.solve;
+      tc.j = (int)(p / sp.rx);
+      tc.i = (int)(p - (long long)tc.j * sp.rx) - NGV;
+      tc.j -= NGV;
+      tc.k = (int)tr.tk - NGV;
+    }
     const SolveDev& s = solves[tc.s];
-    if (!s.ctl->active) continue;
-    if (tc.i >= s.IM + NGV || tc.j >= s.JM + NGV) continue;
     const long long o = pad_off(s, tc.i, tc.j, tc.k);
     const long long sy = s.nx, sz = (long long)s.nx * s.ny;
     const Consts<R>& CS = consts_of<R>(s);
@@ -994,7 +1016,8 @@ __global__ void __maxnreg__(sizeof(R) == 4 ? 40 : 64) k_viscous(const SolveDev* 
     // Sutherland's law, (1 + C) / (T + C) * T^1.5 (src/Block3d.cpp:777), as
     // (1 + C) T^2 / sqrt(T (T + C)^2): one reciprocal square root, no division.
     const R TC = Tl + C;
-    const R mu = (((R)1 + C) * (Tl * Tl)) * rsqrt(Tl * (TC * TC));
+    const R C1 = sizeof(R) == 8 ? (R)s.C_T_inf1 : (R)1 + C;  // 1 + C (binary64: formed once on the host)
+    const R mu = (C1 * (Tl * Tl)) * rsqrt(Tl * (TC * TC));
     if (tc.i >= 0 && tc.i < s.IM && tc.j >= 0 && tc.j < s.JM && tc.k >= 0 && tc.k < s.KM) {
       if constexpr (MIXED) {
         at(s, s.muf, s.V, o) = mu;
@@ -1046,9 +1069,15 @@ __global__ void __maxnreg__(sizeof(R) == 4 ? 40 : 64) k_viscous(const SolveDev* 
 // FP32-mixed: the flux differences are binary32, the RK3 accumulation of the
 // conserved state binary64.
 
-template <typename R>
+// STAGE 1..3 makes the stage a compile-time constant, so each launch's code
+// holds one RK3 combination and no cell evaluates another stage's arithmetic
+// (the binary64 update); STAGE 0 takes it at run time from rstage (the FP32-mixed
+// update, whose per-launch weights already keep one combination per cell and
+// which allocates registers better this way).
+template <typename R, int STAGE>
 __device__ __forceinline__ void update_tiles(const SolveDev* __restrict__ solves, const TileRef* __restrict__ tiles,
-                                             int ntiles, int stage) {
+                                             int ntiles, int rstage) {
+  const int stage = STAGE ? STAGE : rstage;
   constexpr bool MIXED = sizeof(R) == 4;
   for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
     TileCell tc = tile_cell(tiles[t], 0);
@@ -1218,14 +1247,14 @@ __device__ __forceinline__ void update_tiles(const SolveDev* __restrict__ solves
 // 11% faster at 80 registers (24 warps per SM, a few spills) than unconstrained
 // (126 registers); the binary32 one (memory-latency bound) 12% faster at 64
 // (32 warps per SM) than at 80.
-template <typename R>
+template <typename R, int STAGE>
 __global__ void __maxnreg__(80) k_update(const SolveDev* __restrict__ solves,
-                                         const TileRef* __restrict__ tiles, int ntiles, int stage) {
-  update_tiles<R>(solves, tiles, ntiles, stage);
+                                         const TileRef* __restrict__ tiles, int ntiles) {
+  update_tiles<R, STAGE>(solves, tiles, ntiles, STAGE);
 }
 __global__ void __maxnreg__(64) k_update_f32(const SolveDev* __restrict__ solves,
                                               const TileRef* __restrict__ tiles, int ntiles, int stage) {
-  update_tiles<float>(solves, tiles, ntiles, stage);
+  update_tiles<float, 0>(solves, tiles, ntiles, stage);
 }
 
 // ---------------------------------------------------------------------------
@@ -1449,7 +1478,9 @@ static void stage_ty(const SolveDev* d, const StageTables& T, int stage, const L
   if constexpr (sizeof(R) == 4) {
     CBNS_LAUNCH(pf, KID_UPDATE, st, (k_update_f32<<<g, nt, 0, st>>>(d, tiles, ntiles, stage)));
   } else {
-    CBNS_LAUNCH(pf, KID_UPDATE, st, (k_update<R><<<g, nt, 0, st>>>(d, tiles, ntiles, stage)));
+    if (stage == 1) CBNS_LAUNCH(pf, KID_UPDATE, st, (k_update<R, 1><<<g, nt, 0, st>>>(d, tiles, ntiles)));
+    else if (stage == 2) CBNS_LAUNCH(pf, KID_UPDATE, st, (k_update<R, 2><<<g, nt, 0, st>>>(d, tiles, ntiles)));
+    else CBNS_LAUNCH(pf, KID_UPDATE, st, (k_update<R, 3><<<g, nt, 0, st>>>(d, tiles, ntiles)));
   }
 }
 

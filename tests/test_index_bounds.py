@@ -134,3 +134,29 @@ def test_paired_face_kernel_covers_each_face_once():
                 for c in lanes[:1 + pair]:
                     stored[c] = stored.get(c, 0) + 1
         assert len(stored) == ex * ey * ez and set(stored.values()) == {1}
+
+
+def test_plane_tiles_cover_each_ring_exactly():
+    """Binary64 k_viscous walks the NGV ring (rx x ry x rz points, rx = IM + 2*NGV) in
+    plane tiles: tile q of plane k covers the flattened points p = q*32*rows + t
+    of that plane, with j = p // rx, i = p % rx; points past rx*ry are dropped.
+    Every ring point is visited exactly once and q fits the split 16-bit fields."""
+    for (IM, JM, KM), rows in itertools.product([(4, 5, 6), (33, 17, 9), (64, 7, 3), (256, 256, 2)], (2, 4, 8)):
+        rx, ry, rz = IM + 2 * NGV, JM + 2 * NGV, KM + 2 * NGV
+        per = 32 * rows
+        nq = -(-(rx * ry) // per)
+        assert nq < 2 ** 32 and rz < 2 ** 16
+        seen = {}
+        for k in range(rz):
+            for q in range(nq):
+                ti, tj = q & 0xFFFF, q >> 16
+                first = (ti + 65536 * tj) * per
+                for t in range(per):
+                    p = first + t
+                    if p >= rx * ry:
+                        continue
+                    j, i = divmod(p, rx)
+                    c = (i - NGV, j - NGV, k - NGV)
+                    assert -NGV <= c[0] < IM + NGV and -NGV <= c[1] < JM + NGV
+                    seen[c] = seen.get(c, 0) + 1
+        assert len(seen) == rx * ry * rz and set(seen.values()) == {1}
