@@ -34,6 +34,7 @@ STATUS_NAMES = {
 
 CBNS_FP64 = 0
 CBNS_FP32_MIXED = 1
+CBNS_FP64_FF = 2
 
 
 class CbnsParams(ctypes.Structure):

@@ -158,6 +158,8 @@ def probe():
         _probe.cbns_probe_peak.argtypes = [c_int, c_dp]
         _probe.cbns_probe_rcp64.restype = c_int
         _probe.cbns_probe_rcp64.argtypes = [c_vp, c_vp, c_vp, ctypes.c_longlong]
+        _probe.cbns_probe_ff.restype = c_int
+        _probe.cbns_probe_ff.argtypes = [c_vp, c_vp, c_vp, ctypes.c_longlong]
     return _probe
 
 

@@ -30,7 +30,7 @@ cudaError_t launch_dt_raw(const SolveDev* d, int sidx, const TileRef* tiles, int
                           bool mixed, const LaunchCfg& cfg, cudaStream_t st, Profiler* pf);
 cudaError_t launch_set_dt(const SolveDev* d, int sidx, double dt, cudaStream_t st);
 cudaError_t launch_reset_ctl(SolveCtl* ctl, double t, double t_end, cudaStream_t st);
-cudaError_t launch_stage(const SolveDev* d, const StageTables& T, int stage, const LaunchCfg& cfg, bool mixed,
+cudaError_t launch_stage(const SolveDev* d, const StageTables& T, int stage, const LaunchCfg& cfg, int precision,
                          cudaStream_t st, Profiler* pf);
 cudaError_t launch_diag(const SolveDev* d, int sidx, const TileRef* tiles, int ntiles, double* partials,
                         int nparts, double inv_n, double* out, cudaStream_t st, Profiler* pf);
@@ -121,11 +121,12 @@ size_t ring_tile_count(long long ex, long long ey, long long ez, bool mixed) {
 
 // Byte offsets of everything a solve's arena holds (see cbns_create).
 struct ArenaLayout {
-  size_t oQ, oQp, oStage, oPrim, oF[3], oTv, oFf[3], oTv32, oU32, oP32, oCtl, oDesc, oTi, oTr, oTp, oPart, oOut,
-      total;
+  size_t oQ, oQp, oStage, oPrim, oF[3], oTv, oFf[3], oTv32, oU32, oP32, oQF, oQpF, oPF, oCtl, oDesc, oTi, oTr, oTp,
+      oPart, oOut, total;
 };
 
-ArenaLayout arena_layout(const SolveDev& s, bool mixed, size_t n_int, size_t n_ring, size_t n_pad, int nparts) {
+ArenaLayout arena_layout(const SolveDev& s, int precision, size_t n_int, size_t n_ring, size_t n_pad, int nparts) {
+  const bool mixed = precision == CBNS_FP32_MIXED;
   ArenaLayout L{};
   size_t off = 0;
   auto take = [&](size_t bytes) {
@@ -141,6 +142,12 @@ ArenaLayout arena_layout(const SolveDev& s, bool mixed, size_t n_int, size_t n_r
   if (!mixed) {
     for (int d = 0; d < 3; ++d) L.oF[d] = take(sizeof(double) * NEQ * (size_t)s.IV);
     L.oTv = take(sizeof(double) * kViscTerms * (size_t)s.RV);
+    if (precision == CBNS_FP64_FF) {
+      const size_t f2V = sizeof(float2) * (size_t)s.V;
+      L.oQF = take(NEQ * f2V);
+      L.oQpF = take(NEQ * f2V);
+      L.oPF = take(5 * f2V);
+    }
   } else {
     L.oU32 = take(NEQ * fV);  // U4 (4 values per cell), then UE
     L.oP32 = take(9 * fV);    // PA and PB (4 values per cell each), then mu
@@ -233,7 +240,7 @@ cbns_status cbns_create(const cbns_params* p, uint32_t IM, uint32_t JM, uint32_t
                         cbns_handle** out) {
   if (!p || !out) return fail(CBNS_ERR_INVALID_ARG, "cbns_create: null argument");
   *out = nullptr;
-  if (precision != CBNS_FP64 && precision != CBNS_FP32_MIXED)
+  if (precision != CBNS_FP64 && precision != CBNS_FP32_MIXED && precision != CBNS_FP64_FF)
     return fail(CBNS_ERR_INVALID_ARG, "cbns_create: unknown precision");
   // The reference's halo exchange sends NG interior layers; a block narrower than
   // NG would send ghost cells.  Above that, the extents are limited by the 16-bit
@@ -300,7 +307,7 @@ cbns_status cbns_create(const cbns_params* p, uint32_t IM, uint32_t JM, uint32_t
   h->nparts = kDiagParts;
   const size_t nt_int = tile_count(IM, JM, KM), nt_ring = ring_tile_count(s.rx, s.ry, s.rz, mixed),
                nt_pad = tile_count(s.nx, s.ny, s.nz);
-  const ArenaLayout L = arena_layout(s, mixed, nt_int, nt_ring, nt_pad, h->nparts);
+  const ArenaLayout L = arena_layout(s, precision, nt_int, nt_ring, nt_pad, h->nparts);
   const size_t off = L.total;
   {
     size_t free_b = 0, total_b = 0;
@@ -345,6 +352,10 @@ cbns_status cbns_create(const cbns_params* p, uint32_t IM, uint32_t JM, uint32_t
     s.UE = nullptr;
     s.PA = s.PB = nullptr;
     s.muf = nullptr;
+    s.ffaces = precision == CBNS_FP64_FF ? 1 : 0;
+    s.QF = s.ffaces ? (float2*)(A + L.oQF) : nullptr;
+    s.QpF = s.ffaces ? (float2*)(A + L.oQpF) : nullptr;
+    s.PF = s.ffaces ? (float2*)(A + L.oPF) : nullptr;
   } else {
     s.U4 = (float4*)(A + oU32);
     s.UE = (float*)(s.U4 + s.V);
@@ -384,6 +395,17 @@ cbns_status cbns_create(const cbns_params* p, uint32_t IM, uint32_t JM, uint32_t
   s.inv_dy = 1.0 / s.dy;
   s.inv_dz = 1.0 / s.dz;
   fill_consts(s);
+  {
+    // float-float constants of CBNS_FP64_FF faces: hi = x rounded to binary32,
+    // lo = the rest rounded
+    auto split = [](double x) {
+      const float hi = (float)x;
+      return make_float2(hi, (float)(x - (double)hi));
+    };
+    s.ff_gam1 = split(s.gam1);
+    s.ff_gamma = split(s.gamma);
+    s.ff_hgam1 = split(0.5 * s.gam1);
+  }
   h->d_ctl = (SolveCtl*)(A + oCtl);
   s.ctl = h->d_ctl;
   h->d_desc = (SolveDev*)(A + oDesc);
@@ -501,7 +523,7 @@ cbns_status cbns_calc_dt(cbns_handle* h, double* dt) {
 
 static cbns_status enqueue_stage(cbns_handle* h, int stage) {
   const StageTables T{h->d_tiles_int, h->n_int, h->d_tiles_ring, h->n_ring};
-  CBNS_CUDA(launch_stage(h->d_desc, T, stage, LaunchCfg{}, h->desc.mixed != 0, h->stream, h->pf()));
+  CBNS_CUDA(launch_stage(h->d_desc, T, stage, LaunchCfg{}, h->precision, h->stream, h->pf()));
   return CBNS_OK;
 }
 
@@ -782,7 +804,7 @@ static cbns_status batch_enqueue_step(cbns_batch* b) {
   CBNS_CUDA(launch_dt(b->d_descs, n, b->d_int[ri], b->n_int[ri], 0.0, false, b->mixed, b->cfg, b->stream, nullptr));
   const StageTables T{b->d_int[ri], b->n_int[ri], b->d_ring[ri], b->n_ring[ri]};
   for (int st = 1; st <= 3; ++st)
-    CBNS_CUDA(launch_stage(b->d_descs, T, st, b->cfg, b->mixed, b->stream, nullptr));
+    CBNS_CUDA(launch_stage(b->d_descs, T, st, b->cfg, b->precision, b->stream, nullptr));
   return CBNS_OK;
 }
 
@@ -844,6 +866,7 @@ cbns_status cbns_batch_create(cbns_handle* const* handles, int n, cbns_batch** o
   };
   b->device = handles[0]->device;
   b->mixed = handles[0]->precision == CBNS_FP32_MIXED;
+  b->precision = handles[0]->precision;
   b->handles.assign(handles, handles + n);
   cudaError_t e = cudaSetDevice(b->device);
   if (e != cudaSuccess) return bail(cuda_fail(e, "cudaSetDevice"));
@@ -1023,7 +1046,7 @@ cbns_status cbns_footprint(uint32_t IM, uint32_t JM, uint32_t KM, int precision,
   SolveDev s{};
   set_extents(s, IM, JM, KM);
   const bool mixed = precision == CBNS_FP32_MIXED;
-  ArenaLayout L = arena_layout(s, mixed, tile_count(IM, JM, KM), ring_tile_count(s.rx, s.ry, s.rz, mixed),
+  ArenaLayout L = arena_layout(s, precision, tile_count(IM, JM, KM), ring_tile_count(s.rx, s.ry, s.rz, mixed),
                                tile_count(s.nx, s.ny, s.nz), kDiagParts);
   *bytes = L.total;
   return CBNS_OK;

@@ -137,6 +137,16 @@ struct SolveDev {
   Consts<float> cf;
   SolveCtl* ctl;
   double C_T_inf1;  // 1 + C_T_inf, Sutherland's law (binary64 viscous terms)
+  // Binary64 solves with float-float faces (CBNS_FP64_FF): the face kernel's
+  // inputs as float-float pairs {hi, lo}, written with the binary64 state by the
+  // update and start-up kernels: the state Q and Q_p (5 blocks of V each) and
+  // the face primitives sqrt(rho), H, u, v, w (5 blocks of V); the constants
+  // gamma - 1, gamma and (gamma - 1)/2.  Null / unused otherwise.
+  int ffaces;
+  float2* QF;
+  float2* QpF;
+  float2* PF;
+  float2 ff_gam1, ff_gamma, ff_hgam1;
 };
 
 template <typename R>
@@ -265,6 +275,30 @@ struct TileRef {
 // the tile number within the plane is ti + 65536 tj, the plane tk.
 __host__ __device__ inline long long plane_tile_first(const TileRef& t, int threads) {
   return ((long long)t.ti + 65536ll * t.tj) * threads;
+}
+
+// ---------------------------------------------------------------------------
+// Tile walk.  Every kernel loops over its tile table with a grid stride, so it
+// runs either one tile per CTA or persistently with fewer CTAs than tiles.
+
+struct TileCell {
+  int s;  // solve index
+  int i, j, k;
+};
+
+// A tile is TILE_X cells along i by blockDim.x/32 rows along j (one CTA).  The
+// row count is a launch-time choice (the batch autotuner picks 2, 4 or 8), not a
+// template parameter, so every launch shape runs the same compiled kernel and
+// therefore the same arithmetic: results do not depend on the launch shape.
+constexpr int kMaxThreads = 256;
+
+__device__ __forceinline__ TileCell tile_cell(const TileRef& t, int origin) {
+  TileCell c;
+  c.s = t.solve;
+  c.i = origin + t.ti * TILE_X + (int)(threadIdx.x % TILE_X);
+  c.j = origin + t.tj * (int)(blockDim.x / TILE_X) + (int)(threadIdx.x / TILE_X);
+  c.k = origin + t.tk;
+  return c;
 }
 
 __host__ __device__ inline long long pad_off(const SolveDev& s, int i, int j, int k) {

@@ -1,0 +1,224 @@
+// cbns_ff_faces.cu — the inviscid face fluxes of CBNS_FP64_FF solves: the
+// binary64 face kernel's scheme (Roe-averaged characteristic WENO5 with local
+// Lax-Friedrichs splitting; src/Block3d.cpp:555-748, src/eigenvectors_roe.cpp,
+// src/weno.cpp, src/lf_flux.cpp) evaluated in float-float arithmetic
+// (cbns_ff.cuh) on the binary32 pipes, one face per thread.
+//
+// The inputs are float-float copies of the binary64 state and of the face
+// primitives (sqrt(rho), H, u, v, w), split once per cell by the binary64 update
+// and start-up kernels, so this kernel issues no binary64 arithmetic except one
+// addition per stored flux component, which rounds the float-float flux to the
+// binary64 array the binary64 update reads.  Each step below is the binary64
+// kernel's (cbns_kernels.cu, face_core), operation for operation where the
+// float-float forms allow; the notes there give the algebra.
+#include <cuda_runtime.h>
+
+#include "cbns_device.cuh"
+#include "cbns_ff.cuh"
+#include "cbns_prof.h"
+
+namespace cbns {
+
+namespace {
+
+__device__ __forceinline__ ff ld(const SolveDev& s, const float2* p, long long n, long long i) {
+  const float2 v = at(s, p, n, i);
+  return ff{v.x, v.y};
+}
+
+__device__ __forceinline__ ff cst(float2 v) { return ff{v.x, v.y}; }
+
+// sqrt(rho), H and the velocity of one cell beside a face.
+struct SideFF {
+  ff sr, h, u, v, w;
+};
+
+__device__ __forceinline__ SideFF side_ff(const SolveDev& s, long long o) {
+  const long long V = s.V, n5 = 5 * V;
+  const float2* P = s.PF;
+  return SideFF{ld(s, P, n5, o), ld(s, P, n5, V + o), ld(s, P, n5, 2 * V + o), ld(s, P, n5, 3 * V + o),
+                ld(s, P, n5, 4 * V + o)};
+}
+
+struct WenoFF {
+  ff num, den;
+};
+
+// One biased WENO5 stencil as the binary64 weno5_side: the indicators taken four
+// times over, 4 (eps + IS_k) = 13/3 D_k^2 + e_k^2 + 4 eps, a_k their squares,
+// num = a2 a3 g1 + 6 a1 a3 g2 + 3 a1 a2 g3 and den = a2 a3 + 6 a1 a3 + 3 a1 a2.
+__device__ __forceinline__ void weno5_side_ff(ff D1, ff C1, ff D2, ff C2, ff D3, ff C3, ff e1, ff e2, ff e3,
+                                              ff g1, ff g2s, ff g3s, WenoFF& out) {
+  constexpr ff eps4 = ff_const(4.0e-6);
+  const ff is1 = ff_fma(C1, D1, ff_sqr_add(e1, eps4));
+  const ff is2 = ff_fma(C2, D2, ff_sqr_add(e2, eps4));
+  const ff is3 = ff_fma(C3, D3, ff_sqr_add(e3, eps4));
+  const ff a1 = ff_sqr(is1), a2 = ff_sqr(is2), a3 = ff_sqr(is3);
+  const ff p1 = a2 * a3, q2 = a1 * a3, q3 = a1 * a2;
+  out.den = ff_fma(6.0f, q2, ff_fma(3.0f, q3, p1));
+  out.num = ff_fma(q2, g2s, ff_fma(q3, g3s, p1 * g1));
+}
+
+// Both reconstructions of one characteristic field (the binary64 weno5_pair):
+// with d_m = v_{m+1} - v_m and the arguments g1, 6 g2, 3 g3,
+//   left:  D = d1-d0, d2-d1, d3-d2;  e = 3 d1 - d0, d1 + d2, d3 - 3 d2;
+//          g1 = 5/6 d1 - 1/3 d0,  6 g2 = d1 + 2 d2,  3 g3 = 2 d2 - d3/2;
+//   right: D = d4-d3, d3-d2, d2-d1;  e = d4 - 3 d3, d2 + d3, 3 d2 - d1;
+//          g1 = 1/3 d4 - 5/6 d3,  6 g2 = -(d3 + 2 d2),  3 g3 = d1/2 - 2 d2.
+__device__ __forceinline__ void weno5_pair_ff(const ff (&v)[6], WenoFF& L, WenoFF& Rt) {
+  const ff d0 = v[1] - v[0], d1 = v[2] - v[1], d2 = v[3] - v[2], d3 = v[4] - v[3], d4 = v[5] - v[4];
+  const ff D1 = d1 - d0, D2 = d2 - d1, D3 = d3 - d2, D4 = d4 - d3;
+  constexpr ff c13 = ff_const(13.0 / 3.0);
+  const ff C1 = c13 * D1, C2 = c13 * D2, C3 = c13 * D3, C4 = c13 * D4;
+  constexpr ff k56 = ff_const(5.0 / 6.0), k13 = ff_const(1.0 / 3.0);
+  const ff t2 = ff_scale(d2, 2.0f);
+  weno5_side_ff(D1, C1, D2, C2, D3, C3, ff_fma(3.0f, d1, -d0), d1 + d2, ff_fma(-3.0f, d2, d3),
+                ff_fma(k56, d1, -(k13 * d0)), t2 + d1, t2 - ff_scale(d3, 0.5f), L);
+  weno5_side_ff(D4, C4, D3, C3, D2, C2, ff_fma(-3.0f, d3, d4), d2 + d3, ff_fma(3.0f, d2, -d1),
+                ff_fma(-k56, d3, k13 * d4), -(t2 + d3), ff_scale(d1, 0.5f) - t2, Rt);
+}
+
+// The face flux (binary64 face_core's steps; the stored flux is twice the
+// reference's, the halves folded into the update's 0.5/h).
+template <int D>
+__device__ __forceinline__ void face_core_ff(const SolveDev& s, const ff (&W)[6][NEQ], const SideFF& Ls,
+                                             const SideFF& Rs, ff (&out)[NEQ]) {
+  constexpr int T1 = (D + 1) % 3;
+  constexpr int T2 = (D + 2) % 3;
+  const ff gam1 = cst(s.ff_gam1), gamma = cst(s.ff_gamma), hgam1 = cst(s.ff_hgam1);
+
+  // Roe average: f_R + wL (f_L - f_R), wL = sqrt(rho_L) / (sqrt(rho_L) + sqrt(rho_R)).
+  ff Uv[3], HH;
+  {
+    const ff wL = Ls.sr * ff_rcp(Ls.sr + Rs.sr);
+    Uv[0] = ff_fma(wL, Ls.u - Rs.u, Rs.u);
+    Uv[1] = ff_fma(wL, Ls.v - Rs.v, Rs.v);
+    Uv[2] = ff_fma(wL, Ls.w - Rs.w, Rs.w);
+    HH = ff_fma(wL, Ls.h - Rs.h, Rs.h);
+  }
+  const ff q2 = ff_sqr_add(Uv[2], ff_sqr_add(Uv[1], ff_sqr(Uv[0])));
+  const ff hq2 = ff_scale(q2, 0.5f);
+  const ff c2 = gam1 * (HH - hq2);
+  const ff ic = ff_rsqrt(c2);  // 1/c
+  const ff cc = c2 * ic;
+  const ff K = (hgam1 * ic) * ic;
+  const ff hic = ff_scale(ic, 0.5f);
+  const ff un = Uv[D], u1 = Uv[T1], u2 = Uv[T2];
+
+  // Characteristic projections of the six stencil cells.
+  ff w[NEQ][6];
+#pragma unroll
+  for (int m = 0; m < 6; ++m) {
+    const ff f0 = W[m][0], f4 = W[m][4];
+    const ff fm[3] = {W[m][1], W[m][2], W[m][3]};
+    const ff t = ff_fma(-Uv[2], fm[2], ff_fma(-Uv[1], fm[1], ff_fma(-Uv[0], fm[0], ff_fma(hq2, f0, f4))));
+    const ff A = K * t;
+    const ff g = ff_fma(un, f0, -fm[D]);
+    w[0][m] = ff_fma(hic, g, A);
+    w[1][m] = f0 - ff_scale(A, 2.0f);
+    w[2][m] = ff_fma(-hic, g, A);
+    w[3][m] = ff_fma(-u1, f0, fm[T1]);
+    w[4][m] = ff_fma(-u2, f0, fm[T2]);
+  }
+
+  // Left- and right-biased reconstructions, r = base + num / den.
+  ff rl[NEQ], rr[NEQ];
+#pragma unroll
+  for (int n = 0; n < NEQ; ++n) {
+    WenoFF a, b;
+    weno5_pair_ff(w[n], a, b);
+    rl[n] = ff_fma(a.num, ff_rcp(a.den), w[n][2]);
+    rr[n] = ff_fma(b.num, ff_rcp(b.den), w[n][3]);
+  }
+
+  // Back to conserved variables.
+  const ff uncc = un * cc;
+  ff rhoL, mL[3], EL, rhoR, mR[3], ER;
+  {
+    const ff sp = rl[0] + rl[2], dm = rl[2] - rl[0];
+    rhoL = sp + rl[1];
+    mL[D] = ff_fma(un, rhoL, cc * dm);
+    mL[T1] = ff_fma(u1, rhoL, rl[3]);
+    mL[T2] = ff_fma(u2, rhoL, rl[4]);
+    EL = ff_fma(HH, sp, ff_fma(uncc, dm, ff_fma(hq2, rl[1], ff_fma(u1, rl[3], u2 * rl[4]))));
+  }
+  {
+    const ff sp = rr[0] + rr[2], dm = rr[2] - rr[0];
+    rhoR = sp + rr[1];
+    mR[D] = ff_fma(un, rhoR, cc * dm);
+    mR[T1] = ff_fma(u1, rhoR, rr[3]);
+    mR[T2] = ff_fma(u2, rhoR, rr[4]);
+    ER = ff_fma(HH, sp, ff_fma(uncc, dm, ff_fma(hq2, rr[1], ff_fma(u1, rr[3], u2 * rr[4]))));
+  }
+
+  // Local Lax-Friedrichs flux; both 1/rho from one reciprocal.
+  const ff ip = ff_rcp(rhoL * rhoR);
+  const ff iL = ip * rhoR, iR = ip * rhoL;
+  ff vL[3], vR[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    vL[a] = mL[a] * iL;
+    vR[a] = mR[a] * iR;
+  }
+  const ff kL = ff_fma(mL[2], vL[2], ff_fma(mL[1], vL[1], mL[0] * vL[0]));
+  const ff kR = ff_fma(mR[2], vR[2], ff_fma(mR[1], vR[1], mR[0] * vR[0]));
+  const ff pL = gam1 * (EL - ff_scale(kL, 0.5f));
+  const ff pR = gam1 * (ER - ff_scale(kR, 0.5f));
+  const ff c2L = (gamma * iL) * pL, c2R = (gamma * iR) * pR;
+  const ff cL = c2L * ff_rsqrt(c2L), cR = c2R * ff_rsqrt(c2R);
+  const ff alpha = ff_max(ff_abs(vR[D]) + cR, ff_abs(vL[D]) + cL);
+  const ff fL = mL[D], fR = mR[D];
+  out[0] = ff_fma(-alpha, rhoR - rhoL, fL + fR);
+  const ff pLR = pL + pR;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const ff fLa = (a == D) ? ff_fma(fL, vL[a], pLR) : fL * vL[a];
+    out[1 + a] = ff_fma(-alpha, mR[a] - mL[a], ff_fma(fR, vR[a], fLa));
+  }
+  out[4] = ff_fma(-alpha, ER - EL, ff_fma(vR[D], ER + pR, vL[D] * (EL + pL)));
+}
+
+// One face per thread over the interior tiles (the binary64 k_inviscid's walk).
+// The stage input is Q's float-float copy in stage 1 and Q_p's in stages 2-3.
+template <int D>
+__global__ void __maxnreg__(128) k_inviscid_ff(const SolveDev* __restrict__ solves,
+                                               const TileRef* __restrict__ tiles, int ntiles, int stage) {
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const TileCell tc = tile_cell(tiles[t], 0);
+    const SolveDev& s = solves[tc.s];
+    if (!s.ctl->active) continue;
+    if (tc.i >= s.IM || tc.j >= s.JM) continue;
+    const float2* U = stage == 1 ? s.QF : s.QpF;
+    const long long st = D == 0 ? 1ll : (D == 1 ? (long long)s.nx : (long long)s.nx * s.ny);
+    const long long V = s.V, c = pad_off(s, tc.i, tc.j, tc.k);
+    ff W[6][NEQ];
+#pragma unroll
+    for (int m = 0; m < 6; ++m) {
+#pragma unroll
+      for (int n = 0; n < NEQ; ++n) W[m][n] = ld(s, U, NEQ * V, n * V + c + (m - 3) * st);
+    }
+    ff f[NEQ];
+    face_core_ff<D>(s, W, side_ff(s, c - st), side_ff(s, c), f);
+    const long long fo = int_off(s, tc.i, tc.j, tc.k);
+    double* F = s.F[D];
+#pragma unroll
+    for (int n = 0; n < NEQ; ++n) at(s, F, NEQ * s.IV, n * s.IV + fo) = ff_to_double(f[n]);
+  }
+}
+
+}  // namespace
+
+// The three face launches of a stage (grid g, nt threads: the binary64 tiles).
+void launch_faces_ff(const SolveDev* d, const TileRef* tiles, int ntiles, int stage, int g, int nt,
+                     cudaStream_t st, Profiler* pf) {
+  auto run = [&](int id, auto kern) {
+    if (pf) pf->before(id, st);
+    kern<<<g, nt, 0, st>>>(d, tiles, ntiles, stage);
+    if (pf) pf->after(st);
+  };
+  run(KID_INVISCID_X, k_inviscid_ff<0>);
+  run(KID_INVISCID_Y, k_inviscid_ff<1>);
+  run(KID_INVISCID_Z, k_inviscid_ff<2>);
+}
+
+}  // namespace cbns

@@ -65,6 +65,7 @@ struct cbns_batch {
   cudaStream_t stream = nullptr;
   std::vector<cbns_handle*> handles;
   bool mixed = false;
+  int precision = CBNS_FP64;
   char* arena = nullptr;
   cbns::SolveDev* d_descs = nullptr;
   cbns::TileRef* d_int[3] = {nullptr, nullptr, nullptr};

@@ -36,35 +36,13 @@
 #include <cmath>
 #include <cstdint>
 
+#include "../../include/cbns_gpu.h"
 #include "cbns_device.cuh"
+#include "cbns_ff.cuh"
 #include "cbns_modes.h"
 #include "cbns_prof.h"
 
 namespace cbns {
-
-// ---------------------------------------------------------------------------
-// Tile walk.  Every kernel loops over its tile table with a grid stride, so it
-// runs either one tile per CTA or persistently with fewer CTAs than tiles.
-
-struct TileCell {
-  int s;  // solve index
-  int i, j, k;
-};
-
-// A tile is TILE_X cells along i by blockDim.x/32 rows along j (one CTA).  The
-// row count is a launch-time choice (the batch autotuner picks 2, 4 or 8), not a
-// template parameter, so every launch shape runs the same compiled kernel and
-// therefore the same arithmetic: results do not depend on the launch shape.
-constexpr int kMaxThreads = 256;
-
-__device__ __forceinline__ TileCell tile_cell(const TileRef& t, int origin) {
-  TileCell c;
-  c.s = t.solve;
-  c.i = origin + t.ti * TILE_X + (int)(threadIdx.x % TILE_X);
-  c.j = origin + t.tj * (int)(blockDim.x / TILE_X) + (int)(threadIdx.x / TILE_X);
-  c.k = origin + t.tk;
-  return c;
-}
 
 // ---------------------------------------------------------------------------
 // Division, reciprocal and square root by compute type.  Binary64 keeps IEEE
@@ -120,6 +98,22 @@ __device__ __forceinline__ void store_prims(const SolveDev& s, long long o, doub
   at(s, s.pd.T, V, o) = q.T;
   at(s, s.pd.srho, V, o) = q.sr;
   at(s, s.pd.H, V, o) = q.H;
+}
+
+// CBNS_FP64_FF solves: the float-float copies the face kernel reads, of a cell's
+// state (into QFo, the copy of the array the state went to) and of its face
+// primitives sqrt(rho), H, u, v, w (split on the integer pipe).
+__device__ __forceinline__ void store_ff(const SolveDev& s, float2* QFo, long long d, const double (&q)[NEQ],
+                                         double sr, double H, double u, double v, double w) {
+  const long long V = s.V, n5 = NEQ * V;
+#pragma unroll
+  for (int n = 0; n < NEQ; ++n) at(s, QFo, n5, n * V + d) = ff_split(q[n]);
+  float2* P = s.PF;
+  at(s, P, n5, d) = ff_split(sr);
+  at(s, P, n5, V + d) = ff_split(H);
+  at(s, P, n5, 2 * V + d) = ff_split(u);
+  at(s, P, n5, 3 * V + d) = ff_split(v);
+  at(s, P, n5, 4 * V + d) = ff_split(w);
 }
 
 // FP32-mixed: the binary32 perturbation state and primitives of a binary64 state.
@@ -217,6 +211,11 @@ __global__ void k_prepare(const SolveDev* __restrict__ solves, const TileRef* __
     }
     store_prims(s, o, q[0], q[1], q[2], q[3], q[4]);
     if (s.mixed) store_mixed(s, o, mixed_cell(s, q));
+    if (s.ffaces) {
+      const Prims64 pr = prims64(s, q[0], q[1], q[2], q[3], q[4]);
+      store_ff(s, s.QF, o, q, pr.sr, pr.H, pr.u, pr.v, pr.w);
+      store_ff(s, s.QpF, o, q, pr.sr, pr.H, pr.u, pr.v, pr.w);
+    }
     const bool interior = tc.i >= 0 && tc.i < s.IM && tc.j >= 0 && tc.j < s.JM && tc.k >= 0 && tc.k < s.KM;
     if (interior) {
       at(s, s.pd.mu, s.V, o) = 1.0;
@@ -1074,7 +1073,7 @@ __global__ void __maxnreg__(sizeof(R) == 4 ? 40 : 64) k_viscous(const SolveDev* 
 // (the binary64 update); STAGE 0 takes it at run time from rstage (the FP32-mixed
 // update, whose per-launch weights already keep one combination per cell and
 // which allocates registers better this way).
-template <typename R, int STAGE>
+template <typename R, int STAGE, bool FF = false>
 __device__ __forceinline__ void update_tiles(const SolveDev* __restrict__ solves, const TileRef* __restrict__ tiles,
                                              int ntiles, int rstage) {
   const int stage = STAGE ? STAGE : rstage;
@@ -1218,6 +1217,7 @@ __device__ __forceinline__ void update_tiles(const SolveDev* __restrict__ solves
         at(s, b, n8, 5 * V + d) = TT;
         at(s, b, n8, 6 * V + d) = sr;
         at(s, b, n8, 7 * V + d) = HH;
+        if constexpr (FF) store_ff(s, stage == 3 ? s.QF : s.QpF, d, qn, sr, HH, uu, vv, ww);
       }
     };
     store(o);
@@ -1247,10 +1247,11 @@ __device__ __forceinline__ void update_tiles(const SolveDev* __restrict__ solves
 // 11% faster at 80 registers (24 warps per SM, a few spills) than unconstrained
 // (126 registers); the binary32 one (memory-latency bound) 12% faster at 64
 // (32 warps per SM) than at 80.
-template <typename R, int STAGE>
+// FF: also the float-float copies of CBNS_FP64_FF solves.
+template <typename R, int STAGE, bool FF>
 __global__ void __maxnreg__(80) k_update(const SolveDev* __restrict__ solves,
                                          const TileRef* __restrict__ tiles, int ntiles) {
-  update_tiles<R, STAGE>(solves, tiles, ntiles, STAGE);
+  update_tiles<R, STAGE, FF>(solves, tiles, ntiles, STAGE);
 }
 __global__ void __maxnreg__(64) k_update_f32(const SolveDev* __restrict__ solves,
                                               const TileRef* __restrict__ tiles, int ntiles, int stage) {
@@ -1373,6 +1374,10 @@ static int grid_for(int ntiles, int max_ctas) {
   return max_ctas > 0 && ntiles > max_ctas ? max_ctas : ntiles;
 }
 
+// cbns_ff_faces.cu
+void launch_faces_ff(const SolveDev* d, const TileRef* tiles, int ntiles, int stage, int g, int nt,
+                     cudaStream_t st, Profiler* pf);
+
 #define CBNS_LAUNCH(pf, id, st, ...) \
   do {                               \
     if (pf) (pf)->before(id, st);    \
@@ -1457,8 +1462,8 @@ cudaError_t launch_set_dt(const SolveDev* d, int sidx, double dt, cudaStream_t s
 }
 
 template <typename R>
-static void stage_ty(const SolveDev* d, const StageTables& T, int stage, const LaunchCfg& cfg, cudaStream_t st,
-                     Profiler* pf) {
+static void stage_ty(const SolveDev* d, const StageTables& T, int stage, const LaunchCfg& cfg, bool ff,
+                     cudaStream_t st, Profiler* pf) {
   const TileRef* tiles = T.tiles;
   const int ntiles = T.ntiles;
   const int g = grid_for(ntiles, cfg.max_ctas);
@@ -1468,6 +1473,8 @@ static void stage_ty(const SolveDev* d, const StageTables& T, int stage, const L
     CBNS_LAUNCH(pf, KID_INVISCID_X, st, (k_inviscid_x2<0><<<g, nt2, 0, st>>>(d, tiles, ntiles)));
     CBNS_LAUNCH(pf, KID_INVISCID_Y, st, (k_inviscid_x2<1><<<g, nt2, 0, st>>>(d, tiles, ntiles)));
     CBNS_LAUNCH(pf, KID_INVISCID_Z, st, (k_inviscid_x2<2><<<g, nt2, 0, st>>>(d, tiles, ntiles)));
+  } else if (ff) {
+    launch_faces_ff(d, tiles, ntiles, stage, g, nt, st, pf);
   } else {
     CBNS_LAUNCH(pf, KID_INVISCID_X, st, (k_inviscid<0, R><<<g, nt, 0, st>>>(d, tiles, ntiles, stage)));
     CBNS_LAUNCH(pf, KID_INVISCID_Y, st, (k_inviscid<1, R><<<g, nt, 0, st>>>(d, tiles, ntiles, stage)));
@@ -1478,17 +1485,23 @@ static void stage_ty(const SolveDev* d, const StageTables& T, int stage, const L
   if constexpr (sizeof(R) == 4) {
     CBNS_LAUNCH(pf, KID_UPDATE, st, (k_update_f32<<<g, nt, 0, st>>>(d, tiles, ntiles, stage)));
   } else {
-    if (stage == 1) CBNS_LAUNCH(pf, KID_UPDATE, st, (k_update<R, 1><<<g, nt, 0, st>>>(d, tiles, ntiles)));
-    else if (stage == 2) CBNS_LAUNCH(pf, KID_UPDATE, st, (k_update<R, 2><<<g, nt, 0, st>>>(d, tiles, ntiles)));
-    else CBNS_LAUNCH(pf, KID_UPDATE, st, (k_update<R, 3><<<g, nt, 0, st>>>(d, tiles, ntiles)));
+    if (ff) {
+      if (stage == 1) CBNS_LAUNCH(pf, KID_UPDATE, st, (k_update<R, 1, true><<<g, nt, 0, st>>>(d, tiles, ntiles)));
+      else if (stage == 2) CBNS_LAUNCH(pf, KID_UPDATE, st, (k_update<R, 2, true><<<g, nt, 0, st>>>(d, tiles, ntiles)));
+      else CBNS_LAUNCH(pf, KID_UPDATE, st, (k_update<R, 3, true><<<g, nt, 0, st>>>(d, tiles, ntiles)));
+    } else {
+      if (stage == 1) CBNS_LAUNCH(pf, KID_UPDATE, st, (k_update<R, 1, false><<<g, nt, 0, st>>>(d, tiles, ntiles)));
+      else if (stage == 2) CBNS_LAUNCH(pf, KID_UPDATE, st, (k_update<R, 2, false><<<g, nt, 0, st>>>(d, tiles, ntiles)));
+      else CBNS_LAUNCH(pf, KID_UPDATE, st, (k_update<R, 3, false><<<g, nt, 0, st>>>(d, tiles, ntiles)));
+    }
   }
 }
 
-cudaError_t launch_stage(const SolveDev* d, const StageTables& T, int stage, const LaunchCfg& cfg, bool mixed,
+cudaError_t launch_stage(const SolveDev* d, const StageTables& T, int stage, const LaunchCfg& cfg, int precision,
                          cudaStream_t st, Profiler* pf) {
   if (T.ntiles == 0) return cudaSuccess;
-  if (mixed) stage_ty<float>(d, T, stage, cfg, st, pf);
-  else stage_ty<double>(d, T, stage, cfg, st, pf);
+  if (precision == CBNS_FP32_MIXED) stage_ty<float>(d, T, stage, cfg, false, st, pf);
+  else stage_ty<double>(d, T, stage, cfg, precision == CBNS_FP64_FF, st, pf);
   return cudaGetLastError();
 }
 

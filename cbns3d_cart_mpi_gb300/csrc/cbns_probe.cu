@@ -10,6 +10,7 @@
 
 #include "../../include/cbns_gpu.h"
 #include "cbns_device.cuh"
+#include "cbns_ff.cuh"
 
 namespace {
 
@@ -79,5 +80,34 @@ extern "C" cbns_status cbns_probe_rcp64(const double* x, double* y, double* ref,
   if (!x || !y || !ref || n < 0) return CBNS_ERR_INVALID_ARG;
   if (n == 0) return CBNS_OK;
   k_rcp64<<<1024, 256>>>(x, y, ref, n);
+  return cudaDeviceSynchronize() == cudaSuccess ? CBNS_OK : CBNS_ERR_CUDA;
+}
+
+namespace {
+__global__ void k_ff(const double* __restrict__ x, const double* __restrict__ y, double* __restrict__ out,
+                     long long n) {
+  using namespace cbns;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const float2 a2 = ff_split(x[i]), b2 = ff_split(y[i]);
+    const ff a{a2.x, a2.y}, b{b2.x, b2.y};
+    double* o = out + 6 * i;
+    o[0] = ff_to_double(a);
+    o[1] = ff_to_double(ff_rcp(a));
+    o[2] = ff_to_double(ff_rsqrt(a));
+    o[3] = ff_to_double(a * b);
+    o[4] = ff_to_double(a + b);
+    o[5] = ff_to_double(ff_fma(a, b, a));
+  }
+}
+}  // namespace
+
+// The float-float building blocks of the CBNS_FP64_FF face kernel on n device
+// value pairs (x, y): out[6 i .. 6 i + 5] = the binary64 value of split(x),
+// 1/x, 1/sqrt(x), x*y, x+y and x*y + x, each evaluated in float-float from the
+// splits (test of their accuracy); device pointers, synchronous.
+extern "C" cbns_status cbns_probe_ff(const double* x, const double* y, double* out, long long n) {
+  if (!x || !y || !out || n < 0) return CBNS_ERR_INVALID_ARG;
+  if (n == 0) return CBNS_OK;
+  k_ff<<<1024, 256>>>(x, y, out, n);
   return cudaDeviceSynchronize() == cudaSuccess ? CBNS_OK : CBNS_ERR_CUDA;
 }

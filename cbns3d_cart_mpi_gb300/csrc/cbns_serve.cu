@@ -284,7 +284,7 @@ extern "C" {
 cbns_status cbns_server_create(const cbns_server_opts* opts, cbns_server** out) {
   if (!opts || !out) return serve_fail(CBNS_ERR_INVALID_ARG, "cbns_server_create: null argument");
   *out = nullptr;
-  if (opts->precision != CBNS_FP64 && opts->precision != CBNS_FP32_MIXED)
+  if (opts->precision != CBNS_FP64 && opts->precision != CBNS_FP32_MIXED && opts->precision != CBNS_FP64_FF)
     return serve_fail(CBNS_ERR_INVALID_ARG, "cbns_server_create: unknown precision");
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {

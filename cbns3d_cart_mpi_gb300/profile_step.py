@@ -1,6 +1,6 @@
 """A fixed number of RK3 steps of one solve, for kernel profilers (ncu).
 
-  python -m cbns3d_cart_mpi_gb300.profile_step [--N 256] [--precision fp64|fp32_mixed] [--steps 2]
+  python -m cbns3d_cart_mpi_gb300.profile_step [--N 256] [--precision fp64|fp32_mixed|fp64_ff] [--steps 2]
 
 Builds the Taylor-Green state on the device (cbns_init_tgv), then takes
 `steps` steps through cbns_step, whose kernels are launched one by one: per
@@ -18,7 +18,7 @@ from .solver import Solver
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--N", type=int, default=256)
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32_mixed"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32_mixed", "fp64_ff"])
     ap.add_argument("--steps", type=int, default=2)
     args = ap.parse_args()
     s = Solver(tgv_params(args.N, t_end=2.0), precision=args.precision)

@@ -11,7 +11,8 @@ import os
 import numpy as np
 
 from . import _lib
-from ._abi import CBNS_FINISHED, CBNS_FP32_MIXED, CBNS_FP64, CBNS_OK, NEQ, NG, STATUS_NAMES, CbnsParams
+from ._abi import (CBNS_FINISHED, CBNS_FP32_MIXED, CBNS_FP64, CBNS_FP64_FF, CBNS_OK, NEQ, NG, STATUS_NAMES,
+                   CbnsParams)
 
 
 class CbnsError(RuntimeError):
@@ -31,7 +32,7 @@ def _ptr(a):
     return a.ctypes.data_as(ctypes.c_void_p)
 
 
-PRECISIONS = {"fp64": CBNS_FP64, "fp32_mixed": CBNS_FP32_MIXED}
+PRECISIONS = {"fp64": CBNS_FP64, "fp32_mixed": CBNS_FP32_MIXED, "fp64_ff": CBNS_FP64_FF}
 
 
 class Solver:

@@ -49,7 +49,10 @@ typedef enum cbns_status {
 
 typedef enum cbns_precision {
   CBNS_FP64 = 0,       /* every operation in IEEE binary64 */
-  CBNS_FP32_MIXED = 1  /* WENO, projections and fluxes in binary32; state, RK3 and sums in binary64 */
+  CBNS_FP32_MIXED = 1, /* WENO, projections and fluxes in binary32; state, RK3 and sums in binary64 */
+  CBNS_FP64_FF = 2     /* as CBNS_FP64, but the inviscid face fluxes (Roe eigenvectors, WENO5,
+                          Lax-Friedrichs) in float-float arithmetic: pairs of binary32 numbers,
+                          about 47 significant bits, on the binary32 pipes */
 } cbns_precision;
 
 /*
@@ -247,7 +250,7 @@ void* cbns_batch_stream(cbns_batch* b);
 typedef struct cbns_server cbns_server;
 
 typedef struct cbns_server_opts {
-  int precision;                /* CBNS_FP64 or CBNS_FP32_MIXED */
+  int precision;                /* a cbns_precision */
   uint64_t memory_budget_bytes; /* device bytes for request state; 0 = 80% of free memory */
   uint32_t max_active;          /* most requests stepped together; 0 = no limit */
   uint32_t steps_per_round;     /* batch steps between scheduling rounds; 0 = 10 */

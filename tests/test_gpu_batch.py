@@ -27,7 +27,7 @@ def make(precision, t_ends=None):
     return out
 
 
-@pytest.mark.parametrize("precision", ["fp64", "fp32_mixed"])
+@pytest.mark.parametrize("precision", ["fp64", "fp32_mixed", "fp64_ff"])
 def test_batch_equals_alone_bitwise(precision):
     from cbns3d_cart_mpi_gb300.solver import Batch
     alone = make(precision)
@@ -42,7 +42,7 @@ def test_batch_equals_alone_bitwise(precision):
         assert a.time() == s.time()
 
 
-@pytest.mark.parametrize("precision", ["fp64", "fp32_mixed"])
+@pytest.mark.parametrize("precision", ["fp64", "fp32_mixed", "fp64_ff"])
 def test_every_launch_shape_gives_the_same_bits(precision):
     from cbns3d_cart_mpi_gb300.solver import Batch
     ref = None

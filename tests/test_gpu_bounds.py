@@ -8,7 +8,7 @@ access goes to element 0 instead, so nothing faults.  A child process loads
 that build (CBNS_GPU_LIB) and runs the stage, step-graph, batch, asynchronous
 and allocation-free paths on blocks at and near the smallest extents (NG = 4),
 odd and non-cubic shapes and an odd JM for the FP32-mixed two-row face kernel,
-in both precisions.  Every call must return CBNS_OK and every state must be
+in every precision.  Every call must return CBNS_OK and every state must be
 bitwise the one the normal build gives (a check changes addresses, never
 arithmetic).  tests/test_index_bounds.py restates the same offset arithmetic
 on the CPU.
@@ -39,7 +39,7 @@ def run_cases(out_path):
     from cbns3d_cart_mpi_gb300.solver import Batch, Solver, initial_condition_perturbed
 
     res = {}
-    for prec in ("fp64", "fp32_mixed"):
+    for prec in ("fp64", "fp32_mixed", "fp64_ff"):
         solves = []
         for q, (IM, JM, KM) in enumerate(SHAPES):
             p = tgv_params(IM, JM=JM, KM=KM, Re=800.0, Mach=0.2)

@@ -237,18 +237,20 @@ def test_diagnostics_match_oracle():
     assert abs(ke - ko) <= 1e-13 * ko and abs(en - eo) <= 1e-13 * eo
 
 
+@pytest.mark.parametrize("precision", ["fp64", "fp64_ff"])
 @pytest.mark.parametrize("Re,Mach,shape,seed", [(400.0, 0.3, (24, 20, 16), 11), (3200.0, 0.05, (20, 28, 12), 12),
                                                 (900.0, 0.15, (33, 17, 9), 13)])
-def test_parameter_corners_vs_oracle(Re, Mach, shape, seed):
+def test_parameter_corners_vs_oracle(Re, Mach, shape, seed, precision):
     """The ensemble and serving workloads draw Re in [400, 3200] and Ma in
     [0.05, 0.3] with perturbed initial data: corners of that range on odd block
-    shapes, 20 steps against the oracle at the parity bar."""
+    shapes, 20 steps against the oracle at the parity bar.  Float-float faces
+    (about 47 bits) get ten times the binary64 run's absolute bound."""
     from oracle.oracle import OracleBlock
     from cbns3d_cart_mpi_gb300.solver import Solver, initial_condition_perturbed
     IM, JM, KM = shape
     p = tgv_params(IM, JM=JM, KM=KM, Re=Re, Mach=Mach)
     Q0 = initial_condition_perturbed(p, seed=seed, amp=1e-3, nmodes=16, kmax=4)
-    s = Solver(p)
+    s = Solver(p, precision=precision)
     s.upload_Q(Q0, 0.0)
     o = OracleBlock(p)
     o.set_Q(Q0, 0.0)
@@ -256,7 +258,41 @@ def test_parameter_corners_vs_oracle(Re, Mach, shape, seed):
         dt, t = s.step()
         dto, to = o.step()
         assert abs(dt - dto) <= 1e-13 * dto, n
-    assert_close(interior(s.download_Q()), interior(o.get_Q()), 1e-11, "Re %g Ma %g" % (Re, Mach), tight=1e-13)
+    Qg, Qo = interior(s.download_Q()), interior(o.get_Q())
+    print(precision, "Re %g Ma %g rel Linf" % (Re, Mach), dict(zip(FIELDS, rel_linf(Qg, Qo))))
+    assert_close(Qg, Qo, 1e-11, "%s Re %g Ma %g" % (precision, Re, Mach),
+                 tight=1e-13 if precision == "fp64" else 1e-12)
+
+
+def test_fp64_ff_history_64_100_steps(golden_dir):
+    """CBNS_FP64_FF (float-float faces) at the binary64 parity bar: 64^3 TGV,
+    100 RK3 steps, against the reference's own state (every 4th cell) and its
+    KE and enstrophy history, and against the binary64 GPU run's full state."""
+    from cbns3d_cart_mpi_gb300.solver import Solver, initial_condition
+    g = load(golden_dir, "tgv64_hist.npz")
+    p = tgv_params(64)
+    states = {}
+    for prec in ("fp64", "fp64_ff"):
+        s = Solver(p, precision=prec)
+        s.upload_Q(initial_condition(p), 0.0)
+        worst_ke = worst_en = 0.0
+        for n in range(1, 101):
+            dt, t = s.step()
+            assert abs(dt - g["dt"][n - 1]) <= 1e-12 * g["dt"][n - 1], (prec, n)
+            if n % 10 == 0:
+                m = n // 10
+                ke, en = s.diagnostics()
+                worst_ke = max(worst_ke, abs(ke - g["ke"][m]) / g["ke"][m])
+                worst_en = max(worst_en, abs(en - g["enstrophy"][m]) / g["enstrophy"][m])
+        assert worst_ke <= 1e-10 and worst_en <= 1e-10, (prec, worst_ke, worst_en)
+        states[prec] = interior(s.download_Q())
+        s.close()
+        print(prec, "64^3 x 100 steps vs reference (every 4th cell): rel Linf",
+              dict(zip(FIELDS, rel_linf(states[prec][::4, ::4, ::4], g["Q100_sub"]))), "; KE", worst_ke,
+              "; enstrophy", worst_en)
+    assert_close(states["fp64_ff"][::4, ::4, ::4], g["Q100_sub"], 1e-11, "fp64_ff step 100 vs reference")
+    print("fp64_ff vs fp64 full state: rel Linf", dict(zip(FIELDS, rel_linf(states["fp64_ff"], states["fp64"]))))
+    assert_close(states["fp64_ff"], states["fp64"], 1e-11, "fp64_ff vs fp64 step 100")
 
 
 def test_face_reciprocal_within_one_ulp_of_ieee_division():
@@ -284,3 +320,56 @@ def test_face_reciprocal_within_one_ulp_of_ieee_division():
     ulps = np.abs(yb - rb)
     print("rcp64 vs 1.0/x: max %d ulp, %.3g of values differ" % (ulps.max(), (ulps > 0).mean()))
     assert ulps.max() <= 1
+
+
+def test_float_float_building_blocks_against_binary64():
+    """The float-float arithmetic of CBNS_FP64_FF faces (csrc/cbns_ff.cuh) on the
+    GPU against numpy's binary64: the split of a binary64 value into two binary32
+    parts keeps 47 bits (relative error below 2^-46); reciprocal, reciprocal
+    square root and product within 2^-44 relative; sum and x*y + x within 2^-44
+    of the operands' magnitudes.  Below binary32's normal range a split is 0 (an
+    absolute error under 2^-126), and a value beyond it splits to NaN."""
+    import ctypes
+
+    import torch
+
+    from cbns3d_cart_mpi_gb300 import _lib
+    rng = np.random.default_rng(11)
+    m = 1 << 18
+    # Float-float shares binary32's exponent range: the split is tried over
+    # [1e-30, 1e30], the arithmetic where results and their low parts stay normal.
+    x = np.concatenate([10.0 ** rng.uniform(-30, 30, m), 10.0 ** rng.uniform(-9, 9, m), rng.uniform(0.1, 10.0, m)])
+    y = np.concatenate([np.ones(m), 10.0 ** rng.uniform(-9, 9, m), rng.uniform(-10.0, 10.0, m)])
+    x[m:m + m // 2] *= np.where(rng.random(m // 2) < 0.5, -1.0, 1.0)  # signed values for the split and sum
+    special = np.array([0.0, -0.0, 1e-35, -1e-35, 1e-40, 3e38, 1e39, -1e300])
+    dev = torch.device("cuda", torch.cuda.current_device())
+    xs = np.concatenate([x, special])
+    ys = np.concatenate([y, np.ones(special.size)])
+    xd, yd = torch.from_numpy(xs).to(dev), torch.from_numpy(ys).to(dev)
+    out = torch.empty(6 * xs.size, dtype=torch.float64, device=dev)
+    st = _lib.probe().cbns_probe_ff(ctypes.c_void_p(xd.data_ptr()), ctypes.c_void_p(yd.data_ptr()),
+                                    ctypes.c_void_p(out.data_ptr()), xs.size)
+    assert st == 0
+    o = out.cpu().numpy().reshape(-1, 6)
+    r, sp = o[:x.size], o[x.size:]
+    a = slice(m, x.size)  # the arithmetic's operands
+    xa, ya, ra = x[a], y[a], r[a]
+    pos = xa > 0
+    errs = {
+        "split": np.abs(r[:, 0] - x) / np.abs(x),
+        "rcp": np.abs(ra[pos, 1] * xa[pos] - 1.0),
+        "rsqrt": np.abs(ra[pos, 2] * np.sqrt(xa[pos]) - 1.0),
+        "mul": np.abs(ra[:, 3] - xa * ya) / np.abs(xa * ya),
+        "add": np.abs(ra[:, 4] - (xa + ya)) / (np.abs(xa) + np.abs(ya)),
+        "fma": np.abs(ra[:, 5] - (xa * ya + xa)) / (np.abs(xa * ya) + np.abs(xa)),
+    }
+    print("float-float max relative errors (log2):", {k: round(float(np.log2(v.max())), 2) for k, v in errs.items()})
+    assert errs["split"].max() < 2.0 ** -46
+    for k in ("rcp", "rsqrt", "mul", "add", "fma"):
+        assert errs[k].max() < 2.0 ** -44, k
+    # specials: signed zeros, below the normal range, beyond it
+    assert sp[0, 0] == 0.0 and sp[1, 0] == 0.0 and np.signbit(sp[1, 0])
+    assert abs(sp[2, 0] - 1e-35) <= 2.0 ** -23 * 1e-35 and abs(sp[3, 0] + 1e-35) <= 2.0 ** -23 * 1e-35
+    assert sp[4, 0] == 0.0
+    assert abs(sp[5, 0] - 3e38) <= 2.0 ** -46 * 3e38
+    assert np.isnan(sp[6, 0]) and np.isnan(sp[7, 0])

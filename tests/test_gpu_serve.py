@@ -58,7 +58,7 @@ def test_device_initial_condition_matches_host():
 LONG = dict(N=32, JM=32, KM=32, Re=1200.0, Mach=0.1, t_end=1.0, seed=7)
 
 
-@pytest.mark.parametrize("precision", ["fp64", "fp32_mixed"])
+@pytest.mark.parametrize("precision", ["fp64", "fp32_mixed", "fp64_ff"])
 def test_results_same_alone_and_in_the_mix(precision):
     """Two requests start; once the server has stepped them for a round, two more
     arrive.  The late ones must be admitted after the first ones and before the

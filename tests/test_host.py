@@ -270,17 +270,22 @@ def test_block_size_limit_follows_memory_not_a_31_bit_index():
     """Offsets are 64-bit, so a block is limited by device memory (cbns_create
     compares cbns_footprint's arena size with the free bytes) and by the 16-bit
     tile coordinates, not by 5 (N+8)^3 < 2^31 (N ~ 745).  The arena of a 768^3
-    block fits the 280 GB a GB300 offers in both precisions, 1024^3 does not."""
+    block fits the 280 GB a GB300 offers in every precision, 1024^3 does not."""
     from cbns3d_cart_mpi_gb300.solver import CbnsError, footprint
     hbm = 280e9
     per_cell = {}
-    for prec in ("fp64", "fp32_mixed"):
+    for prec in ("fp64", "fp32_mixed", "fp64_ff"):
         fp768 = footprint(768, 768, 768, prec)
         assert fp768 < hbm, (prec, fp768)
         assert footprint(1024, 1024, 1024, prec) > hbm
         per_cell[prec] = fp768 / 776 ** 3
-        # grows with the padded volume: about 380 bytes per padded cell
-        assert 300 < per_cell[prec] < 420, per_cell
+        # grows with the padded volume: about 380 bytes per padded cell (500 with
+        # the float-float copies)
+        assert 300 < per_cell[prec] < 520, per_cell
+    # Float-float faces add float-float copies of Q and Q_p and of five face
+    # primitives: 15 pairs of binary32 (120 bytes) per padded cell.
+    extra = footprint(256, 256, 256, "fp64_ff") - footprint(256, 256, 256, "fp64")
+    assert abs(extra - 120 * 264 ** 3) < 4096, extra
     # 745^3 and 746^3 straddle the old 31-bit limit; both are accepted now.
     assert footprint(746, 746, 746) > footprint(745, 745, 745)
     # Tile coordinates are 16-bit: 65535 - 2 NG cells along an axis is the most.
