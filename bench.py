@@ -52,6 +52,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-mixed", action="store_true", help="skip the FP32-mixed leg")
+    ap.add_argument("--no-ff", action="store_true", help="skip the float-float faces leg (CBNS_FP64_FF)")
     ap.add_argument("--no-large", action="store_true", help="skip the 512^3 and 768^3 blocks")
     return ap.parse_args()
 
@@ -318,37 +319,42 @@ def run_ours(args, rank, world, local):
             "hbm_gbs_min_state": state_bytes_per_step(N, N, N) / (step_ms * 1e-3) * 1e-9,
         }
 
-    # FP32-mixed leg: same workload, same number of steps; error against the
-    # binary64 state after the same steps.
-    if not args.no_mixed:
-        Q64 = s.download_Q()
-        sm = Solver(p, precision="fp32_mixed")
-        sm.upload_Q(Q0, 0.0)
-        mstream = torch.cuda.ExternalStream(sm.stream)
-        sm.run(args.warmup)
+    # The other precisions' legs: same workload, same number of steps (warm-up,
+    # timed, profiled), and the error against the binary64 state after them.
+    Q64 = s.download_Q() if not (args.no_mixed and args.no_ff) else None
+
+    def precision_leg(prec):
+        sx = Solver(p, precision=prec)
+        sx.upload_Q(Q0, 0.0)
+        xstream = torch.cuda.ExternalStream(sx.stream)
+        sx.run(args.warmup)
         torch.cuda.synchronize()
         barrier(world)
-        m0 = torch.cuda.Event(enable_timing=True)
-        m1 = torch.cuda.Event(enable_timing=True)
-        m0.record(mstream)
-        sm.run(args.steps)
-        m1.record(mstream)
-        m1.synchronize()
-        mms = reduce_max(m0.elapsed_time(m1), world)
-        sm.profile_begin()
-        sm.run(args.steps)
-        mprof = sm.profile_end()
-        Qm = sm.download_Q()
-        sm.close()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(xstream)
+        sx.run(args.steps)
+        e1.record(xstream)
+        e1.synchronize()
+        xms = reduce_max(e0.elapsed_time(e1), world)
+        sx.profile_begin()
+        sx.run(args.steps)
+        xprof = sx.profile_end()
+        a = sx.download_Q()[NG:-NG, NG:-NG, NG:-NG].reshape(-1, 5)
+        sx.close()
+        b = Q64[NG:-NG, NG:-NG, NG:-NG].reshape(-1, 5)
+        # L-inf error over each field's scale; the three momentum fields share
+        # the largest momentum magnitude (rho w starts at exactly zero, so its own
+        # maximum is no scale in the first steps).
+        scale = np.abs(b).max(axis=0)
+        scale[1:4] = scale[1:4].max()
+        err = (np.abs(a - b).max(axis=0) / scale).tolist()
+        return xms, xprof, err
+
+    # FP32-mixed leg.
+    if not args.no_mixed:
+        mms, mprof, err = precision_leg("fp32_mixed")
         if rank == 0:
-            a = Qm[NG:-NG, NG:-NG, NG:-NG].reshape(-1, 5)
-            b = Q64[NG:-NG, NG:-NG, NG:-NG].reshape(-1, 5)
-            # L-inf error over each field's scale; the three momentum fields share
-            # the largest momentum magnitude (rho w starts at exactly zero, so its own
-            # maximum is no scale in the first steps).
-            scale = np.abs(b).max(axis=0)
-            scale[1:4] = scale[1:4].max()
-            err = (np.abs(a - b).max(axis=0) / scale).tolist()
             mtot = sum(v[1] for v in mprof.values())
             mdom = max(mprof, key=lambda k: mprof[k][1])
             if mdom.startswith("inviscid_"):
@@ -379,6 +385,36 @@ def run_ours(args, rank, world, local):
                 "kernels": {k: {"launches": v[0], "ms_per_launch": v[1] / v[0], "share": v[1] / mtot}
                             for k, v in mprof.items()},
                 "roofline": mroof,
+            }
+
+    # Float-float faces leg (CBNS_FP64_FF): the binary64 solve with its face
+    # fluxes in float-float arithmetic on the binary32 pipes.  The face kernel's
+    # roofline: binary32 instructions issued (ncu count per face) over the
+    # binary32 FMA pipe's measured instruction rate.
+    if not args.no_ff:
+        fms, fprof, ferr = precision_leg("fp64_ff")
+        if rank == 0:
+            ftot = sum(v[1] for v in fprof.values())
+            fper = fprof["inviscid_x"][1] / fprof["inviscid_x"][0]
+            froof = {"bound": "fp32-pipe", "kernel": "inviscid_x", "unit": "TFLOP/s",
+                     "peak": probe_peak(fp64=False), "peak_source": "binary32 FMA throughput measured live "
+                                                                  "(cbns_probe_peak)"}
+            finst = counts.get("inviscid_x_ff_fp32_inst_per_face")
+            if finst:
+                issued = finst * N ** 3 / (fper * 1e-3)  # binary32 instructions per second
+                froof["fp32_inst_per_face"] = finst
+                froof["achieved"] = issued * 2.0 * 1e-12  # as FMA-equivalent TFLOP/s
+                froof["frac"] = froof["achieved"] / froof["peak"]
+                froof["note"] = ("float-float arithmetic: binary32 instructions per face (ncu) over the pipe's "
+                                 "instruction rate; the reference's 1570 FLOPs per face take about 3.6 of them each")
+            line["fp64_ff"] = {
+                "value": world * cells * args.steps / (fms * 1e-3), "unit": UNIT, "ms_per_step": fms / args.steps,
+                "speedup_vs_fp64": ms / fms,
+                "linf_vs_fp64_over_field_scale": dict(zip(["rho", "rho*u", "rho*v", "rho*w", "E"], ferr)),
+                "error_after_steps": args.warmup + 2 * args.steps,
+                "kernels": {k: {"launches": v[0], "ms_per_launch": v[1] / v[0], "share": v[1] / ftot}
+                            for k, v in fprof.items()},
+                "roofline": froof,
             }
 
     # e2e: host buffers through the C ABI, copies inside the timed region.  Every

@@ -13,6 +13,8 @@
 // float-float forms allow; the notes there give the algebra.
 #include <cuda_runtime.h>
 
+#include <mutex>
+
 #include "cbns_device.cuh"
 #include "cbns_ff.cuh"
 #include "cbns_prof.h"
@@ -78,18 +80,40 @@ __device__ __forceinline__ void weno5_pair_ff(const ff (&v)[6], WenoFF& L, WenoF
                 ff_fma(-k56, d3, k13 * d4), -(t2 + d3), ff_scale(d1, 0.5f) - t2, Rt);
 }
 
+// Per-thread float-float slots in shared memory: slot k of thread tid is the
+// pair of binary32 words (2k, 2k+1) of a thread-minor array, so a warp's accesses
+// to one slot are 32 consecutive words (no bank conflicts).  A thread touches
+// only its own slots, so no barrier is needed.
+struct Slots {
+  float* base;
+  int T, tid;
+  __device__ __forceinline__ void put(int k, ff v) const {
+    base[(2 * k) * T + tid] = v.hi;
+    base[(2 * k + 1) * T + tid] = v.lo;
+  }
+  __device__ __forceinline__ ff get(int k) const { return ff{base[(2 * k) * T + tid], base[(2 * k + 1) * T + tid]}; }
+};
+constexpr int kFaceSlots = NEQ * 6;  // the characteristic fields of the six stencil cells
+
 // The face flux (binary64 face_core's steps; the stored flux is twice the
-// reference's, the halves folded into the update's 0.5/h).
+// reference's, the halves folded into the update's 0.5/h).  A face is about
+// 6,000 binary32 instructions; written out in full for the six stencil cells
+// and five fields it overflows the instruction cache, so the projections (per
+// cell) and the reconstructions (per field) run as loops over the thread's
+// shared-memory slots, one copy of each body.  U: the stage input's float-float
+// copy, c the face's cell (the face between c - st and c).
 template <int D>
-__device__ __forceinline__ void face_core_ff(const SolveDev& s, const ff (&W)[6][NEQ], const SideFF& Ls,
-                                             const SideFF& Rs, ff (&out)[NEQ]) {
+__device__ __forceinline__ void face_ff(const SolveDev& s, const float2* __restrict__ U, long long c,
+                                        long long st, const Slots& sl, ff (&out)[NEQ]) {
   constexpr int T1 = (D + 1) % 3;
   constexpr int T2 = (D + 2) % 3;
+  const long long V = s.V, n5 = NEQ * V;
   const ff gam1 = cst(s.ff_gam1), gamma = cst(s.ff_gamma), hgam1 = cst(s.ff_hgam1);
 
   // Roe average: f_R + wL (f_L - f_R), wL = sqrt(rho_L) / (sqrt(rho_L) + sqrt(rho_R)).
   ff Uv[3], HH;
   {
+    const SideFF Ls = side_ff(s, c - st), Rs = side_ff(s, c);
     const ff wL = Ls.sr * ff_rcp(Ls.sr + Rs.sr);
     Uv[0] = ff_fma(wL, Ls.u - Rs.u, Rs.u);
     Uv[1] = ff_fma(wL, Ls.v - Rs.v, Rs.v);
@@ -105,30 +129,48 @@ __device__ __forceinline__ void face_core_ff(const SolveDev& s, const ff (&W)[6]
   const ff hic = ff_scale(ic, 0.5f);
   const ff un = Uv[D], u1 = Uv[T1], u2 = Uv[T2];
 
-  // Characteristic projections of the six stencil cells.
-  ff w[NEQ][6];
+  // Characteristic projections of the six stencil cells c-3 .. c+2 into slots
+  // 6 n + m; the next cell's state is loaded while this one is projected.
+  ff f[NEQ];
 #pragma unroll
+  for (int n = 0; n < NEQ; ++n) f[n] = ld(s, U, n5, n * V + c - 3 * st);
+#pragma unroll 1
   for (int m = 0; m < 6; ++m) {
-    const ff f0 = W[m][0], f4 = W[m][4];
-    const ff fm[3] = {W[m][1], W[m][2], W[m][3]};
+    ff g5[NEQ];
+    const long long o = c + (m - 2) * st;  // the next cell (not loaded after the last)
+#pragma unroll
+    for (int n = 0; n < NEQ; ++n) g5[n] = m < 5 ? ld(s, U, n5, n * V + o) : f[n];
+    const ff f0 = f[0], f4 = f[4];
+    const ff fm[3] = {f[1], f[2], f[3]};
     const ff t = ff_fma(-Uv[2], fm[2], ff_fma(-Uv[1], fm[1], ff_fma(-Uv[0], fm[0], ff_fma(hq2, f0, f4))));
     const ff A = K * t;
     const ff g = ff_fma(un, f0, -fm[D]);
-    w[0][m] = ff_fma(hic, g, A);
-    w[1][m] = f0 - ff_scale(A, 2.0f);
-    w[2][m] = ff_fma(-hic, g, A);
-    w[3][m] = ff_fma(-u1, f0, fm[T1]);
-    w[4][m] = ff_fma(-u2, f0, fm[T2]);
+    sl.put(m, ff_fma(hic, g, A));
+    sl.put(6 + m, f0 - ff_scale(A, 2.0f));
+    sl.put(12 + m, ff_fma(-hic, g, A));
+    sl.put(18 + m, ff_fma(-u1, f0, fm[T1]));
+    sl.put(24 + m, ff_fma(-u2, f0, fm[T2]));
+#pragma unroll
+    for (int n = 0; n < NEQ; ++n) f[n] = g5[n];
   }
 
-  // Left- and right-biased reconstructions, r = base + num / den.
+  // Left- and right-biased reconstructions of each field, r = base + num / den,
+  // into the field's slots 6 n (left) and 6 n + 1 (right).
+#pragma unroll 1
+  for (int n = 0; n < NEQ; ++n) {
+    ff v[6];
+#pragma unroll
+    for (int m = 0; m < 6; ++m) v[m] = sl.get(6 * n + m);
+    WenoFF a, b;
+    weno5_pair_ff(v, a, b);
+    sl.put(6 * n, ff_fma(a.num, ff_rcp(a.den), v[2]));
+    sl.put(6 * n + 1, ff_fma(b.num, ff_rcp(b.den), v[3]));
+  }
   ff rl[NEQ], rr[NEQ];
 #pragma unroll
   for (int n = 0; n < NEQ; ++n) {
-    WenoFF a, b;
-    weno5_pair_ff(w[n], a, b);
-    rl[n] = ff_fma(a.num, ff_rcp(a.den), w[n][2]);
-    rr[n] = ff_fma(b.num, ff_rcp(b.den), w[n][3]);
+    rl[n] = sl.get(6 * n);
+    rr[n] = sl.get(6 * n + 1);
   }
 
   // Back to conserved variables.
@@ -180,9 +222,12 @@ __device__ __forceinline__ void face_core_ff(const SolveDev& s, const ff (&W)[6]
 
 // One face per thread over the interior tiles (the binary64 k_inviscid's walk).
 // The stage input is Q's float-float copy in stage 1 and Q_p's in stages 2-3.
+// Dynamic shared memory: kFaceSlots float-float slots per thread.
 template <int D>
 __global__ void __maxnreg__(128) k_inviscid_ff(const SolveDev* __restrict__ solves,
                                                const TileRef* __restrict__ tiles, int ntiles, int stage) {
+  extern __shared__ float face_slots[];
+  const Slots sl{face_slots, (int)blockDim.x, (int)threadIdx.x};
   for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
     const TileCell tc = tile_cell(tiles[t], 0);
     const SolveDev& s = solves[tc.s];
@@ -190,15 +235,8 @@ __global__ void __maxnreg__(128) k_inviscid_ff(const SolveDev* __restrict__ solv
     if (tc.i >= s.IM || tc.j >= s.JM) continue;
     const float2* U = stage == 1 ? s.QF : s.QpF;
     const long long st = D == 0 ? 1ll : (D == 1 ? (long long)s.nx : (long long)s.nx * s.ny);
-    const long long V = s.V, c = pad_off(s, tc.i, tc.j, tc.k);
-    ff W[6][NEQ];
-#pragma unroll
-    for (int m = 0; m < 6; ++m) {
-#pragma unroll
-      for (int n = 0; n < NEQ; ++n) W[m][n] = ld(s, U, NEQ * V, n * V + c + (m - 3) * st);
-    }
     ff f[NEQ];
-    face_core_ff<D>(s, W, side_ff(s, c - st), side_ff(s, c), f);
+    face_ff<D>(s, U, pad_off(s, tc.i, tc.j, tc.k), st, sl, f);
     const long long fo = int_off(s, tc.i, tc.j, tc.k);
     double* F = s.F[D];
 #pragma unroll
@@ -211,9 +249,18 @@ __global__ void __maxnreg__(128) k_inviscid_ff(const SolveDev* __restrict__ solv
 // The three face launches of a stage (grid g, nt threads: the binary64 tiles).
 void launch_faces_ff(const SolveDev* d, const TileRef* tiles, int ntiles, int stage, int g, int nt,
                      cudaStream_t st, Profiler* pf) {
+  // shared memory for kFaceSlots float-float slots per thread, up to 256 threads
+  constexpr int kMaxBytes = 256 * kFaceSlots * 2 * (int)sizeof(float);
+  static std::once_flag once;
+  std::call_once(once, [] {
+    cudaFuncSetAttribute(k_inviscid_ff<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxBytes);
+    cudaFuncSetAttribute(k_inviscid_ff<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxBytes);
+    cudaFuncSetAttribute(k_inviscid_ff<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxBytes);
+  });
+  const size_t smem = (size_t)nt * kFaceSlots * 2 * sizeof(float);
   auto run = [&](int id, auto kern) {
     if (pf) pf->before(id, st);
-    kern<<<g, nt, 0, st>>>(d, tiles, ntiles, stage);
+    kern<<<g, nt, smem, st>>>(d, tiles, ntiles, stage);
     if (pf) pf->after(st);
   };
   run(KID_INVISCID_X, k_inviscid_ff<0>);
