@@ -146,7 +146,7 @@ ArenaLayout arena_layout(const SolveDev& s, int precision, size_t n_int, size_t 
       const size_t f2V = sizeof(float2) * (size_t)s.V;
       L.oQF = take(NEQ * f2V);
       L.oQpF = take(NEQ * f2V);
-      L.oPF = take(5 * f2V);
+      L.oPF = take(kFFPrims * f2V);
     }
   } else {
     L.oU32 = take(NEQ * fV);  // U4 (4 values per cell), then UE
@@ -405,6 +405,18 @@ cbns_status cbns_create(const cbns_params* p, uint32_t IM, uint32_t JM, uint32_t
     s.ff_gam1 = split(s.gam1);
     s.ff_gamma = split(s.gamma);
     s.ff_hgam1 = split(0.5 * s.gam1);
+    const Consts<double>& c = s.cd;
+    const double hf[3] = {c.hfx, c.hfy, c.hfz}, c12[3] = {c.c12x, c.c12y, c.c12z},
+                 c23[3] = {c.c23x, c.c23y, c.c23z};
+    for (int d = 0; d < 3; ++d) {
+      s.ff_hf[d] = split(hf[d]);
+      s.ff_c12[d] = split(c12[d]);
+      s.ff_c23[d] = split(c23[d]);
+    }
+    s.ff_Re_inv = split(s.Re_inv);
+    s.ff_kappa = split(s.kappa);
+    s.ff_C = split(s.C_T_inf);
+    s.ff_C1 = split(s.C_T_inf1);
   }
   h->d_ctl = (SolveCtl*)(A + oCtl);
   s.ctl = h->d_ctl;

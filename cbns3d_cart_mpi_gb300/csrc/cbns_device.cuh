@@ -137,17 +137,27 @@ struct SolveDev {
   Consts<float> cf;
   SolveCtl* ctl;
   double C_T_inf1;  // 1 + C_T_inf, Sutherland's law (binary64 viscous terms)
-  // Binary64 solves with float-float faces (CBNS_FP64_FF): the face kernel's
-  // inputs as float-float pairs {hi, lo}, written with the binary64 state by the
-  // update and start-up kernels: the state Q and Q_p (5 blocks of V each) and
-  // the face primitives sqrt(rho), H, u, v, w (5 blocks of V); the constants
-  // gamma - 1, gamma and (gamma - 1)/2.  Null / unused otherwise.
+  // CBNS_FP64_FF solves: the binary64 state, RK3 and primitives, with the face
+  // fluxes, the viscous terms and the flux differences in float-float
+  // arithmetic.  Its inputs as float-float pairs {hi, lo}, written with the
+  // binary64 state by the update and start-up kernels: the state Q and Q_p (5
+  // blocks of V each) and the primitives sqrt(rho), H, u, v, w, T (kFFPrims
+  // blocks of V).  The face fluxes and viscous terms are float-float pairs in
+  // the bytes of F[d] and Tv (8 bytes a value in both forms).  Float-float
+  // constants: gamma - 1, gamma, (gamma - 1)/2; 0.5/h, the 4th-order weights
+  // c12 and c23 per direction; 1/Re, kappa, C and 1 + C of Sutherland's law.
+  // Null / unused otherwise.
   int ffaces;
   float2* QF;
   float2* QpF;
   float2* PF;
   float2 ff_gam1, ff_gamma, ff_hgam1;
+  float2 ff_hf[3], ff_c12[3], ff_c23[3];
+  float2 ff_Re_inv, ff_kappa, ff_C, ff_C1;
 };
+
+// Blocks of SolveDev::PF: sqrt(rho), H, u, v, w, T.
+constexpr int kFFPrims = 6;
 
 template <typename R>
 __host__ __device__ inline const Consts<R>& consts_of(const SolveDev& s);

@@ -36,7 +36,7 @@ struct SideFF {
 };
 
 __device__ __forceinline__ SideFF side_ff(const SolveDev& s, long long o) {
-  const long long V = s.V, n5 = 5 * V;
+  const long long V = s.V, n5 = kFFPrims * V;
   const float2* P = s.PF;
   return SideFF{ld(s, P, n5, o), ld(s, P, n5, V + o), ld(s, P, n5, 2 * V + o), ld(s, P, n5, 3 * V + o),
                 ld(s, P, n5, 4 * V + o)};
@@ -238,9 +238,74 @@ __global__ void __maxnreg__(128) k_inviscid_ff(const SolveDev* __restrict__ solv
     ff f[NEQ];
     face_ff<D>(s, U, pad_off(s, tc.i, tc.j, tc.k), st, sl, f);
     const long long fo = int_off(s, tc.i, tc.j, tc.k);
-    double* F = s.F[D];
+    float2* F = reinterpret_cast<float2*>(s.F[D]);
 #pragma unroll
-    for (int n = 0; n < NEQ; ++n) at(s, F, NEQ * s.IV, n * s.IV + fo) = ff_to_double(f[n]);
+    for (int n = 0; n < NEQ; ++n) at(s, F, NEQ * s.IV, n * s.IV + fo) = make_float2(f[n].hi, f[n].lo);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Viscous terms on the NGV ring (the binary64 k_viscous in float-float: the
+// 4th-order gradients of u, v, w, T, Sutherland mu, the six stresses and three
+// energy fluxes; src/calc_gradient.cpp:17-66, src/Block3d.cpp:750-868).  The
+// terms are float-float pairs in Tv's bytes; mu (interior, lagged into the time
+// step) is stored in binary64.  Plane tiles over the ring, as the binary64 kernel.
+
+__device__ __forceinline__ ff d4_ff(const SolveDev& s, const float2* f, long long n, long long o, long long st,
+                                    ff c12, ff c23) {
+  // ((f[-2] - f[+2]) c12 + (f[+1] - f[-1]) c23), the 1/h folded into the weights
+  return ff_fma(ld(s, f, n, o - 2 * st) - ld(s, f, n, o + 2 * st), c12,
+                (ld(s, f, n, o + st) - ld(s, f, n, o - st)) * c23);
+}
+
+__global__ void __launch_bounds__(256) k_viscous_ff(const SolveDev* __restrict__ solves,
+                                                    const TileRef* __restrict__ tiles, int ntiles) {
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const TileRef tr = tiles[t];
+    const SolveDev& s = solves[tr.solve];
+    if (!s.ctl->active) continue;
+    const long long p = plane_tile_first(tr, (int)blockDim.x) + threadIdx.x;
+    if (p >= (long long)s.rx * s.ry) continue;
+    const int jr = (int)(p / s.rx);
+    const int i = (int)(p - (long long)jr * s.rx) - NGV, j = jr - NGV, k = (int)tr.tk - NGV;
+    const long long V = s.V;
+    const long long o = pad_off(s, i, j, k);
+    const long long sy = s.nx, sz = (long long)s.nx * s.ny;
+    const float2* P = s.PF;
+    const float2 *Pu = P + 2 * V, *Pv = P + 3 * V, *Pw = P + 4 * V, *PT = P + 5 * V;
+    const long long nb = V;  // each block's extent (the checked build's bound)
+    const ff ax = cst(s.ff_c12[0]), bx = cst(s.ff_c23[0]), ay = cst(s.ff_c12[1]), by = cst(s.ff_c23[1]),
+             az = cst(s.ff_c12[2]), bz = cst(s.ff_c23[2]);
+    const ff ux = d4_ff(s, Pu, nb, o, 1, ax, bx), uy = d4_ff(s, Pu, nb, o, sy, ay, by),
+             uz = d4_ff(s, Pu, nb, o, sz, az, bz);
+    const ff vx = d4_ff(s, Pv, nb, o, 1, ax, bx), vy = d4_ff(s, Pv, nb, o, sy, ay, by),
+             vz = d4_ff(s, Pv, nb, o, sz, az, bz);
+    const ff wx = d4_ff(s, Pw, nb, o, 1, ax, bx), wy = d4_ff(s, Pw, nb, o, sy, ay, by),
+             wz = d4_ff(s, Pw, nb, o, sz, az, bz);
+    const ff Tx = d4_ff(s, PT, nb, o, 1, ax, bx), Ty = d4_ff(s, PT, nb, o, sy, ay, by),
+             Tz = d4_ff(s, PT, nb, o, sz, az, bz);
+    const ff uu = ld(s, Pu, nb, o), vv = ld(s, Pv, nb, o), ww = ld(s, Pw, nb, o), Tl = ld(s, PT, nb, o);
+    // Sutherland's law as (1 + C) T^2 / sqrt(T (T + C)^2).
+    const ff TC = Tl + cst(s.ff_C);
+    const ff mu = (cst(s.ff_C1) * ff_sqr(Tl)) * ff_rsqrt(Tl * ff_sqr(TC));
+    if (i >= 0 && i < s.IM && j >= 0 && j < s.JM && k >= 0 && k < s.KM) at(s, s.pd.mu, V, o) = ff_to_double(mu);
+    const ff mr = mu * cst(s.ff_Re_inv);
+    const ff m23 = ff_const(2.0 / 3.0) * mr;
+    const ff txx = m23 * ((ff_scale(ux, 2.0f) - vy) - wz);
+    const ff tyy = m23 * ((ff_scale(vy, 2.0f) - ux) - wz);
+    const ff tzz = m23 * ((ff_scale(wz, 2.0f) - ux) - vy);
+    const ff txy = mr * (uy + vx);
+    const ff txz = mr * (uz + wx);
+    const ff tyz = mr * (vz + wy);
+    const ff mk = mr * cst(s.ff_kappa);
+    const ff ex = ff_fma(ww, txz, ff_fma(vv, txy, uu * txx)) - mk * Tx;
+    const ff ey = ff_fma(ww, tyz, ff_fma(vv, tyy, uu * txy)) - mk * Ty;
+    const ff ez = ff_fma(ww, tzz, ff_fma(vv, tyz, uu * txz)) - mk * Tz;
+    const long long r = ring_off(s, i, j, k), RV = s.RV, n9 = kViscTerms * RV;
+    float2* Tv = reinterpret_cast<float2*>(s.Tv);
+    const ff terms[kViscTerms] = {txx, tyy, tzz, txy, txz, tyz, ex, ey, ez};
+#pragma unroll
+    for (int q = 0; q < kViscTerms; ++q) at(s, Tv, n9, q * RV + r) = make_float2(terms[q].hi, terms[q].lo);
   }
 }
 
@@ -266,6 +331,14 @@ void launch_faces_ff(const SolveDev* d, const TileRef* tiles, int ntiles, int st
   run(KID_INVISCID_X, k_inviscid_ff<0>);
   run(KID_INVISCID_Y, k_inviscid_ff<1>);
   run(KID_INVISCID_Z, k_inviscid_ff<2>);
+}
+
+// The viscous launch of a stage over the ring's plane tiles (grid g, nt threads).
+void launch_viscous_ff(const SolveDev* d, const TileRef* ring, int nring, int g, int nt, cudaStream_t st,
+                       Profiler* pf) {
+  if (pf) pf->before(KID_VISCOUS, st);
+  k_viscous_ff<<<g, nt, 0, st>>>(d, ring, nring);
+  if (pf) pf->after(st);
 }
 
 }  // namespace cbns

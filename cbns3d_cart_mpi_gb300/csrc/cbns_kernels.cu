@@ -100,20 +100,21 @@ __device__ __forceinline__ void store_prims(const SolveDev& s, long long o, doub
   at(s, s.pd.H, V, o) = q.H;
 }
 
-// CBNS_FP64_FF solves: the float-float copies the face kernel reads, of a cell's
-// state (into QFo, the copy of the array the state went to) and of its face
-// primitives sqrt(rho), H, u, v, w (split on the integer pipe).
+// CBNS_FP64_FF solves: the float-float copies the face and viscous kernels
+// read, of a cell's state (into QFo, the copy of the array the state went to)
+// and of its primitives sqrt(rho), H, u, v, w, T (split on the integer pipe).
 __device__ __forceinline__ void store_ff(const SolveDev& s, float2* QFo, long long d, const double (&q)[NEQ],
-                                         double sr, double H, double u, double v, double w) {
-  const long long V = s.V, n5 = NEQ * V;
+                                         double sr, double H, double u, double v, double w, double T) {
+  const long long V = s.V, n5 = NEQ * V, np = kFFPrims * V;
 #pragma unroll
   for (int n = 0; n < NEQ; ++n) at(s, QFo, n5, n * V + d) = ff_split(q[n]);
   float2* P = s.PF;
-  at(s, P, n5, d) = ff_split(sr);
-  at(s, P, n5, V + d) = ff_split(H);
-  at(s, P, n5, 2 * V + d) = ff_split(u);
-  at(s, P, n5, 3 * V + d) = ff_split(v);
-  at(s, P, n5, 4 * V + d) = ff_split(w);
+  at(s, P, np, d) = ff_split(sr);
+  at(s, P, np, V + d) = ff_split(H);
+  at(s, P, np, 2 * V + d) = ff_split(u);
+  at(s, P, np, 3 * V + d) = ff_split(v);
+  at(s, P, np, 4 * V + d) = ff_split(w);
+  at(s, P, np, 5 * V + d) = ff_split(T);
 }
 
 // FP32-mixed: the binary32 perturbation state and primitives of a binary64 state.
@@ -213,8 +214,8 @@ __global__ void k_prepare(const SolveDev* __restrict__ solves, const TileRef* __
     if (s.mixed) store_mixed(s, o, mixed_cell(s, q));
     if (s.ffaces) {
       const Prims64 pr = prims64(s, q[0], q[1], q[2], q[3], q[4]);
-      store_ff(s, s.QF, o, q, pr.sr, pr.H, pr.u, pr.v, pr.w);
-      store_ff(s, s.QpF, o, q, pr.sr, pr.H, pr.u, pr.v, pr.w);
+      store_ff(s, s.QF, o, q, pr.sr, pr.H, pr.u, pr.v, pr.w, pr.T);
+      store_ff(s, s.QpF, o, q, pr.sr, pr.H, pr.u, pr.v, pr.w, pr.T);
     }
     const bool interior = tc.i >= 0 && tc.i < s.IM && tc.j >= 0 && tc.j < s.JM && tc.k >= 0 && tc.k < s.KM;
     if (interior) {
@@ -1143,6 +1144,32 @@ __device__ __forceinline__ void update_tiles(const SolveDev* __restrict__ solves
         df = fma_(at(s, F0, n5, n * IV + fx) - at(s, F0, n5, n * IV + fo), idx, n > 0 ? dv[n - 1] : 0.0f);
         df = fma_(at(s, F1, n5, n * IV + fy) - at(s, F1, n5, n * IV + fo), idy, df);
         df = fma_(at(s, F2, n5, n * IV + fz) - at(s, F2, n5, n * IV + fo), idz, df);
+      } else if constexpr (FF) {
+        // CBNS_FP64_FF: the same chain in float-float arithmetic, from the
+        // float-float face fluxes and viscous terms (pairs in F's and Tv's
+        // bytes), rounded to binary64 once.
+        const long long n5 = NEQ * IV;
+        auto ld = [&](const double* a, long long n, long long i2) {
+          const float2 v = at(s, reinterpret_cast<const float2*>(a), n, i2);
+          return ff{v.x, v.y};
+        };
+        auto cf = [](float2 v) { return ff{v.x, v.y}; };
+        ff d = (ld(F0, n5, n * IV + fx) - ld(F0, n5, n * IV + fo)) * cf(s.ff_hf[0]);
+        d = ff_fma(ld(F1, n5, n * IV + fy) - ld(F1, n5, n * IV + fo), cf(s.ff_hf[1]), d);
+        d = ff_fma(ld(F2, n5, n * IV + fz) - ld(F2, n5, n * IV + fo), cf(s.ff_hf[2]), d);
+        if (n > 0) {
+          const long long n9 = kViscTerms * RV;
+          const long long vx = visc_term(n, 0) * RV + r, vy = visc_term(n, 1) * RV + r,
+                          vz = visc_term(n, 2) * RV + r;
+          const double* Tv = s.Tv;
+          d = ff_fma(ld(Tv, n9, vx - 2) - ld(Tv, n9, vx + 2), -cf(s.ff_c12[0]), d);
+          d = ff_fma(ld(Tv, n9, vx + 1) - ld(Tv, n9, vx - 1), -cf(s.ff_c23[0]), d);
+          d = ff_fma(ld(Tv, n9, vy - 2 * ry) - ld(Tv, n9, vy + 2 * ry), -cf(s.ff_c12[1]), d);
+          d = ff_fma(ld(Tv, n9, vy + ry) - ld(Tv, n9, vy - ry), -cf(s.ff_c23[1]), d);
+          d = ff_fma(ld(Tv, n9, vz - 2 * rz) - ld(Tv, n9, vz + 2 * rz), -cf(s.ff_c12[2]), d);
+          d = ff_fma(ld(Tv, n9, vz + rz) - ld(Tv, n9, vz - rz), -cf(s.ff_c23[2]), d);
+        }
+        df = ff_to_double(d);
       } else {
         // Inviscid flux differences, then minus the viscous divergence, as one
         // chain of fused multiply-adds with the 1/h-folded weights negated.
@@ -1217,7 +1244,7 @@ __device__ __forceinline__ void update_tiles(const SolveDev* __restrict__ solves
         at(s, b, n8, 5 * V + d) = TT;
         at(s, b, n8, 6 * V + d) = sr;
         at(s, b, n8, 7 * V + d) = HH;
-        if constexpr (FF) store_ff(s, stage == 3 ? s.QF : s.QpF, d, qn, sr, HH, uu, vv, ww);
+        if constexpr (FF) store_ff(s, stage == 3 ? s.QF : s.QpF, d, qn, sr, HH, uu, vv, ww, TT);
       }
     };
     store(o);
@@ -1247,9 +1274,10 @@ __device__ __forceinline__ void update_tiles(const SolveDev* __restrict__ solves
 // 11% faster at 80 registers (24 warps per SM, a few spills) than unconstrained
 // (126 registers); the binary32 one (memory-latency bound) 12% faster at 64
 // (32 warps per SM) than at 80.
-// FF: also the float-float copies of CBNS_FP64_FF solves.
+// FF: CBNS_FP64_FF solves (float-float flux differences and copies); their
+// float-float chain needs more than the binary64 update's 80 registers.
 template <typename R, int STAGE, bool FF>
-__global__ void __maxnreg__(80) k_update(const SolveDev* __restrict__ solves,
+__global__ void __maxnreg__(FF ? 128 : 80) k_update(const SolveDev* __restrict__ solves,
                                          const TileRef* __restrict__ tiles, int ntiles) {
   update_tiles<R, STAGE, FF>(solves, tiles, ntiles, STAGE);
 }
@@ -1377,6 +1405,8 @@ static int grid_for(int ntiles, int max_ctas) {
 // cbns_ff_faces.cu
 void launch_faces_ff(const SolveDev* d, const TileRef* tiles, int ntiles, int stage, int g, int nt,
                      cudaStream_t st, Profiler* pf);
+void launch_viscous_ff(const SolveDev* d, const TileRef* ring, int nring, int g, int nt, cudaStream_t st,
+                       Profiler* pf);
 
 #define CBNS_LAUNCH(pf, id, st, ...) \
   do {                               \
@@ -1480,8 +1510,11 @@ static void stage_ty(const SolveDev* d, const StageTables& T, int stage, const L
     CBNS_LAUNCH(pf, KID_INVISCID_Y, st, (k_inviscid<1, R><<<g, nt, 0, st>>>(d, tiles, ntiles, stage)));
     CBNS_LAUNCH(pf, KID_INVISCID_Z, st, (k_inviscid<2, R><<<g, nt, 0, st>>>(d, tiles, ntiles, stage)));
   }
-  CBNS_LAUNCH(pf, KID_VISCOUS, st,
-              (k_viscous<R><<<grid_for(T.nring, cfg.max_ctas), nt, 0, st>>>(d, T.ring, T.nring)));
+  if (ff)
+    launch_viscous_ff(d, T.ring, T.nring, grid_for(T.nring, cfg.max_ctas), nt, st, pf);
+  else
+    CBNS_LAUNCH(pf, KID_VISCOUS, st,
+                (k_viscous<R><<<grid_for(T.nring, cfg.max_ctas), nt, 0, st>>>(d, T.ring, T.nring)));
   if constexpr (sizeof(R) == 4) {
     CBNS_LAUNCH(pf, KID_UPDATE, st, (k_update_f32<<<g, nt, 0, st>>>(d, tiles, ntiles, stage)));
   } else {
