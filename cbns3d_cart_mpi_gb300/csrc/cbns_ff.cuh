@@ -57,19 +57,17 @@ __device__ __forceinline__ ff operator+(ff a, ff b) {
 }
 __device__ __forceinline__ ff operator-(ff a, ff b) { return a + (-b); }
 
-// DWTimesDW: the exact product of the high parts plus the two cross terms.
+// DWTimesDW: the exact product of the high parts plus the two cross terms.  The
+// pair (p, e) is returned without renormalising: a product has no cancellation,
+// so |e| stays within about one ulp of p (at most ulp(p)/2 from the exact
+// product's error plus two cross terms each below 2^-23 |p|), which every
+// operation here accepts as a float-float operand (the renormalising Fast2Sum
+// would cost three additions per product).
 __device__ __forceinline__ ff operator*(ff a, ff b) {
   const float p = a.hi * b.hi;
   float e = fmaf(a.hi, b.hi, -p);
   e = fmaf(a.lo, b.hi, fmaf(a.hi, b.lo, e));
-  return ff_fast2sum(p, e);
-}
-
-// Float-float times a binary32 number c (DWTimesFP).
-__device__ __forceinline__ ff ff_mul(ff a, float c) {
-  const float p = a.hi * c;
-  const float e = fmaf(a.lo, c, fmaf(a.hi, c, -p));
-  return ff_fast2sum(p, e);
+  return ff{p, e};
 }
 
 // Times a power of two: exact.
@@ -100,10 +98,10 @@ __device__ __forceinline__ ff ff_sqr_add(ff a, ff c) {
   return ff_fast2sum(s.hi, s.lo + (e + c.lo));
 }
 
-__device__ __forceinline__ ff ff_sqr(ff a) {
+__device__ __forceinline__ ff ff_sqr(ff a) {  // unrenormalised, as operator*
   const float p = a.hi * a.hi;
   const float e = fmaf(a.hi + a.hi, a.lo, fmaf(a.hi, a.hi, -p));
-  return ff_fast2sum(p, e);
+  return ff{p, e};
 }
 
 // 1/a for a positive normal float-float a.  y = estimate of 1/a.hi; the residual
