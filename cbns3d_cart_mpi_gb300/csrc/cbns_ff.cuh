@@ -90,6 +90,34 @@ __device__ __forceinline__ ff ff_fma(float c, ff b, ff d) {
   return ff_fast2sum(s.hi, s.lo + (e + d.lo));
 }
 
+// Accumulating forms: the same results without the final Fast2Sum, for a value
+// that is used only as the addend of another float-float operation (whose TwoSum
+// takes any high part exactly and folds the low part into its error term) or is
+// widened to binary64.  A chain of multiply-adds renormalises once, at its end.
+__device__ __forceinline__ ff ff_fma_acc(ff a, ff b, ff c) {
+  const float p = a.hi * b.hi;
+  float e = fmaf(a.hi, b.hi, -p);
+  e = fmaf(a.lo, b.hi, fmaf(a.hi, b.lo, e));
+  const ff s = ff_two_sum(p, c.hi);
+  return ff{s.hi, s.lo + (e + c.lo)};
+}
+__device__ __forceinline__ ff ff_fma_acc(float c, ff b, ff d) {
+  const float p = c * b.hi;
+  const float e = fmaf(c, b.lo, fmaf(c, b.hi, -p));
+  const ff s = ff_two_sum(p, d.hi);
+  return ff{s.hi, s.lo + (e + d.lo)};
+}
+__device__ __forceinline__ ff ff_add_acc(ff a, ff b) {
+  const ff s = ff_two_sum(a.hi, b.hi);
+  return ff{s.hi, s.lo + (a.lo + b.lo)};
+}
+__device__ __forceinline__ ff ff_sqr_add_acc(ff a, ff c) {
+  const float p = a.hi * a.hi;
+  const float e = fmaf(a.hi + a.hi, a.lo, fmaf(a.hi, a.hi, -p));
+  const ff s = ff_two_sum(p, c.hi);
+  return ff{s.hi, s.lo + (e + c.lo)};
+}
+
 // a^2 + c.
 __device__ __forceinline__ ff ff_sqr_add(ff a, ff c) {
   const float p = a.hi * a.hi;

@@ -1147,7 +1147,7 @@ __device__ __forceinline__ void update_tiles(const SolveDev* __restrict__ solves
       } else if constexpr (FF) {
         // CBNS_FP64_FF: the same chain in float-float arithmetic, from the
         // float-float face fluxes and viscous terms (pairs in F's and Tv's
-        // bytes), rounded to binary64 once.
+        // bytes), accumulated without renormalising and rounded to binary64 once.
         const long long n5 = NEQ * IV;
         auto ld = [&](const double* a, long long n, long long i2) {
           const float2 v = at(s, reinterpret_cast<const float2*>(a), n, i2);
@@ -1155,19 +1155,19 @@ __device__ __forceinline__ void update_tiles(const SolveDev* __restrict__ solves
         };
         auto cf = [](float2 v) { return ff{v.x, v.y}; };
         ff d = (ld(F0, n5, n * IV + fx) - ld(F0, n5, n * IV + fo)) * cf(s.ff_hf[0]);
-        d = ff_fma(ld(F1, n5, n * IV + fy) - ld(F1, n5, n * IV + fo), cf(s.ff_hf[1]), d);
-        d = ff_fma(ld(F2, n5, n * IV + fz) - ld(F2, n5, n * IV + fo), cf(s.ff_hf[2]), d);
+        d = ff_fma_acc(ld(F1, n5, n * IV + fy) - ld(F1, n5, n * IV + fo), cf(s.ff_hf[1]), d);
+        d = ff_fma_acc(ld(F2, n5, n * IV + fz) - ld(F2, n5, n * IV + fo), cf(s.ff_hf[2]), d);
         if (n > 0) {
           const long long n9 = kViscTerms * RV;
           const long long vx = visc_term(n, 0) * RV + r, vy = visc_term(n, 1) * RV + r,
                           vz = visc_term(n, 2) * RV + r;
           const double* Tv = s.Tv;
-          d = ff_fma(ld(Tv, n9, vx - 2) - ld(Tv, n9, vx + 2), -cf(s.ff_c12[0]), d);
-          d = ff_fma(ld(Tv, n9, vx + 1) - ld(Tv, n9, vx - 1), -cf(s.ff_c23[0]), d);
-          d = ff_fma(ld(Tv, n9, vy - 2 * ry) - ld(Tv, n9, vy + 2 * ry), -cf(s.ff_c12[1]), d);
-          d = ff_fma(ld(Tv, n9, vy + ry) - ld(Tv, n9, vy - ry), -cf(s.ff_c23[1]), d);
-          d = ff_fma(ld(Tv, n9, vz - 2 * rz) - ld(Tv, n9, vz + 2 * rz), -cf(s.ff_c12[2]), d);
-          d = ff_fma(ld(Tv, n9, vz + rz) - ld(Tv, n9, vz - rz), -cf(s.ff_c23[2]), d);
+          d = ff_fma_acc(ld(Tv, n9, vx - 2) - ld(Tv, n9, vx + 2), -cf(s.ff_c12[0]), d);
+          d = ff_fma_acc(ld(Tv, n9, vx + 1) - ld(Tv, n9, vx - 1), -cf(s.ff_c23[0]), d);
+          d = ff_fma_acc(ld(Tv, n9, vy - 2 * ry) - ld(Tv, n9, vy + 2 * ry), -cf(s.ff_c12[1]), d);
+          d = ff_fma_acc(ld(Tv, n9, vy + ry) - ld(Tv, n9, vy - ry), -cf(s.ff_c23[1]), d);
+          d = ff_fma_acc(ld(Tv, n9, vz - 2 * rz) - ld(Tv, n9, vz + 2 * rz), -cf(s.ff_c12[2]), d);
+          d = ff_fma_acc(ld(Tv, n9, vz + rz) - ld(Tv, n9, vz - rz), -cf(s.ff_c23[2]), d);
         }
         df = ff_to_double(d);
       } else {
