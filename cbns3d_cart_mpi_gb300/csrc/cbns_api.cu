@@ -25,9 +25,9 @@ cudaError_t launch_prims_double(const SolveDev* d, const TileRef* tiles, int nti
 cudaError_t launch_init_tgv(const SolveDev* d, int sidx, const TileRef* tiles, int ntiles, double p_inf,
                             const PerturbMode* modes, int nmodes, cudaStream_t st);
 cudaError_t launch_dt(const SolveDev* d, int nsolves, const TileRef* tiles, int ntiles, double t_end,
-                      bool use_t_end, bool mixed, const LaunchCfg& cfg, cudaStream_t st, Profiler* pf);
+                      bool use_t_end, int precision, const LaunchCfg& cfg, cudaStream_t st, Profiler* pf);
 cudaError_t launch_dt_raw(const SolveDev* d, int sidx, const TileRef* tiles, int ntiles, double* out,
-                          bool mixed, const LaunchCfg& cfg, cudaStream_t st, Profiler* pf);
+                          int precision, const LaunchCfg& cfg, cudaStream_t st, Profiler* pf);
 cudaError_t launch_set_dt(const SolveDev* d, int sidx, double dt, cudaStream_t st);
 cudaError_t launch_reset_ctl(SolveCtl* ctl, double t, double t_end, cudaStream_t st);
 cudaError_t launch_stage(const SolveDev* d, const StageTables& T, int stage, const LaunchCfg& cfg, int precision,
@@ -417,6 +417,12 @@ cbns_status cbns_create(const cbns_params* p, uint32_t IM, uint32_t JM, uint32_t
     s.ff_kappa = split(s.kappa);
     s.ff_C = split(s.C_T_inf);
     s.ff_C1 = split(s.C_T_inf1);
+    s.ff_gM2 = split(s.gM2);
+    s.ff_igM2 = split(1.0 / s.gM2);
+    s.ff_ggam1 = split(c.gamma_gam1_inv);
+    s.ff_Cdt2 = split(c.C_dt_v2);
+    s.ff_sum_ih = split(c.sum_ih);
+    s.ff_sum_ih2 = split(c.sum_ih2);
   }
   h->d_ctl = (SolveCtl*)(A + oCtl);
   s.ctl = h->d_ctl;
@@ -511,8 +517,9 @@ cbns_status cbns_download_prims(cbns_handle* h, double* rho, double* u, double* 
   if (st != CBNS_OK) return st;
   const SolveDev& s = h->desc;
   const size_t bytes = sizeof(double) * (size_t)s.V;
-  // FP32-mixed solves step with binary32 primitives; form the binary64 ones of Q.
-  if (s.mixed) CBNS_CUDA(launch_prims_double(h->d_desc, h->d_tiles_pad, h->n_pad, h->stream));
+  // FP32-mixed solves step with binary32 primitives and CBNS_FP64_FF solves with
+  // float-float ones; form the binary64 ones of Q.
+  if (s.mixed || s.ffaces) CBNS_CUDA(launch_prims_double(h->d_desc, h->d_tiles_pad, h->n_pad, h->stream));
   double* dst[6] = {rho, u, v, w, p, T};
   double* src[6] = {s.pd.rho, s.pd.u, s.pd.v, s.pd.w, s.pd.p, s.pd.T};
   for (int a = 0; a < 6; ++a)
@@ -525,7 +532,7 @@ cbns_status cbns_calc_dt(cbns_handle* h, double* dt) {
   cbns_status st = check_handle(h, "cbns_calc_dt");
   if (st != CBNS_OK) return st;
   if (!dt) return fail(CBNS_ERR_INVALID_ARG, "cbns_calc_dt: null output");
-  CBNS_CUDA(launch_dt_raw(h->d_desc, 0, h->d_tiles_int, h->n_int, h->d_out, h->desc.mixed != 0, LaunchCfg{},
+  CBNS_CUDA(launch_dt_raw(h->d_desc, 0, h->d_tiles_int, h->n_int, h->d_out, h->precision, LaunchCfg{},
                           h->stream, h->pf()));
   CBNS_CUDA(cudaMemcpyAsync(h->h_out, h->d_out, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   CBNS_CUDA(cudaStreamSynchronize(h->stream));
@@ -550,7 +557,7 @@ cbns_status cbns_stage(cbns_handle* h, double dt, int stage) {
 }
 
 static cbns_status enqueue_step(cbns_handle* h, double t_end, bool use_t_end) {
-  CBNS_CUDA(launch_dt(h->d_desc, 1, h->d_tiles_int, h->n_int, t_end, use_t_end, h->desc.mixed != 0, LaunchCfg{},
+  CBNS_CUDA(launch_dt(h->d_desc, 1, h->d_tiles_int, h->n_int, t_end, use_t_end, h->precision, LaunchCfg{},
                       h->stream, h->pf()));
   for (int s = 1; s <= 3; ++s) {
     cbns_status st = enqueue_stage(h, s);
@@ -813,7 +820,7 @@ int rows_index(int rows) { return rows == 2 ? 0 : (rows == 8 ? 2 : 1); }
 static cbns_status batch_enqueue_step(cbns_batch* b) {
   const int ri = rows_index(b->cfg.tile_rows);
   const int n = (int)b->handles.size();
-  CBNS_CUDA(launch_dt(b->d_descs, n, b->d_int[ri], b->n_int[ri], 0.0, false, b->mixed, b->cfg, b->stream, nullptr));
+  CBNS_CUDA(launch_dt(b->d_descs, n, b->d_int[ri], b->n_int[ri], 0.0, false, b->precision, b->cfg, b->stream, nullptr));
   const StageTables T{b->d_int[ri], b->n_int[ri], b->d_ring[ri], b->n_ring[ri]};
   for (int st = 1; st <= 3; ++st)
     CBNS_CUDA(launch_stage(b->d_descs, T, st, b->cfg, b->precision, b->stream, nullptr));

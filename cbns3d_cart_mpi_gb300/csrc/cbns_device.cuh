@@ -154,6 +154,9 @@ struct SolveDev {
   float2 ff_gam1, ff_gamma, ff_hgam1;
   float2 ff_hf[3], ff_c12[3], ff_c23[3];
   float2 ff_Re_inv, ff_kappa, ff_C, ff_C1;
+  // the primitives and time step of CBNS_FP64_FF: gamma M^2, 1/(gamma M^2),
+  // gamma/(gamma - 1), 2 C_dt_v, sum 1/h, sum 1/h^2
+  float2 ff_gM2, ff_igM2, ff_ggam1, ff_Cdt2, ff_sum_ih, ff_sum_ih2;
 };
 
 // Blocks of SolveDev::PF: sqrt(rho), H, u, v, w, T.

@@ -117,6 +117,28 @@ __device__ __forceinline__ void store_ff(const SolveDev& s, float2* QFo, long lo
   at(s, P, np, 5 * V + d) = ff_split(T);
 }
 
+// CBNS_FP64_FF: the primitives of a state in float-float (prims64's formulas),
+// from the state's float-float split.
+struct PrimsFF {
+  ff u, v, w, p, T, sr, H;
+};
+
+__device__ __forceinline__ PrimsFF prims_ff(const SolveDev& s, const ff (&q)[NEQ]) {
+  auto cf = [](float2 v) { return ff{v.x, v.y}; };
+  const ff rs = ff_rsqrt(q[0]);
+  const ff ir = ff_sqr(rs);
+  PrimsFF r;
+  r.u = q[1] * ir;
+  r.v = q[2] * ir;
+  r.w = q[3] * ir;
+  const ff q2 = ff_sqr_add(r.w, ff_sqr_add_acc(r.v, ff_sqr(r.u)));
+  r.p = cf(s.ff_gam1) * (q[4] - ff_scale(q[0] * q2, 0.5f));
+  r.T = (cf(s.ff_gM2) * r.p) * ir;
+  r.sr = q[0] * rs;
+  r.H = ff_fma(cf(s.ff_ggam1) * r.p, ir, ff_scale(q2, 0.5f));
+  return r;
+}
+
 // FP32-mixed: the binary32 perturbation state and primitives of a binary64 state.
 // rho' = rho - rho_ref and E' = E - E_ref are formed in binary64 before rounding,
 // so binary32 keeps 24 bits of the fluctuations; p' = p - p_ref and
@@ -324,6 +346,29 @@ __device__ __forceinline__ R dt_speed(const SolveDev& s, long long o) {
   return (fabs(uu) + fabs(vv) + fabs(ww)) + fma_(c, C.sum_ih, fv * C.sum_ih2);
 }
 
+// CBNS_FP64_FF: the same speed in float-float, from the float-float primitives
+// (rho = sqrt(rho)^2, p = rho T / (gamma M^2)) and the binary64 mu, widened once.
+__device__ __forceinline__ double dt_speed_ff(const SolveDev& s, long long o) {
+  const long long V = s.V, np = kFFPrims * V;
+  auto ld = [&](int b) {
+    const float2 v = at(s, s.PF, np, b * V + o);
+    return ff{v.x, v.y};
+  };
+  auto cf = [](float2 v) { return ff{v.x, v.y}; };
+  const ff sr = ld(0), uu = ld(2), vv = ld(3), ww = ld(4), TT = ld(5);
+  const float2 m2 = ff_split(at(s, s.pd.mu, V, o));
+  const ff mu{m2.x, m2.y};
+  const ff rr = ff_sqr(sr);
+  const ff gp = cf(s.ff_gamma) * ((rr * TT) * cf(s.ff_igM2));
+  const ff z = ff_rsqrt(gp * rr);
+  const ff c = gp * z;
+  const ff q2 = ff_sqr_add(ww, ff_sqr_add_acc(vv, ff_sqr(uu)));
+  const ff q = q2.hi > 0.0f ? q2 * ff_rsqrt(q2) : ff{0.0f, 0.0f};
+  const ff fv = ((cf(s.ff_Cdt2) * mu) * q) * z;
+  const ff a = (ff_abs(uu) + ff_abs(vv)) + ff_abs(ww);
+  return ff_to_double(a + ff_fma(c, cf(s.ff_sum_ih), fv * cf(s.ff_sum_ih2)));
+}
+
 // Each CTA walks its tiles (grid stride) keeping a running per-thread maximum,
 // and folds it into the solve's control block (one block reduction and one
 // atomicMax) only when the next tile belongs to another solve or the walk ends.
@@ -331,7 +376,7 @@ __device__ __forceinline__ R dt_speed(const SolveDev& s, long long o) {
 // about one atomic per CTA instead of one per tile.  The running maximum stays
 // in the compute type and is widened once per fold (exact and monotonic, so
 // the same maximum); whether the solve has finished is tested once per solve.
-template <typename R>
+template <typename R, bool FF>
 __global__ void __launch_bounds__(kMaxThreads) k_dt_reduce(const SolveDev* __restrict__ solves,
                                                            const TileRef* __restrict__ tiles, int ntiles,
                                                            double t_end, int use_t_end, int skip_finished) {
@@ -350,7 +395,11 @@ __global__ void __launch_bounds__(kMaxThreads) k_dt_reduce(const SolveDev* __res
       live_solve = tc.s;
     }
     if (live && tc.i < s.IM && tc.j < s.JM) {
-      const R sum = dt_speed<R>(s, pad_off(s, tc.i, tc.j, tc.k));
+      R sum;
+      if constexpr (FF)
+        sum = dt_speed_ff(s, pad_off(s, tc.i, tc.j, tc.k));
+      else
+        sum = dt_speed<R>(s, pad_off(s, tc.i, tc.j, tc.k));
       if (sum > run) run = sum;  // a NaN is skipped, as the reference's ternary does
     }
     const int tn = t + (int)gridDim.x;
@@ -1215,9 +1264,22 @@ __device__ __forceinline__ void update_tiles(const SolveDev* __restrict__ solves
     // Primitives of the new state (once), then the cell and its ghost images.
     double uu = 0, vv = 0, ww = 0, pp = 0, TT = 0, sr = 0, HH = 0;
     MixedCell mc;
+    ff fq[NEQ];
+    PrimsFF pf;
     if constexpr (MIXED) {
       mc = mixed_cell(s, qn);
       if (!(mc.rho > 0.0f) || !(s.cf.p_ref + mc.p > 0.0f)) atomicOr(&ctl->status, kStatusNonphysical);
+    } else if constexpr (FF) {
+      // CBNS_FP64_FF: the float-float split of the state and its float-float
+      // primitives, the only copies the float-float kernels read (binary64
+      // primitives are formed on demand for output)
+#pragma unroll
+      for (int n = 0; n < NEQ; ++n) {
+        const float2 t2 = ff_split(qn[n]);
+        fq[n] = ff{t2.x, t2.y};
+      }
+      pf = prims_ff(s, fq);
+      if (!(qn[0] > 0.0) || !(pf.p.hi > 0.0f)) atomicOr(&ctl->status, kStatusNonphysical);
     } else {
       const Prims64 q = prims64(s, qn[0], qn[1], qn[2], qn[3], qn[4]);
       uu = q.u, vv = q.v, ww = q.w, pp = q.p, TT = q.T, sr = q.sr, HH = q.H;
@@ -1232,6 +1294,14 @@ __device__ __forceinline__ void update_tiles(const SolveDev* __restrict__ solves
       for (int n = 0; n < NEQ; ++n) at(s, out, NEQ * V, n * V + d) = qn[n];
       if constexpr (MIXED) {
         store_mixed(s, d, mc);
+      } else if constexpr (FF) {
+        const long long n5 = NEQ * V, np = kFFPrims * V;
+        float2* QFo = stage == 3 ? s.QF : s.QpF;
+#pragma unroll
+        for (int n = 0; n < NEQ; ++n) at(s, QFo, n5, n * V + d) = make_float2(fq[n].hi, fq[n].lo);
+        const ff pv[kFFPrims] = {pf.sr, pf.H, pf.u, pf.v, pf.w, pf.T};
+#pragma unroll
+        for (int b2 = 0; b2 < kFFPrims; ++b2) at(s, s.PF, np, b2 * V + d) = make_float2(pv[b2].hi, pv[b2].lo);
       } else {
         // the PrimSet arrays are consecutive blocks of V values from pd.rho
         double* b = s.pd.rho;
@@ -1244,7 +1314,6 @@ __device__ __forceinline__ void update_tiles(const SolveDev* __restrict__ solves
         at(s, b, n8, 5 * V + d) = TT;
         at(s, b, n8, 6 * V + d) = sr;
         at(s, b, n8, 7 * V + d) = HH;
-        if constexpr (FF) store_ff(s, stage == 3 ? s.QF : s.QpF, d, qn, sr, HH, uu, vv, ww, TT);
       }
     };
     store(o);
@@ -1452,31 +1521,35 @@ cudaError_t launch_prims_double(const SolveDev* d, const TileRef* tiles, int nti
 // keep the atomics on the control block few.
 constexpr int kDtReduceCtas = 152 * 8;
 
-template <typename R>
+template <typename R, bool FF>
 static void dt_reduce_ty(const SolveDev* d, const TileRef* tiles, int ntiles, double t_end, int use_t_end, int skip,
                          const LaunchCfg& cfg, cudaStream_t st, Profiler* pf) {
   const int g = grid_for(ntiles, (cfg.max_ctas > 0 && cfg.max_ctas < kDtReduceCtas) ? cfg.max_ctas : kDtReduceCtas);
   CBNS_LAUNCH(pf, KID_DT_REDUCE, st,
-              (k_dt_reduce<R><<<g, 32 * cfg.tile_rows, 0, st>>>(d, tiles, ntiles, t_end, use_t_end, skip)));
+              (k_dt_reduce<R, FF><<<g, 32 * cfg.tile_rows, 0, st>>>(d, tiles, ntiles, t_end, use_t_end, skip)));
+}
+
+static void dt_reduce_prec(const SolveDev* d, const TileRef* tiles, int ntiles, double t_end, int use_t_end,
+                           int skip, int precision, const LaunchCfg& cfg, cudaStream_t st, Profiler* pf) {
+  if (precision == CBNS_FP32_MIXED)
+    dt_reduce_ty<float, false>(d, tiles, ntiles, t_end, use_t_end, skip, cfg, st, pf);
+  else if (precision == CBNS_FP64_FF)
+    dt_reduce_ty<double, true>(d, tiles, ntiles, t_end, use_t_end, skip, cfg, st, pf);
+  else
+    dt_reduce_ty<double, false>(d, tiles, ntiles, t_end, use_t_end, skip, cfg, st, pf);
 }
 
 cudaError_t launch_dt(const SolveDev* d, int nsolves, const TileRef* tiles, int ntiles, double t_end,
-                      bool use_t_end, bool mixed, const LaunchCfg& cfg, cudaStream_t st, Profiler* pf) {
-  if (ntiles > 0) {
-    if (mixed) dt_reduce_ty<float>(d, tiles, ntiles, t_end, use_t_end ? 1 : 0, 1, cfg, st, pf);
-    else dt_reduce_ty<double>(d, tiles, ntiles, t_end, use_t_end ? 1 : 0, 1, cfg, st, pf);
-  }
+                      bool use_t_end, int precision, const LaunchCfg& cfg, cudaStream_t st, Profiler* pf) {
+  if (ntiles > 0) dt_reduce_prec(d, tiles, ntiles, t_end, use_t_end ? 1 : 0, 1, precision, cfg, st, pf);
   CBNS_LAUNCH(pf, KID_DT_FINALIZE, st,
               (k_dt_finalize<<<(nsolves + 127) / 128, 128, 0, st>>>(d, nsolves, t_end, use_t_end ? 1 : 0)));
   return cudaGetLastError();
 }
 
 cudaError_t launch_dt_raw(const SolveDev* d, int sidx, const TileRef* tiles, int ntiles, double* out,
-                          bool mixed, const LaunchCfg& cfg, cudaStream_t st, Profiler* pf) {
-  if (ntiles > 0) {
-    if (mixed) dt_reduce_ty<float>(d, tiles, ntiles, 0.0, 0, 0, cfg, st, pf);
-    else dt_reduce_ty<double>(d, tiles, ntiles, 0.0, 0, 0, cfg, st, pf);
-  }
+                          int precision, const LaunchCfg& cfg, cudaStream_t st, Profiler* pf) {
+  if (ntiles > 0) dt_reduce_prec(d, tiles, ntiles, 0.0, 0, 0, precision, cfg, st, pf);
   CBNS_LAUNCH(pf, KID_DT_FINALIZE, st, (k_dt_raw<<<1, 1, 0, st>>>(d, sidx, out)));
   return cudaGetLastError();
 }

@@ -77,7 +77,8 @@ def main():
     ap.add_argument("--solves", type=int, default=64)
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--seed", type=int, default=0)
-    ap.add_argument("--precision", default="both", choices=["fp64", "fp32_mixed", "both"])
+    ap.add_argument("--precision", default="both",
+                    help="fp64, fp32_mixed, fp64_ff, a comma-separated list, or both (fp64,fp32_mixed)")
     ap.add_argument("--no-tune", action="store_true")
     args = ap.parse_args()
     cases = draw(args.solves, args.seed)
@@ -87,20 +88,23 @@ def main():
            "cells": cells, "grid_counts": {str(g): sum(c["N"] == g for c in cases) for g in GRIDS}}
     states = {}
     t0 = time.perf_counter()
-    for prec in (["fp64", "fp32_mixed"] if args.precision == "both" else [args.precision]):
+    precs = ["fp64", "fp32_mixed"] if args.precision == "both" else args.precision.split(",")
+    for prec in precs:
         res, b, solvers = run_batch(cases, prec, args.steps, tune=not args.no_tune)
         out[prec] = res
         states[prec] = [s.download_Q() for s in solvers]
         b.close()
         for s in solvers:
             s.close()
-    if len(states) == 2:
-        errs = np.array([rel_linf(m, d) for m, d in zip(states["fp32_mixed"], states["fp64"])])
-        out["fp32_mixed_vs_fp64_rel_linf_max"] = dict(zip(["rho", "rho*u", "rho*v", "rho*w", "E"],
-                                                          errs.max(axis=0).tolist()))
-        out["fp32_mixed_vs_fp64_rel_linf_median"] = dict(zip(["rho", "rho*u", "rho*v", "rho*w", "E"],
-                                                             np.median(errs, axis=0).tolist()))
-        out["fp32_mixed_speedup"] = out["fp32_mixed"]["cell_rk3_steps_per_s"] / out["fp64"]["cell_rk3_steps_per_s"]
+    for prec in states:
+        if prec == "fp64" or "fp64" not in states:
+            continue
+        errs = np.array([rel_linf(m, d) for m, d in zip(states[prec], states["fp64"])])
+        out[prec + "_vs_fp64_rel_linf_max"] = dict(zip(["rho", "rho*u", "rho*v", "rho*w", "E"],
+                                                       errs.max(axis=0).tolist()))
+        out[prec + "_vs_fp64_rel_linf_median"] = dict(zip(["rho", "rho*u", "rho*v", "rho*w", "E"],
+                                                          np.median(errs, axis=0).tolist()))
+        out[prec + "_speedup"] = out[prec]["cell_rk3_steps_per_s"] / out["fp64"]["cell_rk3_steps_per_s"]
     out["wall_s"] = time.perf_counter() - t0
     print(json.dumps(out))
 

@@ -73,7 +73,7 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--rates", default="0.25,0.5,1.0")
     ap.add_argument("--requests", type=int, default=24)
-    ap.add_argument("--precision", default="fp32_mixed", choices=["fp64", "fp32_mixed"])
+    ap.add_argument("--precision", default="fp32_mixed", choices=["fp64", "fp32_mixed", "fp64_ff"])
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--t-end", type=float, default=1.0)
     ap.add_argument("--steps-per-round", type=int, default=20)

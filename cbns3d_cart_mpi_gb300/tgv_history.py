@@ -1,15 +1,19 @@
-"""Taylor-Green vortex history: binary64 and FP32-mixed side by side.
+"""Taylor-Green vortex history: precisions side by side.
 
   python -m cbns3d_cart_mpi_gb300.tgv_history [--N 256] [--times 0.5,1,2] [--every 10] [--out FILE]
+      [--precisions fp64,fp32_mixed] [--history-vs FILE]
 
 Runs the reference's Taylor-Green case (Re 1600, Ma 0.1, CFL 0.5, its mesh and
-initial condition) on one GPU in binary64 and in FP32-mixed, each as replayed
-step graphs, recording kinetic energy and enstrophy every `every` steps.  Each
-listed time is an end time the solve clips its last step to (the reference's
-t_end rule), so both precisions reach exactly the same times; there the two
-states are compared (relative L-inf and L2 per conserved field, FP32-mixed
-against binary64).  Writes a JSON file with the histories, the errors and the
-wall time of each run.
+initial condition) on one GPU in each precision (default binary64 and
+FP32-mixed), each as replayed step graphs, recording kinetic energy and
+enstrophy every `every` steps.  Each listed time is an end time the solve clips
+its last step to (the reference's t_end rule), so all precisions reach exactly
+the same times; there each state is compared with the binary64 one when
+binary64 is among the runs (relative L-inf and L2 per conserved field).
+--history-vs names the text history of an earlier binary64 run (columns: step,
+t, KE, enstrophy, ...): each run's KE and enstrophy are compared with it at the
+same steps.  Writes a JSON file with the histories, the errors and the wall
+time of each run.
 """
 import argparse
 import json
@@ -68,27 +72,46 @@ def main():
     ap.add_argument("--times", default="0.5,1,2")
     ap.add_argument("--every", type=int, default=10)
     ap.add_argument("--out", default="tgv_history.json")
+    ap.add_argument("--precisions", default="fp64,fp32_mixed")
+    ap.add_argument("--history-vs", default=None)
     args = ap.parse_args()
+    precs = args.precisions.split(",")
     times = [float(x) for x in args.times.split(",")]
     Q0 = initial_condition(tgv_params(args.N))
     out = {"case": "TGV %d^3, Re 1600, Ma 0.1, CFL 0.5, reference mesh and initial condition" % args.N,
            "times": times, "every": args.every}
     states = {}
-    for prec in ("fp64", "fp32_mixed"):
+    for prec in precs:
         t0 = time.perf_counter()
         hist, st, steps, gpu_ms = run(args.N, prec, times, args.every, Q0)
         out[prec] = {"steps": steps, "gpu_ms": gpu_ms, "wall_s": time.perf_counter() - t0,
                      "cell_rk3_steps_per_s": args.N ** 3 * steps / (gpu_ms * 1e-3),
                      "history": [list(h) for h in hist]}
         states[prec] = st
-    out["fp32_mixed_vs_fp64"] = {}
-    for te in times:
-        linf, l2 = errors(states["fp32_mixed"][te], states["fp64"][te])
-        out["fp32_mixed_vs_fp64"][str(te)] = {"rel_linf": linf, "rel_l2": l2}
+    for prec in precs:
+        if prec == "fp64" or "fp64" not in states:
+            continue
+        out[prec + "_vs_fp64"] = {}
+        for te in times:
+            linf, l2 = errors(states[prec][te], states["fp64"][te])
+            out[prec + "_vs_fp64"][str(te)] = {"rel_linf": linf, "rel_l2": l2}
+    if args.history_vs:
+        ref = {}
+        with open(args.history_vs) as f:
+            for line in f:
+                if line.strip() and not line.startswith("#"):
+                    c = line.split()
+                    ref[int(c[0])] = (float(c[2]), float(c[3]))
+        for prec in precs:
+            common = [h for h in out[prec]["history"] if h[0] in ref]
+            out[prec + "_vs_history"] = {
+                "file": args.history_vs, "points": len(common),
+                "ke_rel_max": max(abs(h[2] - ref[h[0]][0]) / abs(ref[h[0]][0]) for h in common),
+                "enstrophy_rel_max": max(abs(h[3] - ref[h[0]][1]) / abs(ref[h[0]][1]) for h in common)}
     with open(args.out, "w") as f:
         json.dump(out, f)
-    print(json.dumps({k: v for k, v in out.items() if k not in ("fp64", "fp32_mixed")}))
-    for prec in ("fp64", "fp32_mixed"):
+    print(json.dumps({k: v for k, v in out.items() if k not in precs}))
+    for prec in precs:
         print(prec, {k: v for k, v in out[prec].items() if k != "history"})
 
 
