@@ -102,8 +102,22 @@ int main(int argc, char** argv) {
   }
   const uint32_t IM = sp.IM, JM = sp.JM, KM = sp.KM;
   std::string ckpt = std::string(sp.checkpoint_fname) + "000.dat";
+  // The command line stays the reference's; the environment variable
+  // CBNS_PRECISION picks the arithmetic: fp64 (default), fp64_ff or fp32_mixed.
+  int precision = CBNS_FP64;
+  if (const char* pe = std::getenv("CBNS_PRECISION")) {
+    const std::string ps(pe);
+    if (ps == "fp64_ff") {
+      precision = CBNS_FP64_FF;
+    } else if (ps == "fp32_mixed") {
+      precision = CBNS_FP32_MIXED;
+    } else if (ps != "fp64") {
+      std::cerr << "Error: CBNS_PRECISION must be fp64, fp64_ff or fp32_mixed\n";
+      return 1;
+    }
+  }
   cbns_handle* h = nullptr;
-  if ((st = cbns_create(&sp, IM, JM, KM, CBNS_FP64, &h)) != CBNS_OK) {
+  if ((st = cbns_create(&sp, IM, JM, KM, precision, &h)) != CBNS_OK) {
     std::cerr << "cbns_create failed: " << cbns_last_error() << "\n";
     return 1;
   }

@@ -85,3 +85,48 @@ def test_driver_rejects_more_than_one_process(tmp_path):
     write_input_txt(tgv_params(8), str(tmp_path / "input.txt"))
     r = subprocess.run([build.DRIVER, "2", "1", "1"], cwd=tmp_path, capture_output=True, text=True, timeout=60)
     assert r.returncode != 0 and "dimX * dimY * dimZ" in r.stderr
+
+
+def test_driver_float_float_precision(tmp_path):
+    """CBNS_PRECISION=fp64_ff runs the reference's loop with float-float
+    arithmetic: the driver's checkpoint is bitwise the library's fp64_ff state
+    after the same steps, and within the binary64 parity bar of binary64's."""
+    import os
+
+    from cbns3d_cart_mpi_gb300 import build
+    from cbns3d_cart_mpi_gb300.params import write_input_txt
+    from cbns3d_cart_mpi_gb300.solver import Solver, initial_condition, read_bin
+
+    p = tgv_params(12, JM=8, KM=10, t_end=0.06, nstep_max=100)
+    p.checkpoint_freq = 3
+    p.num_output = 1
+    write_input_txt(p, str(tmp_path / "input.txt"))
+    env = dict(os.environ, CBNS_PRECISION="fp64_ff")
+    r = subprocess.run([build.DRIVER, "1", "1", "1"], cwd=tmp_path, capture_output=True, text=True, timeout=120,
+                       env=env)
+    assert r.returncode == 0, r.stderr
+    t_ck, Qck = read_bin(str(tmp_path / "checkpoint000.dat"), 12, 8, 10)
+    states = {}
+    for prec in ("fp64_ff", "fp64"):
+        s = Solver(p, precision=prec)
+        s.upload_Q(initial_condition(p), 0.0)
+        for _ in range(6):
+            s.step()
+        states[prec] = s.download_Q()
+        s.close()
+    assert np.array_equal(Qck, states["fp64_ff"])
+    a = Qck[4:-4, 4:-4, 4:-4].reshape(-1, 5)
+    b = states["fp64"][4:-4, 4:-4, 4:-4].reshape(-1, 5)
+    assert (np.abs(a - b).max(axis=0) / np.abs(b).max(axis=0) <= 1e-11).all()
+
+
+def test_driver_rejects_an_unknown_precision(tmp_path):
+    import os
+
+    from cbns3d_cart_mpi_gb300 import build
+    from cbns3d_cart_mpi_gb300.params import write_input_txt
+    write_input_txt(tgv_params(8), str(tmp_path / "input.txt"))
+    env = dict(os.environ, CBNS_PRECISION="fp16")
+    r = subprocess.run([build.DRIVER, "1", "1", "1"], cwd=tmp_path, capture_output=True, text=True, timeout=60,
+                       env=env)
+    assert r.returncode != 0 and "CBNS_PRECISION" in r.stderr
