@@ -316,13 +316,21 @@ __global__ void __launch_bounds__(256) k_viscous_ff(const SolveDev* __restrict__
 void launch_faces_ff(const SolveDev* d, const TileRef* tiles, int ntiles, int stage, int g, int nt,
                      cudaStream_t st, Profiler* pf) {
   // shared memory for kFaceSlots float-float slots per thread, up to 256 threads
+  // (above the 48 KB default): the kernels' attribute, set once per device
   constexpr int kMaxBytes = 256 * kFaceSlots * 2 * (int)sizeof(float);
-  static std::once_flag once;
-  std::call_once(once, [] {
-    cudaFuncSetAttribute(k_inviscid_ff<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxBytes);
-    cudaFuncSetAttribute(k_inviscid_ff<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxBytes);
-    cudaFuncSetAttribute(k_inviscid_ff<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxBytes);
-  });
+  constexpr int kMaxDevices = 64;
+  static std::mutex mu;
+  static bool opted[kMaxDevices] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) == cudaSuccess && dev >= 0 && dev < kMaxDevices) {
+    std::lock_guard<std::mutex> lock(mu);
+    if (!opted[dev]) {
+      cudaFuncSetAttribute(k_inviscid_ff<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxBytes);
+      cudaFuncSetAttribute(k_inviscid_ff<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxBytes);
+      cudaFuncSetAttribute(k_inviscid_ff<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxBytes);
+      opted[dev] = true;
+    }
+  }
   const size_t smem = (size_t)nt * kFaceSlots * 2 * sizeof(float);
   auto run = [&](int id, auto kern) {
     if (pf) pf->before(id, st);
