@@ -223,9 +223,11 @@ __device__ __forceinline__ void face_ff(const SolveDev& s, const float2* __restr
 
 // One face per thread over the interior tiles (the binary64 k_inviscid's walk).
 // The stage input is Q's float-float copy in stage 1 and Q_p's in stages 2-3.
-// Dynamic shared memory: kFaceSlots float-float slots per thread.
+// Dynamic shared memory: kFaceSlots float-float slots per thread.  Register cap
+// 80 (no spills): six 128-thread CTAs per SM, where 128 registers fit four;
+// measured 0.5-3% faster, the results bitwise the same.
 template <int D>
-__global__ void __maxnreg__(128) k_inviscid_ff(const SolveDev* __restrict__ solves,
+__global__ void __maxnreg__(80) k_inviscid_ff(const SolveDev* __restrict__ solves,
                                                const TileRef* __restrict__ tiles, int ntiles, int stage) {
   extern __shared__ float face_slots[];
   const Slots sl{face_slots, (int)blockDim.x, (int)threadIdx.x};
@@ -325,9 +327,13 @@ void launch_faces_ff(const SolveDev* d, const TileRef* tiles, int ntiles, int st
   if (cudaGetDevice(&dev) == cudaSuccess && dev >= 0 && dev < kMaxDevices) {
     std::lock_guard<std::mutex> lock(mu);
     if (!opted[dev]) {
-      cudaFuncSetAttribute(k_inviscid_ff<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxBytes);
-      cudaFuncSetAttribute(k_inviscid_ff<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxBytes);
-      cudaFuncSetAttribute(k_inviscid_ff<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxBytes);
+      // and the largest shared-memory carveout, so that the slots of as many
+      // CTAs as the registers allow fit on an SM
+      for (const void* k : {(const void*)k_inviscid_ff<0>, (const void*)k_inviscid_ff<1>,
+                             (const void*)k_inviscid_ff<2>}) {
+        cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxBytes);
+        cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+      }
       opted[dev] = true;
     }
   }
