@@ -121,8 +121,8 @@ size_t ring_tile_count(long long ex, long long ey, long long ez, bool mixed) {
 
 // Byte offsets of everything a solve's arena holds (see cbns_create).
 struct ArenaLayout {
-  size_t oQ, oQp, oStage, oPrim, oF[3], oTv, oFf[3], oTv32, oU32, oP32, oQF, oQpF, oPF, oCtl, oDesc, oTi, oTr, oTp,
-      oPart, oOut, total;
+  size_t oQ, oQp, oStage, oPrim, oF[3], oTv, oFf[3], oTv32, oU32, oP32, oQF, oQpF, oPF, oFFa[3], oTvG, oCtl, oDesc,
+      oTi, oTr, oTp, oPart, oOut, total;
 };
 
 ArenaLayout arena_layout(const SolveDev& s, int precision, size_t n_int, size_t n_ring, size_t n_pad, int nparts) {
@@ -139,15 +139,16 @@ ArenaLayout arena_layout(const SolveDev& s, int precision, size_t n_int, size_t 
   L.oQp = take(NEQ * dV);
   L.oStage = take(NEQ * dV);
   L.oPrim = take(9 * dV);
-  if (!mixed) {
+  if (precision == CBNS_FP64_FF) {
+    const size_t f2V = sizeof(float2) * (size_t)s.V;
+    L.oQF = take(NEQ * f2V);
+    L.oQpF = take(NEQ * f2V);
+    L.oPF = take(kFFPrims * f2V);
+    for (int d = 0; d < 3; ++d) L.oFFa[d] = take(sizeof(float4) * 3 * (size_t)s.IV);
+    L.oTvG = take(sizeof(float4) * 6 * (size_t)s.RV);
+  } else if (!mixed) {
     for (int d = 0; d < 3; ++d) L.oF[d] = take(sizeof(double) * NEQ * (size_t)s.IV);
     L.oTv = take(sizeof(double) * kViscTerms * (size_t)s.RV);
-    if (precision == CBNS_FP64_FF) {
-      const size_t f2V = sizeof(float2) * (size_t)s.V;
-      L.oQF = take(NEQ * f2V);
-      L.oQpF = take(NEQ * f2V);
-      L.oPF = take(kFFPrims * f2V);
-    }
   } else {
     L.oU32 = take(NEQ * fV);  // U4 (4 values per cell), then UE
     L.oP32 = take(9 * fV);    // PA and PB (4 values per cell each), then mu
@@ -342,21 +343,27 @@ cbns_status cbns_create(const cbns_params* p, uint32_t IM, uint32_t JM, uint32_t
   s.pd = PrimSet<double>{prim + 0 * s.V, prim + 1 * s.V, prim + 2 * s.V, prim + 3 * s.V, prim + 4 * s.V,
                          prim + 5 * s.V, prim + 6 * s.V, prim + 7 * s.V, prim + 8 * s.V};
   if (!mixed) {
+    s.ffaces = precision == CBNS_FP64_FF ? 1 : 0;
     for (int d = 0; d < 3; ++d) {
-      s.F[d] = (double*)(A + oF[d]);
+      s.F[d] = s.ffaces ? nullptr : (double*)(A + oF[d]);
+      s.FFa[d] = s.ffaces ? (float4*)(A + L.oFFa[d]) : nullptr;
       s.Ff[d] = nullptr;
     }
-    s.Tv = (double*)(A + L.oTv);
+    s.Tv = s.ffaces ? nullptr : (double*)(A + L.oTv);
+    s.TvG = s.ffaces ? (float4*)(A + L.oTvG) : nullptr;
     s.Tvg = nullptr;
     s.U4 = nullptr;
     s.UE = nullptr;
     s.PA = s.PB = nullptr;
     s.muf = nullptr;
-    s.ffaces = precision == CBNS_FP64_FF ? 1 : 0;
     s.QF = s.ffaces ? (float2*)(A + L.oQF) : nullptr;
     s.QpF = s.ffaces ? (float2*)(A + L.oQpF) : nullptr;
     s.PF = s.ffaces ? (float2*)(A + L.oPF) : nullptr;
   } else {
+    s.ffaces = 0;
+    for (int d = 0; d < 3; ++d) s.FFa[d] = nullptr;
+    s.TvG = nullptr;
+    s.QF = s.QpF = s.PF = nullptr;
     s.U4 = (float4*)(A + oU32);
     s.UE = (float*)(s.U4 + s.V);
     s.PA = (float4*)(A + oP32);

@@ -157,6 +157,15 @@ struct SolveDev {
   // the primitives and time step of CBNS_FP64_FF: gamma M^2, 1/(gamma M^2),
   // gamma/(gamma - 1), 2 C_dt_v, sum 1/h, sum 1/h^2
   float2 ff_gM2, ff_igM2, ff_ggam1, ff_Cdt2, ff_sum_ih, ff_sum_ih2;
+  // CBNS_FP64_FF face fluxes and viscous terms, packed so the update reads them
+  // with 16-byte loads (F and Tv are unused in this mode):
+  //   FFa[d]: per interior cell, the five float-float fluxes of its face normal
+  //   to d as three float4 {f0, f1}, {f2, f3}, {f4, 0};
+  //   TvG: per direction d and ring point, the four terms differenced along d
+  //   (visc_term(1..4, d)) as two float4 {t1, t2}, {t3, t4}: element
+  //   (d RV + r) 2 + h.
+  float4* FFa[3];
+  float4* TvG;
 };
 
 // Blocks of SolveDev::PF: sqrt(rho), H, u, v, w, T.

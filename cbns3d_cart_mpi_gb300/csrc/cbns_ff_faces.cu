@@ -241,9 +241,11 @@ __global__ void __maxnreg__(80) k_inviscid_ff(const SolveDev* __restrict__ solve
     ff f[NEQ];
     face_ff<D>(s, U, pad_off(s, tc.i, tc.j, tc.k), st, sl, f);
     const long long fo = int_off(s, tc.i, tc.j, tc.k);
-    float2* F = reinterpret_cast<float2*>(s.F[D]);
-#pragma unroll
-    for (int n = 0; n < NEQ; ++n) at(s, F, NEQ * s.IV, n * s.IV + fo) = make_float2(f[n].hi, f[n].lo);
+    float4* F = s.FFa[D];
+    const long long n3 = 3 * s.IV;
+    at(s, F, n3, 3 * fo) = make_float4(f[0].hi, f[0].lo, f[1].hi, f[1].lo);
+    at(s, F, n3, 3 * fo + 1) = make_float4(f[2].hi, f[2].lo, f[3].hi, f[3].lo);
+    at(s, F, n3, 3 * fo + 2) = make_float4(f[4].hi, f[4].lo, 0.0f, 0.0f);
   }
 }
 
@@ -251,8 +253,9 @@ __global__ void __maxnreg__(80) k_inviscid_ff(const SolveDev* __restrict__ solve
 // Viscous terms on the NGV ring (the binary64 k_viscous in float-float: the
 // 4th-order gradients of u, v, w, T, Sutherland mu, the six stresses and three
 // energy fluxes; src/calc_gradient.cpp:17-66, src/Block3d.cpp:750-868).  The
-// terms are float-float pairs in Tv's bytes; mu (interior, lagged into the time
-// step) is stored in binary64.  Plane tiles over the ring, as the binary64 kernel.
+// terms are float-float, grouped by differencing direction (SolveDev::TvG); mu
+// (interior, lagged into the time step) is stored in binary64.  Plane tiles over
+// the ring, as the binary64 kernel.
 
 __device__ __forceinline__ ff d4_ff(const SolveDev& s, const float2* f, long long n, long long o, long long st,
                                     ff c12, ff c23) {
@@ -304,11 +307,17 @@ __global__ void __launch_bounds__(256) k_viscous_ff(const SolveDev* __restrict__
     const ff ex = ff_fma_acc(ww, txz, ff_fma_acc(vv, txy, uu * txx)) - mk * Tx;
     const ff ey = ff_fma_acc(ww, tyz, ff_fma_acc(vv, tyy, uu * txy)) - mk * Ty;
     const ff ez = ff_fma_acc(ww, tzz, ff_fma_acc(vv, tyz, uu * txz)) - mk * Tz;
-    const long long r = ring_off(s, i, j, k), RV = s.RV, n9 = kViscTerms * RV;
-    float2* Tv = reinterpret_cast<float2*>(s.Tv);
+    // grouped by differencing direction: the four terms of equations 1..4
+    // differenced along d, two float4 per direction and ring point
+    const long long r = ring_off(s, i, j, k), RV = s.RV, n6 = 6 * RV;
     const ff terms[kViscTerms] = {txx, tyy, tzz, txy, txz, tyz, ex, ey, ez};
 #pragma unroll
-    for (int q = 0; q < kViscTerms; ++q) at(s, Tv, n9, q * RV + r) = make_float2(terms[q].hi, terms[q].lo);
+    for (int d = 0; d < 3; ++d) {
+      const ff a = terms[visc_term(1, d)], b = terms[visc_term(2, d)], c = terms[visc_term(3, d)],
+               e = terms[visc_term(4, d)];
+      at(s, s.TvG, n6, 2 * (d * RV + r)) = make_float4(a.hi, a.lo, b.hi, b.lo);
+      at(s, s.TvG, n6, 2 * (d * RV + r) + 1) = make_float4(c.hi, c.lo, e.hi, e.lo);
+    }
   }
 }
 

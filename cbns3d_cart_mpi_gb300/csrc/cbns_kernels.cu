@@ -1183,6 +1183,53 @@ __device__ __forceinline__ void update_tiles(const SolveDev* __restrict__ solves
       direction(RV + r, ry, CS.c12y, CS.c23y);
       direction(2 * RV + r, rz, CS.c12z, CS.c23z);
     }
+    // CBNS_FP64_FF: every equation's chain of the binary64 update below (the
+    // inviscid flux differences along x, y, z, then minus the 4th-order viscous
+    // divergence along x, y, z) in float-float arithmetic, all equations at
+    // once: per direction, the faces' fluxes are three 16-byte loads per face and
+    // the four terms differenced along it two 16-byte loads per ring point.
+    // Accumulated without renormalising, rounded to binary64 once per equation.
+    double dff[NEQ];
+    if constexpr (FF) {
+      auto cf = [](float2 v) { return ff{v.x, v.y}; };
+      ff acc[NEQ];
+      const long long n3 = 3 * IV, n6 = 6 * RV;
+      const long long fn[3] = {fx, fy, fz}, rs[3] = {1, ry, rz};
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        const float4* G = s.FFa[d];
+        const float4 o0 = at(s, G, n3, 3 * fo), o1 = at(s, G, n3, 3 * fo + 1), o2 = at(s, G, n3, 3 * fo + 2);
+        const float4 x0 = at(s, G, n3, 3 * fn[d]), x1 = at(s, G, n3, 3 * fn[d] + 1),
+                     x2 = at(s, G, n3, 3 * fn[d] + 2);
+        const ff dif[NEQ] = {ff{x0.x, x0.y} - ff{o0.x, o0.y}, ff{x0.z, x0.w} - ff{o0.z, o0.w},
+                             ff{x1.x, x1.y} - ff{o1.x, o1.y}, ff{x1.z, x1.w} - ff{o1.z, o1.w},
+                             ff{x2.x, x2.y} - ff{o2.x, o2.y}};
+        const ff h = cf(s.ff_hf[d]);
+#pragma unroll
+        for (int n = 0; n < NEQ; ++n) acc[n] = d == 0 ? dif[n] * h : ff_fma_acc(dif[n], h, acc[n]);
+      }
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        const float4* T = s.TvG;
+        const long long b0 = 2 * (d * RV + r), sd = 2 * rs[d];
+        const float4 m2a = at(s, T, n6, b0 - 2 * sd), m2b = at(s, T, n6, b0 - 2 * sd + 1);
+        const float4 p2a = at(s, T, n6, b0 + 2 * sd), p2b = at(s, T, n6, b0 + 2 * sd + 1);
+        const float4 m1a = at(s, T, n6, b0 - sd), m1b = at(s, T, n6, b0 - sd + 1);
+        const float4 p1a = at(s, T, n6, b0 + sd), p1b = at(s, T, n6, b0 + sd + 1);
+        const ff m2[4] = {ff{m2a.x, m2a.y}, ff{m2a.z, m2a.w}, ff{m2b.x, m2b.y}, ff{m2b.z, m2b.w}};
+        const ff p2[4] = {ff{p2a.x, p2a.y}, ff{p2a.z, p2a.w}, ff{p2b.x, p2b.y}, ff{p2b.z, p2b.w}};
+        const ff m1[4] = {ff{m1a.x, m1a.y}, ff{m1a.z, m1a.w}, ff{m1b.x, m1b.y}, ff{m1b.z, m1b.w}};
+        const ff p1[4] = {ff{p1a.x, p1a.y}, ff{p1a.z, p1a.w}, ff{p1b.x, p1b.y}, ff{p1b.z, p1b.w}};
+        const ff c12 = -cf(s.ff_c12[d]), c23 = -cf(s.ff_c23[d]);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          acc[1 + q] = ff_fma_acc(m2[q] - p2[q], c12, acc[1 + q]);
+          acc[1 + q] = ff_fma_acc(p1[q] - m1[q], c23, acc[1 + q]);
+        }
+      }
+#pragma unroll
+      for (int n = 0; n < NEQ; ++n) dff[n] = ff_to_double(acc[n]);
+    }
     double qn[NEQ];
 #pragma unroll
     for (int n = 0; n < NEQ; ++n) {
@@ -1194,31 +1241,7 @@ __device__ __forceinline__ void update_tiles(const SolveDev* __restrict__ solves
         df = fma_(at(s, F1, n5, n * IV + fy) - at(s, F1, n5, n * IV + fo), idy, df);
         df = fma_(at(s, F2, n5, n * IV + fz) - at(s, F2, n5, n * IV + fo), idz, df);
       } else if constexpr (FF) {
-        // CBNS_FP64_FF: the same chain in float-float arithmetic, from the
-        // float-float face fluxes and viscous terms (pairs in F's and Tv's
-        // bytes), accumulated without renormalising and rounded to binary64 once.
-        const long long n5 = NEQ * IV;
-        auto ld = [&](const double* a, long long n, long long i2) {
-          const float2 v = at(s, reinterpret_cast<const float2*>(a), n, i2);
-          return ff{v.x, v.y};
-        };
-        auto cf = [](float2 v) { return ff{v.x, v.y}; };
-        ff d = (ld(F0, n5, n * IV + fx) - ld(F0, n5, n * IV + fo)) * cf(s.ff_hf[0]);
-        d = ff_fma_acc(ld(F1, n5, n * IV + fy) - ld(F1, n5, n * IV + fo), cf(s.ff_hf[1]), d);
-        d = ff_fma_acc(ld(F2, n5, n * IV + fz) - ld(F2, n5, n * IV + fo), cf(s.ff_hf[2]), d);
-        if (n > 0) {
-          const long long n9 = kViscTerms * RV;
-          const long long vx = visc_term(n, 0) * RV + r, vy = visc_term(n, 1) * RV + r,
-                          vz = visc_term(n, 2) * RV + r;
-          const double* Tv = s.Tv;
-          d = ff_fma_acc(ld(Tv, n9, vx - 2) - ld(Tv, n9, vx + 2), -cf(s.ff_c12[0]), d);
-          d = ff_fma_acc(ld(Tv, n9, vx + 1) - ld(Tv, n9, vx - 1), -cf(s.ff_c23[0]), d);
-          d = ff_fma_acc(ld(Tv, n9, vy - 2 * ry) - ld(Tv, n9, vy + 2 * ry), -cf(s.ff_c12[1]), d);
-          d = ff_fma_acc(ld(Tv, n9, vy + ry) - ld(Tv, n9, vy - ry), -cf(s.ff_c23[1]), d);
-          d = ff_fma_acc(ld(Tv, n9, vz - 2 * rz) - ld(Tv, n9, vz + 2 * rz), -cf(s.ff_c12[2]), d);
-          d = ff_fma_acc(ld(Tv, n9, vz + rz) - ld(Tv, n9, vz - rz), -cf(s.ff_c23[2]), d);
-        }
-        df = ff_to_double(d);
+        df = dff[n];
       } else {
         // Inviscid flux differences, then minus the viscous divergence, as one
         // chain of fused multiply-adds with the 1/h-folded weights negated.

@@ -283,9 +283,11 @@ def test_block_size_limit_follows_memory_not_a_31_bit_index():
         # the float-float copies)
         assert 300 < per_cell[prec] < 520, per_cell
     # Float-float solves add float-float copies of Q and Q_p and of six
-    # primitives: 16 pairs of binary32 (128 bytes) per padded cell.
+    # primitives (16 pairs of binary32, 128 bytes, per padded cell), and pack the
+    # face fluxes (48 instead of 40 bytes per interior cell and direction) and the
+    # viscous terms (96 instead of 72 bytes per ring point).
     extra = footprint(256, 256, 256, "fp64_ff") - footprint(256, 256, 256, "fp64")
-    assert abs(extra - 128 * 264 ** 3) < 4096, extra
+    assert abs(extra - (128 * 264 ** 3 + 24 * 256 ** 3 + 24 * 260 ** 3)) < 4096, extra
     # 745^3 and 746^3 straddle the old 31-bit limit; both are accepted now.
     assert footprint(746, 746, 746) > footprint(745, 745, 745)
     # Tile coordinates are 16-bit: 65535 - 2 NG cells along an axis is the most.
