@@ -52,12 +52,14 @@ struct WenoFF {
 __device__ __forceinline__ void weno5_side_ff(ff D1, ff C1, ff D2, ff C2, ff D3, ff C3, ff e1, ff e2, ff e3,
                                               ff g1, ff g2s, ff g3s, WenoFF& out) {
   constexpr ff eps4 = ff_const(4.0e-6);
-  const ff is1 = ff_fma(C1, D1, ff_sqr_add_acc(e1, eps4));
-  const ff is2 = ff_fma(C2, D2, ff_sqr_add_acc(e2, eps4));
-  const ff is3 = ff_fma(C3, D3, ff_sqr_add_acc(e3, eps4));
+  // the indicators and the denominator are sums of positive terms (no
+  // cancellation), left unrenormalised like products
+  const ff is1 = ff_fma_acc(C1, D1, ff_sqr_add_acc(e1, eps4));
+  const ff is2 = ff_fma_acc(C2, D2, ff_sqr_add_acc(e2, eps4));
+  const ff is3 = ff_fma_acc(C3, D3, ff_sqr_add_acc(e3, eps4));
   const ff a1 = ff_sqr(is1), a2 = ff_sqr(is2), a3 = ff_sqr(is3);
   const ff p1 = a2 * a3, q2 = a1 * a3, q3 = a1 * a2;
-  out.den = ff_fma(6.0f, q2, ff_fma_acc(3.0f, q3, p1));
+  out.den = ff_fma_acc(6.0f, q2, ff_fma_acc(3.0f, q3, p1));
   out.num = ff_fma(q2, g2s, ff_fma_acc(q3, g3s, p1 * g1));
 }
 
@@ -120,7 +122,7 @@ __device__ __forceinline__ void face_ff(const SolveDev& s, const float2* __restr
     Uv[2] = ff_fma(wL, Ls.w - Rs.w, Rs.w);
     HH = ff_fma(wL, Ls.h - Rs.h, Rs.h);
   }
-  const ff q2 = ff_sqr_add(Uv[2], ff_sqr_add_acc(Uv[1], ff_sqr(Uv[0])));
+  const ff q2 = ff_sqr_add_acc(Uv[2], ff_sqr_add_acc(Uv[1], ff_sqr(Uv[0])));  // no cancellation
   const ff hq2 = ff_scale(q2, 0.5f);
   const ff c2 = gam1 * (HH - hq2);
   const ff ic = ff_rsqrt(c2);  // 1/c
@@ -146,11 +148,13 @@ __device__ __forceinline__ void face_ff(const SolveDev& s, const float2* __restr
         ff_fma(-Uv[2], fm[2], ff_fma_acc(-Uv[1], fm[1], ff_fma_acc(-Uv[0], fm[0], ff_fma_acc(hq2, f0, f4))));
     const ff A = K * t;
     const ff g = ff_fma(un, f0, -fm[D]);
-    sl.put(m, ff_fma(hic, g, A));
-    sl.put(6 + m, f0 - ff_scale(A, 2.0f));
-    sl.put(12 + m, ff_fma(-hic, g, A));
-    sl.put(18 + m, ff_fma(-u1, f0, fm[T1]));
-    sl.put(24 + m, ff_fma(-u2, f0, fm[T2]));
+    // the characteristic values enter the reconstructions only through
+    // differences and as addends: stored unrenormalised
+    sl.put(m, ff_fma_acc(hic, g, A));
+    sl.put(6 + m, ff_add_acc(f0, ff_scale(A, -2.0f)));
+    sl.put(12 + m, ff_fma_acc(-hic, g, A));
+    sl.put(18 + m, ff_fma_acc(-u1, f0, fm[T1]));
+    sl.put(24 + m, ff_fma_acc(-u2, f0, fm[T2]));
 #pragma unroll
     for (int n = 0; n < NEQ; ++n) f[n] = g5[n];
   }
@@ -183,7 +187,7 @@ __device__ __forceinline__ void face_ff(const SolveDev& s, const float2* __restr
     mL[D] = ff_fma(un, rhoL, cc * dm);
     mL[T1] = ff_fma(u1, rhoL, rl[3]);
     mL[T2] = ff_fma(u2, rhoL, rl[4]);
-    EL = ff_fma(HH, sp, ff_fma_acc(uncc, dm, ff_fma_acc(hq2, rl[1], ff_fma_acc(u1, rl[3], u2 * rl[4]))));
+    EL = ff_fma_acc(HH, sp, ff_fma_acc(uncc, dm, ff_fma_acc(hq2, rl[1], ff_fma_acc(u1, rl[3], u2 * rl[4]))));
   }
   {
     const ff sp = rr[0] + rr[2], dm = rr[2] - rr[0];
@@ -191,7 +195,7 @@ __device__ __forceinline__ void face_ff(const SolveDev& s, const float2* __restr
     mR[D] = ff_fma(un, rhoR, cc * dm);
     mR[T1] = ff_fma(u1, rhoR, rr[3]);
     mR[T2] = ff_fma(u2, rhoR, rr[4]);
-    ER = ff_fma(HH, sp, ff_fma_acc(uncc, dm, ff_fma_acc(hq2, rr[1], ff_fma_acc(u1, rr[3], u2 * rr[4]))));
+    ER = ff_fma_acc(HH, sp, ff_fma_acc(uncc, dm, ff_fma_acc(hq2, rr[1], ff_fma_acc(u1, rr[3], u2 * rr[4]))));
   }
 
   // Local Lax-Friedrichs flux; both 1/rho from one reciprocal.
@@ -203,22 +207,23 @@ __device__ __forceinline__ void face_ff(const SolveDev& s, const float2* __restr
     vL[a] = mL[a] * iL;
     vR[a] = mR[a] * iR;
   }
-  const ff kL = ff_fma(mL[2], vL[2], ff_fma_acc(mL[1], vL[1], mL[0] * vL[0]));
-  const ff kR = ff_fma(mR[2], vR[2], ff_fma_acc(mR[1], vR[1], mR[0] * vR[0]));
+  const ff kL = ff_fma_acc(mL[2], vL[2], ff_fma_acc(mL[1], vL[1], mL[0] * vL[0]));
+  const ff kR = ff_fma_acc(mR[2], vR[2], ff_fma_acc(mR[1], vR[1], mR[0] * vR[0]));
   const ff pL = gam1 * (EL - ff_scale(kL, 0.5f));
   const ff pR = gam1 * (ER - ff_scale(kR, 0.5f));
   const ff c2L = (gamma * iL) * pL, c2R = (gamma * iR) * pR;
   const ff cL = c2L * ff_rsqrt(c2L), cR = c2R * ff_rsqrt(c2R);
   const ff alpha = ff_max(ff_abs(vR[D]) + cR, ff_abs(vL[D]) + cL);
   const ff fL = mL[D], fR = mR[D];
-  out[0] = ff_fma(-alpha, rhoR - rhoL, ff_add_acc(fL, fR));
+  // the fluxes are stored unrenormalised: the update only differences them
+  out[0] = ff_fma_acc(-alpha, rhoR - rhoL, ff_add_acc(fL, fR));
   const ff pLR = ff_add_acc(pL, pR);
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
     const ff fLa = (a == D) ? ff_fma_acc(fL, vL[a], pLR) : fL * vL[a];
-    out[1 + a] = ff_fma(-alpha, mR[a] - mL[a], ff_fma_acc(fR, vR[a], fLa));
+    out[1 + a] = ff_fma_acc(-alpha, mR[a] - mL[a], ff_fma_acc(fR, vR[a], fLa));
   }
-  out[4] = ff_fma(-alpha, ER - EL, ff_fma_acc(vR[D], ER + pR, vL[D] * (EL + pL)));
+  out[4] = ff_fma_acc(-alpha, ER - EL, ff_fma_acc(vR[D], ER + pR, vL[D] * (EL + pL)));
 }
 
 // One face per thread over the interior tiles (the binary64 k_inviscid's walk).
