@@ -279,9 +279,9 @@ def test_block_size_limit_follows_memory_not_a_31_bit_index():
         assert fp768 < hbm, (prec, fp768)
         assert footprint(1024, 1024, 1024, prec) > hbm
         per_cell[prec] = fp768 / 776 ** 3
-        # grows with the padded volume: about 380 bytes per padded cell (500 with
-        # the float-float copies)
-        assert 300 < per_cell[prec] < 520, per_cell
+        # grows with the padded volume: about 380 bytes per padded cell (about 555
+        # with the float-float copies and packed layouts; 768^3 is then 259 GB)
+        assert 300 < per_cell[prec] < 600, per_cell
     # Float-float solves add float-float copies of Q and Q_p and of six
     # primitives (16 pairs of binary32, 128 bytes, per padded cell), and pack the
     # face fluxes (48 instead of 40 bytes per interior cell and direction) and the
