@@ -323,7 +323,7 @@ def run_ours(args, rank, world, local):
     # timed, profiled), and the error against the binary64 state after them.
     Q64 = s.download_Q() if not (args.no_mixed and args.no_ff) else None
 
-    def precision_leg(prec):
+    def precision_leg(prec, e2e=False):
         sx = Solver(p, precision=prec)
         sx.upload_Q(Q0, 0.0)
         xstream = torch.cuda.ExternalStream(sx.stream)
@@ -341,6 +341,24 @@ def run_ours(args, rank, world, local):
         sx.run(args.steps)
         xprof = sx.profile_end()
         a = sx.download_Q()[NG:-NG, NG:-NG, NG:-NG].reshape(-1, 5)
+        xe2e = None
+        if e2e:
+            # end to end as the headline's e2e: host state uploaded and downloaded
+            # every step through the asynchronous calls of one handle
+            xin, xout = sx.pinned_state(), sx.pinned_state()
+            xin[...] = Q0
+            sx.upload_Q_async(xin, 0.0)
+            sx.step_async()
+            sx.download_Q_async(xout)
+            sx.wait()
+            barrier(world)
+            t0 = time.perf_counter()
+            for _ in range(args.steps):
+                sx.upload_Q_async(xin, 0.0)
+                sx.step_async()
+                sx.download_Q_async(xout)
+            sx.wait()
+            xe2e = reduce_max(time.perf_counter() - t0, world)
         sx.close()
         b = Q64[NG:-NG, NG:-NG, NG:-NG].reshape(-1, 5)
         # L-inf error over each field's scale; the three momentum fields share
@@ -349,7 +367,7 @@ def run_ours(args, rank, world, local):
         scale = np.abs(b).max(axis=0)
         scale[1:4] = scale[1:4].max()
         err = (np.abs(a - b).max(axis=0) / scale).tolist()
-        return xms, xprof, err
+        return (xms, xprof, err, xe2e) if e2e else (xms, xprof, err)
 
     # FP32-mixed leg.
     if not args.no_mixed:
@@ -392,7 +410,7 @@ def run_ours(args, rank, world, local):
     # roofline: binary32 instructions issued (ncu count per face) over the
     # binary32 FMA pipe's measured instruction rate.
     if not args.no_ff:
-        fms, fprof, ferr = precision_leg("fp64_ff")
+        fms, fprof, ferr, fe2e = precision_leg("fp64_ff", e2e=not args.no_e2e)
         if rank == 0:
             ftot = sum(v[1] for v in fprof.values())
             fper = fprof["inviscid_x"][1] / fprof["inviscid_x"][0]
@@ -416,6 +434,11 @@ def run_ours(args, rank, world, local):
                             for k, v in fprof.items()},
                 "roofline": froof,
             }
+            if fe2e:
+                nst = int(np.prod(s.shape))
+                line["fp64_ff"]["e2e"] = {"value": world * cells * args.steps / fe2e, "unit": UNIT,
+                                          "h2d_bytes_per_step": nst * 8, "d2h_bytes_per_step": nst * 8,
+                                          "path": "as e2e, on a CBNS_FP64_FF handle"}
 
     # e2e: host buffers through the C ABI, copies inside the timed region.  Every
     # step uploads its input state from pinned host memory, steps, and downloads
