@@ -83,17 +83,18 @@ __device__ __forceinline__ void weno5_pair_ff(const ff (&v)[6], WenoFF& L, WenoF
 }
 
 // Per-thread float-float slots in shared memory: slot k of thread tid is the
-// pair of binary32 words (2k, 2k+1) of a thread-minor array, so a warp's accesses
-// to one slot are 32 consecutive words (no bank conflicts).  A thread touches
-// only its own slots, so no barrier is needed.
+// 8-byte word {hi, lo} k T + tid of a thread-minor float2 array, so a slot is
+// one 64-bit access and a warp's accesses to one slot are 32 consecutive words
+// (no bank conflicts).  A thread touches only its own slots, so no barrier is
+// needed.
 struct Slots {
-  float* base;
+  float2* base;
   int T, tid;
-  __device__ __forceinline__ void put(int k, ff v) const {
-    base[(2 * k) * T + tid] = v.hi;
-    base[(2 * k + 1) * T + tid] = v.lo;
+  __device__ __forceinline__ void put(int k, ff v) const { base[k * T + tid] = make_float2(v.hi, v.lo); }
+  __device__ __forceinline__ ff get(int k) const {
+    const float2 w = base[k * T + tid];
+    return ff{w.x, w.y};
   }
-  __device__ __forceinline__ ff get(int k) const { return ff{base[(2 * k) * T + tid], base[(2 * k + 1) * T + tid]}; }
 };
 constexpr int kFaceSlots = NEQ * 6;  // the characteristic fields of the six stencil cells
 
@@ -234,7 +235,7 @@ __device__ __forceinline__ void face_ff(const SolveDev& s, const float2* __restr
 template <int D>
 __global__ void __maxnreg__(80) k_inviscid_ff(const SolveDev* __restrict__ solves,
                                                const TileRef* __restrict__ tiles, int ntiles, int stage) {
-  extern __shared__ float face_slots[];
+  extern __shared__ float2 face_slots[];
   const Slots sl{face_slots, (int)blockDim.x, (int)threadIdx.x};
   for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
     const TileCell tc = tile_cell(tiles[t], 0);
@@ -264,9 +265,11 @@ __global__ void __maxnreg__(80) k_inviscid_ff(const SolveDev* __restrict__ solve
 
 __device__ __forceinline__ ff d4_ff(const SolveDev& s, const float2* f, long long n, long long o, long long st,
                                     ff c12, ff c23) {
-  // ((f[-2] - f[+2]) c12 + (f[+1] - f[-1]) c23), the 1/h folded into the weights
-  return ff_fma(ld(s, f, n, o - 2 * st) - ld(s, f, n, o + 2 * st), c12,
-                (ld(s, f, n, o + st) - ld(s, f, n, o - st)) * c23);
+  // ((f[-2] - f[+2]) c12 + (f[+1] - f[-1]) c23), the 1/h folded into the weights;
+  // unrenormalised: the gradients enter the stresses through sums, and the
+  // energy fluxes as multiplicands with a low part within a few ulps
+  return ff_fma_acc(ld(s, f, n, o - 2 * st) - ld(s, f, n, o + 2 * st), c12,
+                    (ld(s, f, n, o + st) - ld(s, f, n, o - st)) * c23);
 }
 
 __global__ void __launch_bounds__(256) k_viscous_ff(const SolveDev* __restrict__ solves,
@@ -333,7 +336,7 @@ void launch_faces_ff(const SolveDev* d, const TileRef* tiles, int ntiles, int st
                      cudaStream_t st, Profiler* pf) {
   // shared memory for kFaceSlots float-float slots per thread, up to 256 threads
   // (above the 48 KB default): the kernels' attribute, set once per device
-  constexpr int kMaxBytes = 256 * kFaceSlots * 2 * (int)sizeof(float);
+  constexpr int kMaxBytes = 256 * kFaceSlots * (int)sizeof(float2);
   constexpr int kMaxDevices = 64;
   static std::mutex mu;
   static bool opted[kMaxDevices] = {};
@@ -351,7 +354,7 @@ void launch_faces_ff(const SolveDev* d, const TileRef* tiles, int ntiles, int st
       opted[dev] = true;
     }
   }
-  const size_t smem = (size_t)nt * kFaceSlots * 2 * sizeof(float);
+  const size_t smem = (size_t)nt * kFaceSlots * sizeof(float2);
   auto run = [&](int id, auto kern) {
     if (pf) pf->before(id, st);
     kern<<<g, nt, smem, st>>>(d, tiles, ntiles, stage);

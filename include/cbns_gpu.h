@@ -50,9 +50,11 @@ typedef enum cbns_status {
 typedef enum cbns_precision {
   CBNS_FP64 = 0,       /* every operation in IEEE binary64 */
   CBNS_FP32_MIXED = 1, /* WENO, projections and fluxes in binary32; state, RK3 and sums in binary64 */
-  CBNS_FP64_FF = 2     /* as CBNS_FP64, but the inviscid face fluxes (Roe eigenvectors, WENO5,
-                          Lax-Friedrichs) in float-float arithmetic: pairs of binary32 numbers,
-                          about 47 significant bits, on the binary32 pipes */
+  CBNS_FP64_FF = 2     /* the state, its RK3 combination and the KE/enstrophy sums in binary64;
+                          the face fluxes, viscous terms, flux differences, primitives and the
+                          time step's per-cell speed in float-float arithmetic (pairs of binary32
+                          numbers, about 47 significant bits) on the binary32 pipes.  Within
+                          the binary64 path's 1e-11 parity bar of the reference. */
 } cbns_precision;
 
 /*
