@@ -477,12 +477,12 @@ def run_ours(args, rank, world, local):
                            "synchronous_calls": world * cells * args.steps / seq}
     s.close()
 
-    # Larger blocks, state built on the device: binary64 at 512^3 (50 GB), and
-    # FP32-mixed at 512^3 and at 768^3 (165 GB), above the old 31-bit-index limit
-    # (N ~ 745).
+    # Larger blocks, state built on the device: binary64 at 512^3 (50 GB),
+    # float-float at 512^3 (78 GB) and 768^3 (259 GB), and FP32-mixed at 512^3 and
+    # at 768^3 (165 GB), above the old 31-bit-index limit (N ~ 745).
     if not args.no_large and rank == 0:
         large = []
-        for NL, prec in ((512, "fp64"), (512, "fp32_mixed"), (768, "fp32_mixed")):
+        for NL, prec in ((512, "fp64"), (512, "fp64_ff"), (768, "fp64_ff"), (512, "fp32_mixed"), (768, "fp32_mixed")):
             pl = tgv_params(NL, t_end=2.0)
             try:
                 sl = Solver(pl, precision=prec)

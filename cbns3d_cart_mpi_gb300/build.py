@@ -20,7 +20,7 @@ CSRC = os.path.join(PKG, "csrc")
 LIB = os.path.join(PKG, "lib")
 INCLUDE = os.path.join(ROOT, "include")
 
-GPU_SOURCES = ["cbns_kernels.cu", "cbns_ff_faces.cu", "cbns_api.cu", "cbns_noalloc.cu", "cbns_serve.cu",
+GPU_SOURCES = ["cbns_kernels.cu", "cbns_ff_kernels.cu", "cbns_api.cu", "cbns_noalloc.cu", "cbns_serve.cu",
                "cbns_ckpt.cu"]
 PROBE_SOURCE = "cbns_probe.cu"
 HOST_SOURCES = ["host/cbns_host.cpp"]

@@ -1,16 +1,17 @@
-// cbns_ff_faces.cu — the inviscid face fluxes of CBNS_FP64_FF solves: the
-// binary64 face kernel's scheme (Roe-averaged characteristic WENO5 with local
-// Lax-Friedrichs splitting; src/Block3d.cpp:555-748, src/eigenvectors_roe.cpp,
-// src/weno.cpp, src/lf_flux.cpp) evaluated in float-float arithmetic
-// (cbns_ff.cuh) on the binary32 pipes, one face per thread.
-//
-// The inputs are float-float copies of the binary64 state and of the face
-// primitives (sqrt(rho), H, u, v, w), split once per cell by the binary64 update
-// and start-up kernels, so this kernel issues no binary64 arithmetic except one
-// addition per stored flux component, which rounds the float-float flux to the
-// binary64 array the binary64 update reads.  Each step below is the binary64
-// kernel's (cbns_kernels.cu, face_core), operation for operation where the
-// float-float forms allow; the notes there give the algebra.
+// cbns_ff_kernels.cu — the float-float kernels of CBNS_FP64_FF solves, on the
+// binary32 pipes (arithmetic: cbns_ff.cuh):
+//   k_inviscid_ff<D>  the inviscid face fluxes, one face per thread: the binary64
+//                     face kernel's scheme (Roe-averaged characteristic WENO5 with
+//                     local Lax-Friedrichs splitting; src/Block3d.cpp:555-748,
+//                     src/eigenvectors_roe.cpp, src/weno.cpp, src/lf_flux.cpp)
+//   k_viscous_ff      the viscous terms on the NGV ring (src/calc_gradient.cpp:17-66,
+//                     src/Block3d.cpp:750-868)
+// Their inputs are the float-float copies of the state and of the primitives
+// sqrt(rho), H, u, v, w, T that the update writes with the binary64 state; their
+// outputs are float-float pairs packed for the update's 16-byte loads
+// (SolveDev::FFa, TvG), and mu in binary64 for the time step.  Each step is the
+// binary64 kernels' (cbns_kernels.cu: face_core, k_viscous), operation for
+// operation where the float-float forms allow; the notes there give the algebra.
 #include <cuda_runtime.h>
 
 #include <mutex>

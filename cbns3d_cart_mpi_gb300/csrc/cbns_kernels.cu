@@ -1494,7 +1494,7 @@ static int grid_for(int ntiles, int max_ctas) {
   return max_ctas > 0 && ntiles > max_ctas ? max_ctas : ntiles;
 }
 
-// cbns_ff_faces.cu
+// cbns_ff_kernels.cu
 void launch_faces_ff(const SolveDev* d, const TileRef* tiles, int ntiles, int stage, int g, int nt,
                      cudaStream_t st, Profiler* pf);
 void launch_viscous_ff(const SolveDev* d, const TileRef* ring, int nring, int g, int nt, cudaStream_t st,
