@@ -160,3 +160,34 @@ def test_plane_tiles_cover_each_ring_exactly():
                     assert -NGV <= c[0] < IM + NGV and -NGV <= c[1] < JM + NGV
                     seen[c] = seen.get(c, 0) + 1
         assert len(seen) == rx * ry * rz and set(seen.values()) == {1}
+
+
+@pytest.mark.parametrize("shape", SHAPES)
+def test_float_float_packed_layouts_stay_in_bounds(shape):
+    """CBNS_FP64_FF packs a face's five flux pairs as three float4 per interior
+    cell (FFa[d]: element 3 c + h, 3 IV elements) and, per direction, the four
+    viscous terms differenced along it as two float4 per ring point (TvG: element
+    2 (d RV + r) + h, 6 RV elements).  The update reads the cell's and its
+    periodic neighbour's face words and the terms at r +- 1, 2 ring strides; the
+    face and viscous kernels write the cell's words and every ring point's."""
+    IM, JM, KM = shape
+    g = geom(IM, JM, KM)
+    IV, RV = g["IV"], g["RV"]
+    interior = ((0, 0, 0), (IM, JM, KM))
+    ring = ((-NGV, -NGV, -NGV), (IM + NGV, JM + NGV, KM + NGV))
+    # FFa: the cell (and, wrapped, its neighbour, also an interior cell) times 3, + 0..2
+    lo, hi = span(lambda i, j, k: 3 * int_off(IM, JM, i, j, k), *interior, [0, 1, 2])
+    assert lo >= 0 and hi < 3 * IV
+    # TvG reads: per direction d, 2 (d RV + r + o) + h, o in +-1, +-2 ring strides
+    rstrides = [1, g["rx"], g["rx"] * g["ry"]]
+    for d, st in enumerate(rstrides):
+        offs = [2 * (d * RV + m * st) + h for m in (-2, -1, 1, 2) for h in (0, 1)]
+        lo, hi = span(lambda i, j, k: 2 * ring_off(g, i, j, k), *interior, offs)
+        assert lo >= 0 and hi < 6 * RV
+    # TvG writes: every ring point, every direction
+    lo, hi = span(lambda i, j, k: 2 * ring_off(g, i, j, k), *ring, [2 * d * RV + h for d in range(3) for h in (0, 1)])
+    assert lo >= 0 and hi < 6 * RV
+    # each direction's block stays in its own third: d RV <= d RV + r +- 2 st < (d + 1) RV
+    for st in rstrides:
+        lo, hi = span(lambda i, j, k: ring_off(g, i, j, k), *interior, [-2 * st, 2 * st])
+        assert lo >= 0 and hi < RV
