@@ -430,6 +430,9 @@ cbns_status cbns_create(const cbns_params* p, uint32_t IM, uint32_t JM, uint32_t
     s.ff_Cdt2 = split(c.C_dt_v2);
     s.ff_sum_ih = split(c.sum_ih);
     s.ff_sum_ih2 = split(c.sum_ih2);
+    s.ff_rho_ref = split(s.rho_ref);
+    s.ff_p_ref = split(s.p_ref);
+    s.ff_Ep_ref = split(s.E_ref + s.p_ref);
   }
   h->d_ctl = (SolveCtl*)(A + oCtl);
   s.ctl = h->d_ctl;

@@ -166,6 +166,12 @@ struct SolveDev {
   //   (d RV + r) 2 + h.
   float4* FFa[3];
   float4* TvG;
+  // CBNS_FP64_FF state copies are perturbations of the reference state: QF and
+  // QpF hold (rho - rho_ref, rho u, rho v, rho w, E - E_ref), the differences
+  // taken in binary64 before the split, so float-float's 47 bits are spent on
+  // the fluctuations rather than on E_ref ~ 1/(gamma (gamma-1) M^2).  The
+  // constants rho_ref, p_ref and E_ref + p_ref in float-float:
+  float2 ff_rho_ref, ff_p_ref, ff_Ep_ref;
 };
 
 // Blocks of SolveDev::PF: sqrt(rho), H, u, v, w, T.

@@ -6,8 +6,9 @@
 //                     src/eigenvectors_roe.cpp, src/weno.cpp, src/lf_flux.cpp)
 //   k_viscous_ff      the viscous terms on the NGV ring (src/calc_gradient.cpp:17-66,
 //                     src/Block3d.cpp:750-868)
-// Their inputs are the float-float copies of the state and of the primitives
-// sqrt(rho), H, u, v, w, T that the update writes with the binary64 state; their
+// Their inputs are the float-float copies of the state (its perturbation of the
+// reference state) and of the primitives sqrt(rho), H, u, v, w, T that the update
+// writes with the binary64 state; their
 // outputs are float-float pairs packed for the update's 16-byte loads
 // (SolveDev::FFa, TvG), and mu in binary64 for the time step.  Each step is the
 // binary64 kernels' (cbns_kernels.cu: face_core, k_viscous), operation for
@@ -200,9 +201,16 @@ __device__ __forceinline__ void face_ff(const SolveDev& s, const float2* __restr
     ER = ff_fma_acc(HH, sp, ff_fma_acc(uncc, dm, ff_fma_acc(hq2, rr[1], ff_fma_acc(u1, rr[3], u2 * rr[4]))));
   }
 
-  // Local Lax-Friedrichs flux; both 1/rho from one reciprocal.
-  const ff ip = ff_rcp(rhoL * rhoR);
-  const ff iL = ip * rhoR, iR = ip * rhoL;
+  // Local Lax-Friedrichs flux.  The reconstructed states are perturbations
+  // (rho', m, E') of the reference state (the inputs are, and the projections and
+  // WENO5 are linear and reproduce constants); rho = rho_ref + rho' for the
+  // velocities and the sound speed, and p' = p - p_ref = (gamma - 1)(E' - rho q^2
+  // / 2).  The momentum flux carries p' instead of p: the constant p_ref cancels
+  // in every flux difference.  Both 1/rho from one reciprocal.
+  const ff rref = cst(s.ff_rho_ref), pref = cst(s.ff_p_ref);
+  const ff rhoLf = rhoL + rref, rhoRf = rhoR + rref;
+  const ff ip = ff_rcp(rhoLf * rhoRf);
+  const ff iL = ip * rhoRf, iR = ip * rhoLf;
   ff vL[3], vR[3];
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
@@ -211,9 +219,9 @@ __device__ __forceinline__ void face_ff(const SolveDev& s, const float2* __restr
   }
   const ff kL = ff_fma_acc(mL[2], vL[2], ff_fma_acc(mL[1], vL[1], mL[0] * vL[0]));
   const ff kR = ff_fma_acc(mR[2], vR[2], ff_fma_acc(mR[1], vR[1], mR[0] * vR[0]));
-  const ff pL = gam1 * (EL - ff_scale(kL, 0.5f));
+  const ff pL = gam1 * (EL - ff_scale(kL, 0.5f));  // p - p_ref
   const ff pR = gam1 * (ER - ff_scale(kR, 0.5f));
-  const ff c2L = (gamma * iL) * pL, c2R = (gamma * iR) * pR;
+  const ff c2L = (gamma * iL) * (pL + pref), c2R = (gamma * iR) * (pR + pref);
   const ff cL = c2L * ff_rsqrt(c2L), cR = c2R * ff_rsqrt(c2R);
   const ff alpha = ff_max(ff_abs(vR[D]) + cR, ff_abs(vL[D]) + cL);
   const ff fL = mL[D], fR = mR[D];
@@ -225,7 +233,10 @@ __device__ __forceinline__ void face_ff(const SolveDev& s, const float2* __restr
     const ff fLa = (a == D) ? ff_fma_acc(fL, vL[a], pLR) : fL * vL[a];
     out[1 + a] = ff_fma_acc(-alpha, mR[a] - mL[a], ff_fma_acc(fR, vR[a], fLa));
   }
-  out[4] = ff_fma_acc(-alpha, ER - EL, ff_fma_acc(vR[D], ER + pR, vL[D] * (EL + pL)));
+  // q_n (E + p) with E + p = (E' + p') + (E_ref + p_ref)
+  const ff epref = cst(s.ff_Ep_ref);
+  out[4] = ff_fma_acc(-alpha, ER - EL,
+                      ff_fma_acc(vR[D], (ER + pR) + epref, vL[D] * ((EL + pL) + epref)));
 }
 
 // One face per thread over the interior tiles (the binary64 k_inviscid's walk).

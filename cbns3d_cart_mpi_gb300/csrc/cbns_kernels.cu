@@ -30,7 +30,10 @@
 // stream, with the binary64 state and its RK3 combination kept in binary64;
 // their face kernels (k_inviscid_x2<D>) compute two faces per thread in the
 // lanes of packed binary32x2 instructions, and their binary32 arrays are packed
-// per cell so that a stencil point is one or two 16-byte loads.
+// per cell so that a stencil point is one or two 16-byte loads.  CBNS_FP64_FF
+// solves keep the binary64 state and RK3 combination (k_update<double, S, true>,
+// k_dt_reduce<double, true>) and take their faces and viscous terms from the
+// float-float kernels of cbns_ff_kernels.cu.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -100,14 +103,22 @@ __device__ __forceinline__ void store_prims(const SolveDev& s, long long o, doub
   at(s, s.pd.H, V, o) = q.H;
 }
 
+// The split of a state into the float-float perturbation CBNS_FP64_FF kernels
+// read: (rho - rho_ref, rho u, rho v, rho w, E - E_ref), the differences taken in
+// binary64.
+__device__ __forceinline__ float2 ff_split_state(const SolveDev& s, int n, double q) {
+  return ff_split(n == 0 ? q - s.rho_ref : (n == NEQ - 1 ? q - s.E_ref : q));
+}
+
 // CBNS_FP64_FF solves: the float-float copies the face and viscous kernels
-// read, of a cell's state (into QFo, the copy of the array the state went to)
-// and of its primitives sqrt(rho), H, u, v, w, T (split on the integer pipe).
+// read, of a cell's state (into QFo, the copy of the array the state went to,
+// as the perturbation above) and of its primitives sqrt(rho), H, u, v, w, T
+// (split on the integer pipe).
 __device__ __forceinline__ void store_ff(const SolveDev& s, float2* QFo, long long d, const double (&q)[NEQ],
                                          double sr, double H, double u, double v, double w, double T) {
   const long long V = s.V, n5 = NEQ * V, np = kFFPrims * V;
 #pragma unroll
-  for (int n = 0; n < NEQ; ++n) at(s, QFo, n5, n * V + d) = ff_split(q[n]);
+  for (int n = 0; n < NEQ; ++n) at(s, QFo, n5, n * V + d) = ff_split_state(s, n, q[n]);
   float2* P = s.PF;
   at(s, P, np, d) = ff_split(sr);
   at(s, P, np, V + d) = ff_split(H);
@@ -118,23 +129,26 @@ __device__ __forceinline__ void store_ff(const SolveDev& s, float2* QFo, long lo
 }
 
 // CBNS_FP64_FF: the primitives of a state in float-float (prims64's formulas),
-// from the state's float-float split.
+// from the float-float perturbation q' = (rho - rho_ref, rho u, rho v, rho w,
+// E - E_ref): p = p_ref + (gamma - 1) (E' - rho q^2 / 2), as (gamma - 1) E_ref
+// = p_ref.
 struct PrimsFF {
   ff u, v, w, p, T, sr, H;
 };
 
 __device__ __forceinline__ PrimsFF prims_ff(const SolveDev& s, const ff (&q)[NEQ]) {
   auto cf = [](float2 v) { return ff{v.x, v.y}; };
-  const ff rs = ff_rsqrt(q[0]);
+  const ff rho = q[0] + cf(s.ff_rho_ref);
+  const ff rs = ff_rsqrt(rho);
   const ff ir = ff_sqr(rs);
   PrimsFF r;
   r.u = q[1] * ir;
   r.v = q[2] * ir;
   r.w = q[3] * ir;
-  const ff q2 = ff_sqr_add(r.w, ff_sqr_add_acc(r.v, ff_sqr(r.u)));
-  r.p = cf(s.ff_gam1) * (q[4] - ff_scale(q[0] * q2, 0.5f));
+  const ff q2 = ff_sqr_add_acc(r.w, ff_sqr_add_acc(r.v, ff_sqr(r.u)));  // no cancellation
+  r.p = cf(s.ff_gam1) * (q[4] - ff_scale(rho * q2, 0.5f)) + cf(s.ff_p_ref);
   r.T = (cf(s.ff_gM2) * r.p) * ir;
-  r.sr = q[0] * rs;
+  r.sr = rho * rs;
   r.H = ff_fma(cf(s.ff_ggam1) * r.p, ir, ff_scale(q2, 0.5f));
   return r;
 }
@@ -1293,12 +1307,13 @@ __device__ __forceinline__ void update_tiles(const SolveDev* __restrict__ solves
       mc = mixed_cell(s, qn);
       if (!(mc.rho > 0.0f) || !(s.cf.p_ref + mc.p > 0.0f)) atomicOr(&ctl->status, kStatusNonphysical);
     } else if constexpr (FF) {
-      // CBNS_FP64_FF: the float-float split of the state and its float-float
-      // primitives, the only copies the float-float kernels read (binary64
-      // primitives are formed on demand for output)
+      // CBNS_FP64_FF: the float-float split of the state (its perturbation of
+      // the reference state) and its float-float primitives, the only copies
+      // the float-float kernels read (binary64 primitives are formed on demand
+      // for output)
 #pragma unroll
       for (int n = 0; n < NEQ; ++n) {
-        const float2 t2 = ff_split(qn[n]);
+        const float2 t2 = ff_split_state(s, n, qn[n]);
         fq[n] = ff{t2.x, t2.y};
       }
       pf = prims_ff(s, fq);

@@ -243,9 +243,10 @@ def test_diagnostics_match_oracle():
 def test_parameter_corners_vs_oracle(Re, Mach, shape, seed, precision):
     """The ensemble and serving workloads draw Re in [400, 3200] and Ma in
     [0.05, 0.3] with perturbed initial data: corners of that range on odd block
-    shapes, 20 steps against the oracle at the parity bar.  Float-float
-    arithmetic (about 47 bits) gets ten times the binary64 run's bounds on the
-    time step and on the absolute error."""
+    shapes, 20 steps against the oracle at the parity bar and the binary64
+    run's absolute bound (float-float, in its perturbation form, is as close to
+    the oracle as binary64); float-float's time step, from float-float
+    primitives, gets ten times binary64's bound."""
     from oracle.oracle import OracleBlock
     from cbns3d_cart_mpi_gb300.solver import Solver, initial_condition_perturbed
     IM, JM, KM = shape
@@ -262,8 +263,7 @@ def test_parameter_corners_vs_oracle(Re, Mach, shape, seed, precision):
         assert abs(dt - dto) <= dt_tol * dto, n
     Qg, Qo = interior(s.download_Q()), interior(o.get_Q())
     print(precision, "Re %g Ma %g rel Linf" % (Re, Mach), dict(zip(FIELDS, rel_linf(Qg, Qo))))
-    assert_close(Qg, Qo, 1e-11, "%s Re %g Ma %g" % (precision, Re, Mach),
-                 tight=1e-13 if precision == "fp64" else 1e-12)
+    assert_close(Qg, Qo, 1e-11, "%s Re %g Ma %g" % (precision, Re, Mach), tight=1e-13)
 
 
 def test_fp64_ff_history_64_100_steps(golden_dir):
@@ -375,3 +375,25 @@ def test_float_float_building_blocks_against_binary64():
     assert sp[4, 0] == 0.0
     assert abs(sp[5, 0] - 3e38) <= 2.0 ** -46 * 3e38
     assert np.isnan(sp[6, 0]) and np.isnan(sp[7, 0])
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp64_ff"])
+def test_low_mach_vs_oracle(precision):
+    """Below the workloads' Mach range: Ma 0.02 (energy about 2e3 times the
+    velocity scale, the stiffest ratio for float-float's fixed 47 bits), 20
+    steps on an odd block against the oracle at the parity bar."""
+    from oracle.oracle import OracleBlock
+    from cbns3d_cart_mpi_gb300.solver import Solver, initial_condition_perturbed
+    p = tgv_params(18, JM=14, KM=10, Re=1600.0, Mach=0.02)
+    Q0 = initial_condition_perturbed(p, seed=21, amp=1e-3, nmodes=16, kmax=4)
+    s = Solver(p, precision=precision)
+    s.upload_Q(Q0, 0.0)
+    o = OracleBlock(p)
+    o.set_Q(Q0, 0.0)
+    for n in range(20):
+        dt, _ = s.step()
+        dto, _ = o.step()
+        assert abs(dt - dto) <= (1e-13 if precision == "fp64" else 1e-12) * dto, n
+    Qg, Qo = interior(s.download_Q()), interior(o.get_Q())
+    print(precision, "Ma 0.02 rel Linf", dict(zip(FIELDS, rel_linf(Qg, Qo))))
+    assert_close(Qg, Qo, 1e-11, "%s Ma 0.02" % precision, tight=1e-13)
