@@ -427,6 +427,8 @@ def run_ours(args, rank, world, local):
                                  "instruction rate; the reference's 1570 FLOPs per face take about 3.6 of them each")
             line["fp64_ff"] = {
                 "value": world * cells * args.steps / (fms * 1e-3), "unit": UNIT, "ms_per_step": fms / args.steps,
+                "dtype": "f64 state and RK3; float-float (binary32 pairs) faces, viscous terms, flux "
+                         "differences, primitives and time-step speeds",
                 "speedup_vs_fp64": ms / fms,
                 "linf_vs_fp64_over_field_scale": dict(zip(["rho", "rho*u", "rho*v", "rho*w", "E"], ferr)),
                 "error_after_steps": args.warmup + 2 * args.steps,
