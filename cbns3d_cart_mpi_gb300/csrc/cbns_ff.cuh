@@ -37,15 +37,23 @@ __host__ __device__ constexpr ff ff_const(double x) {
   return ff{(float)x, (float)(x - (double)(float)x)};
 }
 
+// The binary32 additions and multiplications below are __fadd_rn, __fsub_rn and
+// __fmul_rn: the compiler never merges these into a fused multiply-add, which
+// would change what the error-free transformations compute (and make the
+// results depend on how the surrounding code compiles).
+#define FF_ADD(a, b) __fadd_rn((a), (b))
+#define FF_SUB(a, b) __fsub_rn((a), (b))
+#define FF_MUL(a, b) __fmul_rn((a), (b))
+
 __device__ __forceinline__ ff ff_fast2sum(float a, float b) {  // |a| >= |b| or a = 0
-  const float s = a + b;
-  return ff{s, b - (s - a)};
+  const float s = FF_ADD(a, b);
+  return ff{s, FF_SUB(b, FF_SUB(s, a))};
 }
 
 __device__ __forceinline__ ff ff_two_sum(float a, float b) {
-  const float s = a + b;
-  const float v = s - a;
-  return ff{s, (a - (s - v)) + (b - v)};
+  const float s = FF_ADD(a, b);
+  const float v = FF_SUB(s, a);
+  return ff{s, FF_ADD(FF_SUB(a, FF_SUB(s, v)), FF_SUB(b, v))};
 }
 
 __device__ __forceinline__ ff operator-(ff a) { return ff{-a.hi, -a.lo}; }
@@ -53,7 +61,7 @@ __device__ __forceinline__ ff operator-(ff a) { return ff{-a.hi, -a.lo}; }
 // SloppyDWPlusDW: TwoSum of the high parts, the low parts added, renormalised.
 __device__ __forceinline__ ff operator+(ff a, ff b) {
   const ff s = ff_two_sum(a.hi, b.hi);
-  return ff_fast2sum(s.hi, s.lo + (a.lo + b.lo));
+  return ff_fast2sum(s.hi, FF_ADD(s.lo, FF_ADD(a.lo, b.lo)));
 }
 __device__ __forceinline__ ff operator-(ff a, ff b) { return a + (-b); }
 
@@ -64,30 +72,30 @@ __device__ __forceinline__ ff operator-(ff a, ff b) { return a + (-b); }
 // operation here accepts as a float-float operand (the renormalising Fast2Sum
 // would cost three additions per product).
 __device__ __forceinline__ ff operator*(ff a, ff b) {
-  const float p = a.hi * b.hi;
+  const float p = FF_MUL(a.hi, b.hi);
   float e = fmaf(a.hi, b.hi, -p);
   e = fmaf(a.lo, b.hi, fmaf(a.hi, b.lo, e));
   return ff{p, e};
 }
 
 // Times a power of two: exact.
-__device__ __forceinline__ ff ff_scale(ff a, float p2) { return ff{a.hi * p2, a.lo * p2}; }
+__device__ __forceinline__ ff ff_scale(ff a, float p2) { return ff{FF_MUL(a.hi, p2), FF_MUL(a.lo, p2)}; }
 
 // a * b + c, the product's error terms folded into one sloppy sum.
 __device__ __forceinline__ ff ff_fma(ff a, ff b, ff c) {
-  const float p = a.hi * b.hi;
+  const float p = FF_MUL(a.hi, b.hi);
   float e = fmaf(a.hi, b.hi, -p);
   e = fmaf(a.lo, b.hi, fmaf(a.hi, b.lo, e));
   const ff s = ff_two_sum(p, c.hi);
-  return ff_fast2sum(s.hi, s.lo + (e + c.lo));
+  return ff_fast2sum(s.hi, FF_ADD(s.lo, FF_ADD(e, c.lo)));
 }
 
 // c * b + d for a binary32 constant c.
 __device__ __forceinline__ ff ff_fma(float c, ff b, ff d) {
-  const float p = c * b.hi;
+  const float p = FF_MUL(c, b.hi);
   const float e = fmaf(c, b.lo, fmaf(c, b.hi, -p));
   const ff s = ff_two_sum(p, d.hi);
-  return ff_fast2sum(s.hi, s.lo + (e + d.lo));
+  return ff_fast2sum(s.hi, FF_ADD(s.lo, FF_ADD(e, d.lo)));
 }
 
 // Accumulating forms: the same results without the final Fast2Sum, for a value
@@ -95,40 +103,40 @@ __device__ __forceinline__ ff ff_fma(float c, ff b, ff d) {
 // takes any high part exactly and folds the low part into its error term) or is
 // widened to binary64.  A chain of multiply-adds renormalises once, at its end.
 __device__ __forceinline__ ff ff_fma_acc(ff a, ff b, ff c) {
-  const float p = a.hi * b.hi;
+  const float p = FF_MUL(a.hi, b.hi);
   float e = fmaf(a.hi, b.hi, -p);
   e = fmaf(a.lo, b.hi, fmaf(a.hi, b.lo, e));
   const ff s = ff_two_sum(p, c.hi);
-  return ff{s.hi, s.lo + (e + c.lo)};
+  return ff{s.hi, FF_ADD(s.lo, FF_ADD(e, c.lo))};
 }
 __device__ __forceinline__ ff ff_fma_acc(float c, ff b, ff d) {
-  const float p = c * b.hi;
+  const float p = FF_MUL(c, b.hi);
   const float e = fmaf(c, b.lo, fmaf(c, b.hi, -p));
   const ff s = ff_two_sum(p, d.hi);
-  return ff{s.hi, s.lo + (e + d.lo)};
+  return ff{s.hi, FF_ADD(s.lo, FF_ADD(e, d.lo))};
 }
 __device__ __forceinline__ ff ff_add_acc(ff a, ff b) {
   const ff s = ff_two_sum(a.hi, b.hi);
-  return ff{s.hi, s.lo + (a.lo + b.lo)};
+  return ff{s.hi, FF_ADD(s.lo, FF_ADD(a.lo, b.lo))};
 }
 __device__ __forceinline__ ff ff_sqr_add_acc(ff a, ff c) {
-  const float p = a.hi * a.hi;
-  const float e = fmaf(a.hi + a.hi, a.lo, fmaf(a.hi, a.hi, -p));
+  const float p = FF_MUL(a.hi, a.hi);
+  const float e = fmaf(FF_ADD(a.hi, a.hi), a.lo, fmaf(a.hi, a.hi, -p));
   const ff s = ff_two_sum(p, c.hi);
-  return ff{s.hi, s.lo + (e + c.lo)};
+  return ff{s.hi, FF_ADD(s.lo, FF_ADD(e, c.lo))};
 }
 
 // a^2 + c.
 __device__ __forceinline__ ff ff_sqr_add(ff a, ff c) {
-  const float p = a.hi * a.hi;
-  const float e = fmaf(a.hi + a.hi, a.lo, fmaf(a.hi, a.hi, -p));
+  const float p = FF_MUL(a.hi, a.hi);
+  const float e = fmaf(FF_ADD(a.hi, a.hi), a.lo, fmaf(a.hi, a.hi, -p));
   const ff s = ff_two_sum(p, c.hi);
-  return ff_fast2sum(s.hi, s.lo + (e + c.lo));
+  return ff_fast2sum(s.hi, FF_ADD(s.lo, FF_ADD(e, c.lo)));
 }
 
 __device__ __forceinline__ ff ff_sqr(ff a) {  // unrenormalised, as operator*
-  const float p = a.hi * a.hi;
-  const float e = fmaf(a.hi + a.hi, a.lo, fmaf(a.hi, a.hi, -p));
+  const float p = FF_MUL(a.hi, a.hi);
+  const float e = fmaf(FF_ADD(a.hi, a.hi), a.lo, fmaf(a.hi, a.hi, -p));
   return ff{p, e};
 }
 
@@ -139,10 +147,10 @@ __device__ __forceinline__ ff ff_sqr(ff a) {  // unrenormalised, as operator*
 __device__ __forceinline__ ff ff_rcp(ff a) {
   float y;
   asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(a.hi));
-  const float p = a.hi * y;
+  const float p = FF_MUL(a.hi, y);
   const float pe = fmaf(a.hi, y, -p);
-  const float r = fmaf(-a.lo, y, (1.0f - p) - pe);
-  return ff_fast2sum(y, y * fmaf(r, r, r));
+  const float r = fmaf(-a.lo, y, FF_SUB(FF_SUB(1.0f, p), pe));
+  return ff_fast2sum(y, FF_MUL(y, fmaf(r, r, r)));
 }
 
 // 1/sqrt(a) for a positive normal float-float a: y = estimate of 1/sqrt(a.hi),
@@ -150,13 +158,13 @@ __device__ __forceinline__ ff ff_rcp(ff a) {
 __device__ __forceinline__ ff ff_rsqrt(ff a) {
   float y;
   asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(a.hi));
-  const float s = y * y;
+  const float s = FF_MUL(y, y);
   const float se = fmaf(y, y, -s);  // y^2 = s + se exactly
-  const float p = a.hi * s;
+  const float p = FF_MUL(a.hi, s);
   float e = fmaf(a.hi, s, -p);
   e = fmaf(a.hi, se, fmaf(a.lo, s, e));  // a y^2 = p + e to float-float accuracy
-  const float r = (1.0f - p) - e;
-  return ff_fast2sum(y, y * (r * fmaf(0.375f, r, 0.5f)));
+  const float r = FF_SUB(FF_SUB(1.0f, p), e);
+  return ff_fast2sum(y, FF_MUL(y, FF_MUL(r, fmaf(0.375f, r, 0.5f))));
 }
 
 __device__ __forceinline__ ff ff_abs(ff a) { return a.hi < 0.0f ? -a : a; }
@@ -189,7 +197,7 @@ __device__ __forceinline__ float2 ff_split(double x) {
   // 2^(E-23) and subtract 2^(E-23) (exact)
   const unsigned pe = (hb & 0xff800000u) - (23u << 23);
   float hi = __uint_as_float(hb);
-  float lo = __uint_as_float(pe | ((l32 >> 6) & 0x7fffffu)) - __uint_as_float(pe);
+  float lo = FF_SUB(__uint_as_float(pe | ((l32 >> 6) & 0x7fffffu)), __uint_as_float(pe));
   if (e < 920u) {
     lo = __uint_as_float(sign);  // a zero of x's sign, so -0.0 stays -0.0
     if (e < 897u) hi = __uint_as_float(sign);
