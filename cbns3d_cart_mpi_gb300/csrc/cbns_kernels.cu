@@ -1381,10 +1381,13 @@ __device__ __forceinline__ void update_tiles(const SolveDev* __restrict__ solves
 // 11% faster at 80 registers (24 warps per SM, a few spills) than unconstrained
 // (126 registers); the binary32 one (memory-latency bound) 12% faster at 64
 // (32 warps per SM) than at 80.
-// FF: CBNS_FP64_FF solves (float-float flux differences and copies); their
-// float-float chain needs more than the binary64 update's 80 registers.
+// FF: CBNS_FP64_FF solves (float-float flux differences and copies).  That
+// kernel is bound by memory latency, so its cap is set for occupancy: at 64
+// registers eight 128-thread CTAs fit per SM (32 warps) against four at 128, and
+// the launch took 1.34 instead of 1.67 ms at 256^3 despite 4-32 bytes of spill
+// (80 registers: 1.46 ms); results bitwise the same.
 template <typename R, int STAGE, bool FF>
-__global__ void __maxnreg__(FF ? 128 : 80) k_update(const SolveDev* __restrict__ solves,
+__global__ void __maxnreg__(FF ? 64 : 80) k_update(const SolveDev* __restrict__ solves,
                                          const TileRef* __restrict__ tiles, int ntiles) {
   update_tiles<R, STAGE, FF>(solves, tiles, ntiles, STAGE);
 }
