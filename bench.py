@@ -423,8 +423,10 @@ def run_ours(args, rank, world, local):
                 froof["fp32_inst_per_face"] = finst
                 froof["achieved"] = issued * 2.0 * 1e-12  # as FMA-equivalent TFLOP/s
                 froof["frac"] = froof["achieved"] / froof["peak"]
+                ref_per_face = kernel_flops("inviscid_x", N, N, N) / N ** 3
                 froof["note"] = ("float-float arithmetic: binary32 instructions per face (ncu) over the pipe's "
-                                 "instruction rate; the reference's 1570 FLOPs per face take about 3.6 of them each")
+                                 "instruction rate; the reference's %d FLOPs per face take about %.1f of them each"
+                                 % (round(ref_per_face), finst / ref_per_face))
             line["fp64_ff"] = {
                 "value": world * cells * args.steps / (fms * 1e-3), "unit": UNIT, "ms_per_step": fms / args.steps,
                 "dtype": "f64 state and RK3; float-float (binary32 pairs) faces, viscous terms, flux "
