@@ -126,6 +126,8 @@ struct SolveDev {
   float4* PA;   // (u, v, w, T - T_ref), padded
   float4* PB;   // (rho, p - p_ref, sqrt(rho), H), padded
   float* muf;   // Sutherland mu, interior; lagged into calc_dt like the reference
+  // per direction, the face fluxes: IV float4 of equations 0-3, then IV floats
+  // of equation 4 (5 IV floats in all)
   float* Ff[3];
   float4* Tvg;
   // reference state of the perturbation form (u_ref = 0, E_ref = p_ref/(gamma-1))

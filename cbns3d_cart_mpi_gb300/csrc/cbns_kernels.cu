@@ -964,12 +964,16 @@ __global__ void __maxnreg__(128) k_inviscid_x2(const SolveDev* __restrict__ solv
     };
     f2 f[NEQ];
     face_core_x2<D>(s.cf, Ls, Rs, cell, f);
-    float* F = s.Ff[D];
+    // Packed for the update's loads: equations 0-3 as one float4 per face, then
+    // the energy flux in a block of its own (SolveDev::Ff).
+    float4* F4 = reinterpret_cast<float4*>(s.Ff[D]);
+    float* FE = s.Ff[D] + 4 * s.IV;
     const long long fo = int_off(s, i, j, k);
-#pragma unroll
-    for (int n = 0; n < NEQ; ++n) {
-      at(s, F, NEQ * s.IV, n * s.IV + fo) = f[n].v.x;
-      if (pair) at(s, F, NEQ * s.IV, n * s.IV + fo + s.IM) = f[n].v.y;
+    at(s, F4, s.IV, fo) = make_float4(f[0].v.x, f[1].v.x, f[2].v.x, f[3].v.x);
+    at(s, FE, s.IV, fo) = f[4].v.x;
+    if (pair) {
+      at(s, F4, s.IV, fo + s.IM) = make_float4(f[0].v.y, f[1].v.y, f[2].v.y, f[3].v.y);
+      at(s, FE, s.IV, fo + s.IM) = f[4].v.y;
     }
   }
 }
@@ -1197,6 +1201,26 @@ __device__ __forceinline__ void update_tiles(const SolveDev* __restrict__ solves
       direction(RV + r, ry, CS.c12y, CS.c23y);
       direction(2 * RV + r, rz, CS.c12z, CS.c23z);
     }
+    // FP32-mixed: then the inviscid flux differences along x, y, z, each
+    // equation's chain in that order; per direction the cell's and its
+    // neighbour's face are a float4 (equations 0-3) and a float (equation 4).
+    float dfm[NEQ];
+    if constexpr (MIXED) {
+      const float* Fd[3] = {F0, F1, F2};
+      const long long fn[3] = {fx, fy, fz};
+      const float hd[3] = {idx, idy, idz};
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        const float4* F4 = reinterpret_cast<const float4*>(Fd[d]);
+        const float* FE = Fd[d] + 4 * IV;
+        const float4 a = at(s, F4, IV, fo), b = at(s, F4, IV, fn[d]);
+        const float ea = at(s, FE, IV, fo), eb = at(s, FE, IV, fn[d]);
+        const float dif[NEQ] = {b.x - a.x, b.y - a.y, b.z - a.z, b.w - a.w, eb - ea};
+#pragma unroll
+        for (int n = 0; n < NEQ; ++n)
+          dfm[n] = fmaf(dif[n], hd[d], d > 0 ? dfm[n] : (n > 0 ? dv[n - 1] : 0.0f));
+      }
+    }
     // CBNS_FP64_FF: every equation's chain of the binary64 update below (the
     // inviscid flux differences along x, y, z, then minus the 4th-order viscous
     // divergence along x, y, z) in float-float arithmetic, all equations at
@@ -1249,11 +1273,7 @@ __device__ __forceinline__ void update_tiles(const SolveDev* __restrict__ solves
     for (int n = 0; n < NEQ; ++n) {
       R df;
       if constexpr (MIXED) {
-        // the viscous part above, then the inviscid flux differences
-        const long long n5 = NEQ * IV;
-        df = fma_(at(s, F0, n5, n * IV + fx) - at(s, F0, n5, n * IV + fo), idx, n > 0 ? dv[n - 1] : 0.0f);
-        df = fma_(at(s, F1, n5, n * IV + fy) - at(s, F1, n5, n * IV + fo), idy, df);
-        df = fma_(at(s, F2, n5, n * IV + fz) - at(s, F2, n5, n * IV + fo), idz, df);
+        df = dfm[n];
       } else if constexpr (FF) {
         df = dff[n];
       } else {

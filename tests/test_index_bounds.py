@@ -58,6 +58,11 @@ def test_stage_kernels_stay_in_bounds(shape):
     # face fluxes: interior offsets and the periodic neighbour (wrapped)
     lo, hi = span(lambda i, j, k: int_off(IM, JM, i, j, k), *interior, [0])
     assert lo >= 0 and hi < g["IV"]
+    # FP32-mixed face fluxes (Ff[d], 5 IV floats): equations 0-3 as float4 element
+    # f (floats 4 f .. 4 f + 3), equation 4 at float 4 IV + f
+    IV = g["IV"]
+    assert 4 * lo >= 0 and 4 * hi + 3 < 4 * IV
+    assert 4 * IV + lo >= 4 * IV and 4 * IV + hi < 5 * IV
     # k_viscous: ring points i in [-NGV, IM+NGV); derivatives reach +-2 in each direction
     ring = ((-NGV, -NGV, -NGV), (IM + NGV, JM + NGV, KM + NGV))
     for st in strides:
