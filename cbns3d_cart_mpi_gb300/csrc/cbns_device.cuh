@@ -76,6 +76,7 @@ struct PrimSet {
 template <typename R>
 struct Consts {
   R gamma, gam1, gam1_inv, gM2, Re_inv, kappa, C_T_inf, C_dt_v;
+  R hgam1;  // (gamma - 1) / 2
   R inv_dx, inv_dy, inv_dz;
   R hfx, hfy, hfz;  // 0.5 / h: the inviscid face fluxes are stored doubled
   R sum_ih, sum_ih2;  // 1/hx + 1/hy + 1/hz and 1/hx^2 + 1/hy^2 + 1/hz^2 (time step)
@@ -233,6 +234,7 @@ inline void fill_consts(SolveDev& s) {
   c.gamma = s.gamma;
   c.gam1 = s.gam1;
   c.gam1_inv = s.gam1_inv;
+  c.hgam1 = 0.5 * s.gam1;
   c.gM2 = s.gM2;
   c.Re_inv = s.Re_inv;
   c.kappa = s.kappa;
@@ -264,6 +266,7 @@ inline void fill_consts(SolveDev& s) {
   f.gamma = (float)c.gamma;
   f.gam1 = (float)c.gam1;
   f.gam1_inv = (float)c.gam1_inv;
+  f.hgam1 = (float)c.hgam1;
   f.gM2 = (float)c.gM2;
   f.Re_inv = (float)c.Re_inv;
   f.kappa = (float)c.kappa;

@@ -533,10 +533,12 @@ __device__ __forceinline__ void weno5_pair(const R (&v)[6], Weno<R>& L, Weno<R>&
   const R c13 = (R)(13.0 / 3.0);
   const R C1 = c13 * D1, C2 = c13 * D2, C3 = c13 * D3, C4 = c13 * D4;
   const R k56 = (R)(5.0 / 6.0), k13 = (R)(1.0 / 3.0);
+  // 3 g3 of both stencils from one 2 d2 (exact): 2 d2 - d3/2 and d1/2 - 2 d2
+  const R t2 = d2 + d2;
   weno5_side<R>(D1, C1, D2, C2, D3, C3, fma_((R)3, d1, -d0), d1 + d2, fma_((R)-3, d2, d3),
-                fma_(k56, d1, -k13 * d0), fma_((R)2, d2, d1), fma_((R)2, d2, (R)-0.5 * d3), L);
+                fma_(k56, d1, -k13 * d0), fma_((R)2, d2, d1), fma_((R)-0.5, d3, t2), L);
   weno5_side<R>(D4, C4, D3, C3, D2, C2, fma_((R)-3, d3, d4), d2 + d3, fma_((R)3, d2, -d1),
-                fma_(-k56, d3, k13 * d4), fma_((R)-2, d2, -d3), fma_((R)-2, d2, (R)0.5 * d1), Rt);
+                fma_(-k56, d3, k13 * d4), fma_((R)-2, d2, -d3), fma_((R)0.5, d1, -t2), Rt);
 }
 
 // r[n] = base[n] + num[n] / den[n] for ten parts (both states of a face).
@@ -635,7 +637,7 @@ __device__ __forceinline__ void face_core(const SolveDev& s, const double (&W)[6
   const R c2 = gam1 * (HH - hq2);
   const R ic = rsqrt(c2);  // 1/c; c = c^2 * (1/c)
   const R cc = c2 * ic;
-  const R K = ((R)0.5 * gam1) * ic * ic;
+  const R K = (C.hgam1 * ic) * ic;
   const R hic = (R)0.5 * ic;
   const R un = Uv[D], u1 = Uv[T1], u2 = Uv[T2];
 
