@@ -56,6 +56,23 @@ __device__ __forceinline__ ff ff_two_sum(float a, float b) {
   return ff{s, FF_ADD(FF_SUB(a, FF_SUB(s, v)), FF_SUB(b, v))};
 }
 
+// The sum of two non-negative binary32 values with its exact error: Fast2Sum
+// (Dekker) on the larger and the smaller gives the same pair as TwoSum in three
+// additions instead of six (the max and the min go to the ALU pipe, not the FMA
+// pipe).  s is formed from the operands as given, so a NaN still propagates.
+__device__ __forceinline__ ff ff_two_sum_nonneg(float a, float b) {
+  const float s = FF_ADD(a, b);
+  return ff{s, FF_SUB(fminf(a, b), FF_SUB(s, fmaxf(a, b)))};
+}
+template <bool NONNEG>
+__device__ __forceinline__ ff ff_two_sum_as(float a, float b) {
+  if constexpr (NONNEG) {
+    return ff_two_sum_nonneg(a, b);
+  } else {
+    return ff_two_sum(a, b);
+  }
+}
+
 __device__ __forceinline__ ff operator-(ff a) { return ff{-a.hi, -a.lo}; }
 
 // SloppyDWPlusDW: TwoSum of the high parts, the low parts added, renormalised.
@@ -102,35 +119,41 @@ __device__ __forceinline__ ff ff_fma(float c, ff b, ff d) {
 // that is used only as the addend of another float-float operation (whose TwoSum
 // takes any high part exactly and folds the low part into its error term) or is
 // widened to binary64.  A chain of multiply-adds renormalises once, at its end.
+// NONNEG: both the product's and the addend's high parts are known to be >= 0
+// (sums of squares and of products of them), so the TwoSum is the cheaper
+// ff_two_sum_nonneg; the result is the same.
+template <bool NONNEG = false>
 __device__ __forceinline__ ff ff_fma_acc(ff a, ff b, ff c) {
   const float p = FF_MUL(a.hi, b.hi);
   float e = fmaf(a.hi, b.hi, -p);
   e = fmaf(a.lo, b.hi, fmaf(a.hi, b.lo, e));
-  const ff s = ff_two_sum(p, c.hi);
+  const ff s = ff_two_sum_as<NONNEG>(p, c.hi);
   return ff{s.hi, FF_ADD(s.lo, FF_ADD(e, c.lo))};
 }
+template <bool NONNEG = false>
 __device__ __forceinline__ ff ff_fma_acc(float c, ff b, ff d) {
   const float p = FF_MUL(c, b.hi);
   const float e = fmaf(c, b.lo, fmaf(c, b.hi, -p));
-  const ff s = ff_two_sum(p, d.hi);
+  const ff s = ff_two_sum_as<NONNEG>(p, d.hi);
   return ff{s.hi, FF_ADD(s.lo, FF_ADD(e, d.lo))};
 }
 __device__ __forceinline__ ff ff_add_acc(ff a, ff b) {
   const ff s = ff_two_sum(a.hi, b.hi);
   return ff{s.hi, FF_ADD(s.lo, FF_ADD(a.lo, b.lo))};
 }
+// a^2 + c with c.hi >= 0 (sums of squares: the cheaper TwoSum).
 __device__ __forceinline__ ff ff_sqr_add_acc(ff a, ff c) {
   const float p = FF_MUL(a.hi, a.hi);
   const float e = fmaf(FF_ADD(a.hi, a.hi), a.lo, fmaf(a.hi, a.hi, -p));
-  const ff s = ff_two_sum(p, c.hi);
+  const ff s = ff_two_sum_nonneg(p, c.hi);
   return ff{s.hi, FF_ADD(s.lo, FF_ADD(e, c.lo))};
 }
 
-// a^2 + c.
+// a^2 + c with c.hi >= 0.
 __device__ __forceinline__ ff ff_sqr_add(ff a, ff c) {
   const float p = FF_MUL(a.hi, a.hi);
   const float e = fmaf(FF_ADD(a.hi, a.hi), a.lo, fmaf(a.hi, a.hi, -p));
-  const ff s = ff_two_sum(p, c.hi);
+  const ff s = ff_two_sum_nonneg(p, c.hi);
   return ff_fast2sum(s.hi, FF_ADD(s.lo, FF_ADD(e, c.lo)));
 }
 

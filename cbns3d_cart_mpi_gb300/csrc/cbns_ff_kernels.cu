@@ -56,12 +56,13 @@ __device__ __forceinline__ void weno5_side_ff(ff D1, ff C1, ff D2, ff C2, ff D3,
   constexpr ff eps4 = ff_const(4.0e-6);
   // the indicators and the denominator are sums of positive terms (no
   // cancellation), left unrenormalised like products
-  const ff is1 = ff_fma_acc(C1, D1, ff_sqr_add_acc(e1, eps4));
-  const ff is2 = ff_fma_acc(C2, D2, ff_sqr_add_acc(e2, eps4));
-  const ff is3 = ff_fma_acc(C3, D3, ff_sqr_add_acc(e3, eps4));
+  // (C_k = 13/3 D_k, so C_k D_k >= 0: every sum here is of non-negative terms)
+  const ff is1 = ff_fma_acc<true>(C1, D1, ff_sqr_add_acc(e1, eps4));
+  const ff is2 = ff_fma_acc<true>(C2, D2, ff_sqr_add_acc(e2, eps4));
+  const ff is3 = ff_fma_acc<true>(C3, D3, ff_sqr_add_acc(e3, eps4));
   const ff a1 = ff_sqr(is1), a2 = ff_sqr(is2), a3 = ff_sqr(is3);
   const ff p1 = a2 * a3, q2 = a1 * a3, q3 = a1 * a2;
-  out.den = ff_fma_acc(6.0f, q2, ff_fma_acc(3.0f, q3, p1));
+  out.den = ff_fma_acc<true>(6.0f, q2, ff_fma_acc<true>(3.0f, q3, p1));
   out.num = ff_fma(q2, g2s, ff_fma_acc(q3, g3s, p1 * g1));
 }
 
