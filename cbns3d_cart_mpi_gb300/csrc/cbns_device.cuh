@@ -213,19 +213,18 @@ __device__ __forceinline__ T& at(const SolveDev& s, T* base, long long n, long l
 
 // Reciprocal of a positive, normal binary64 value (the face kernel's three
 // divisions: the Roe weight, the shared WENO normalisation, the two 1/rho of
-// the Lax-Friedrichs flux).  Newton-Raphson for 1/x, y <- y + y (1 - x y), whose
-// relative error squares at each step, twice from the hardware's reciprocal
-// estimate (PTX rcp.approx.ftz.f64, which reads the operand's upper 32 bits and
-// returns about 20 good bits): within one ulp of 1/x.  A division a/x in IEEE
-// binary64 costs about 9 FP64 issue slots and 1/x about 6 (measured); this is
-// one estimate and four fused multiply-adds.
+// the Lax-Friedrichs flux).  From the hardware's reciprocal estimate y (PTX
+// rcp.approx.ftz.f64, which reads the operand's upper 32 bits and returns about
+// 20 good bits) one third-order step of the series 1/x = y / (1 - e) =
+// y (1 + e + e^2 + O(e^3)), e = 1 - x y: the estimate's relative error cubed,
+// far below an ulp, so the result is within one ulp of 1/x.  A division a/x in
+// IEEE binary64 costs about 9 FP64 issue slots and 1/x about 6 (measured); this
+// is one estimate and three fused multiply-adds.
 __device__ __forceinline__ double rcp64(double x) {
   double y;
   asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
-  double e = fma(-x, y, 1.0);
-  y = fma(y, e, y);
-  e = fma(-x, y, 1.0);
-  return fma(y, e, y);
+  const double e = fma(-x, y, 1.0);
+  return fma(y, fma(e, e, e), y);
 }
 
 // Fill cd and cf from the binary64 parameters (host side, once per solve).

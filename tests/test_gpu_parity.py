@@ -298,8 +298,8 @@ def test_fp64_ff_history_64_100_steps(golden_dir):
 
 
 def test_face_reciprocal_within_one_ulp_of_ieee_division():
-    """The face kernel's reciprocal (Newton-Raphson from the hardware estimate,
-    csrc/cbns_device.cuh rcp64) against CUDA's IEEE 1.0/x on the GPU: at most one
+    """The face kernel's reciprocal (the hardware estimate and one third-order
+    correction, csrc/cbns_device.cuh rcp64) against CUDA's IEEE 1.0/x on the GPU: at most one
     ulp apart, over values log-uniform in [1e-150, 1e150] (the range the WENO
     normalisation's product is admitted to) and uniform in [0.1, 10] (densities,
     sums of sqrt(rho))."""
