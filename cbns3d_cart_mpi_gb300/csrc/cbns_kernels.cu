@@ -949,14 +949,19 @@ __global__ void __maxnreg__(128) k_inviscid_x2(const SolveDev* __restrict__ solv
     if (i >= s.IM || j >= s.JM) continue;
     const bool pair = j + 1 < s.JM;
     const long long c0 = pad_off(s, i, j, k);
-    const long long c1 = pair ? c0 + s.nx : c0;
     const long long st = D == 0 ? 1ll : (D == 1 ? (long long)s.nx : (long long)s.nx * s.ny);
+    // y faces: row j+1's stencil is row j's shifted by one cell, so its offsets
+    // are written as row j's (c0 + k st), and the five shared cells' loads are
+    // the same expressions.  An unpaired last row's partner lane then reads the
+    // ghost row JM (inside the padding) and is not stored.
+    const long long c1 = (D == 1 || pair) ? c0 + s.nx : c0;
     const long long V = s.V;
-    const SideX2 Ls = side_x2(at(s, s.PA, V, c0 - st), at(s, s.PB, V, c0 - st), at(s, s.PA, V, c1 - st),
-                              at(s, s.PB, V, c1 - st));
-    const SideX2 Rs = side_x2(at(s, s.PA, V, c0), at(s, s.PB, V, c0), at(s, s.PA, V, c1), at(s, s.PB, V, c1));
+    const long long l1 = D == 1 ? c0 : c1 - st, r1 = D == 1 ? c0 + st : c1;
+    const SideX2 Ls = side_x2(at(s, s.PA, V, c0 - st), at(s, s.PB, V, c0 - st), at(s, s.PA, V, l1),
+                              at(s, s.PB, V, l1));
+    const SideX2 Rs = side_x2(at(s, s.PA, V, c0), at(s, s.PB, V, c0), at(s, s.PA, V, r1), at(s, s.PB, V, r1));
     auto cell = [&](int m, f2(&fc)[NEQ]) {
-      const long long o0 = c0 + (m - 3) * st, o1 = c1 + (m - 3) * st;
+      const long long o0 = c0 + (m - 3) * st, o1 = D == 1 ? c0 + (m - 2) * st : c1 + (m - 3) * st;
       const float4 a0 = at(s, s.U4, V, o0), a1 = at(s, s.U4, V, o1);
       fc[0] = lanes(a0.x, a1.x);
       fc[1] = lanes(a0.y, a1.y);

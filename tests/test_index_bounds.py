@@ -55,6 +55,12 @@ def test_stage_kernels_stay_in_bounds(shape):
     for st in strides:
         lo, hi = span(lambda i, j, k: pad_off(g, i, j, k), *interior, [m * st for m in range(-3, 3)])
         assert lo >= 0 and hi < g["V"]
+    # k_inviscid_x2<1> (binary32 y faces, rows j and j+1 of a thread): the partner row
+    # j+1 is always read, the ghost row JM when JM is odd (not stored): its stencil
+    # c + m*st, m in -3..2, and its two side cells
+    partner = ((0, 1, 0), (IM, JM + 1, KM))
+    lo, hi = span(lambda i, j, k: pad_off(g, i, j, k), *partner, [m * strides[1] for m in range(-3, 3)])
+    assert lo >= 0 and hi < g["V"]
     # face fluxes: interior offsets and the periodic neighbour (wrapped)
     lo, hi = span(lambda i, j, k: int_off(IM, JM, i, j, k), *interior, [0])
     assert lo >= 0 and hi < g["IV"]
